@@ -1,0 +1,912 @@
+// Engine context and the C ABI (include/lenia_gb300.h).
+//
+// A context is the GB300 counterpart of the reference's Sim + Program pair
+// (crates/auto-core/src/sim.rs:59-80, program.rs:102-129): it owns the device buffers of every
+// world, the kernel spectra, the work lists of each size class and the CUDA graphs that replay
+// steps.  Worlds of one grid size form a size class; each class is one column launch and one
+// row launch per step over all of its worlds, and classes run as parallel branches of the graph.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.cuh"
+#include "fft_core.cuh"
+#include "step_radix2.cuh"
+#include "step_tc.cuh"
+
+using namespace lenia;
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct SizeClass {
+    int W = 0, H = 0;
+    std::vector<int> worlds;
+    ColItem* d_col = nullptr;
+    int ncol = 0;
+    RowItem* d_row = nullptr;
+    int nrow = 0;
+    int nt_col = 0, nt_row = 0;
+    int nbuf = 1, general = 0, planes = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+struct WorldBuffers {
+    ColItem* d_col = nullptr;  // this world's column items (inspection, U fields)
+    int ncol = 0;
+    RowItem* d_row = nullptr;  // this world's row items (forward transform after writes)
+    int nrow = 0;
+    int cls = 0;
+};
+
+}  // namespace
+
+struct LeniaCtx {
+    std::string err;
+    int device = 0;
+    int path = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<LeniaWorldDesc> desc;
+    std::vector<DevWorld> hw;
+    DevWorld* d_worlds = nullptr;
+    float2* d_tw = nullptr;
+    float* d_stats = nullptr;
+    std::vector<SizeClass> classes;
+    std::vector<WorldBuffers> wb;
+    std::vector<R2World> r2;
+    std::vector<void*> allocs;
+    uint64_t tick = 0;
+    uint64_t bytes = 0;
+    int graph_steps = 64;
+    cudaGraphExec_t graph_big = nullptr, graph_one = nullptr;
+    TcPlan tc;
+};
+
+namespace {
+
+int fail(LeniaCtx* c, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    else g_create_error = buf;
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return fail(ctx, LENIA_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename T>
+int dalloc(LeniaCtx* ctx, T** p, size_t count) {
+    void* v = nullptr;
+    cudaError_t e = cudaMalloc(&v, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(ctx, LENIA_ENOMEM, "device allocation of %zu bytes failed: %s", count * sizeof(T),
+                    cudaGetErrorString(e));
+    }
+    ctx->allocs.push_back(v);
+    ctx->bytes += count * sizeof(T);
+    *p = (T*)v;
+    return 0;
+}
+
+bool supported_side(uint32_t n) {
+    uint32_t m = (n % 3 == 0) ? n / 3 : n;
+    if (m == 0 || (m & (m - 1)) != 0) return false;
+    return n >= 32 && n <= 4096;
+}
+bool is_pow2(uint32_t n) { return n && !(n & (n - 1)); }
+
+// ---------------------------------------------------------------- kernel shapes in FP64
+double lenia_core64(double q) { return (q <= 0.0 || q >= 1.0) ? 0.0 : std::exp(4.0 - 1.0 / (q * (1.0 - q))); }
+
+double shape64(const LeniaKernel& k, double r) {
+    switch (k.shape) {
+    case LENIA_SHAPE_LENIA: {
+        int B = k.nshells < 1 ? 1 : k.nshells;
+        double q = r / k.radius;
+        if (q <= 0.0 || q >= 1.0) return 0.0;
+        double bq = B * q;
+        int i = (int)std::floor(bq);
+        if (i >= B) return 0.0;
+        return (double)k.beta[i] * lenia_core64(bq - i);
+    }
+    case LENIA_SHAPE_SL_INNER: {
+        double ri = k.radius / 3.0, aa = 0.5;
+        return std::min(std::max((ri + aa - r) / (2 * aa), 0.0), 1.0);
+    }
+    case LENIA_SHAPE_SL_OUTER: {
+        double ra = k.radius, ri = k.radius / 3.0, aa = 0.5;
+        return std::min(std::max((ra + aa - r) / (2 * aa), 0.0), 1.0) * std::min(std::max((r - ri + aa) / (2 * aa), 0.0), 1.0);
+    }
+    case LENIA_SHAPE_RING: return (r >= k.ring_lo && r < k.ring_hi) ? 1.0 : 0.0;
+    }
+    return 0.0;
+}
+
+// Kernel.reach of spectral.rs:111-116 (size guard) and a bound on the support.
+int guard_reach(const LeniaKernel& k) {
+    switch (k.shape) {
+    case LENIA_SHAPE_LENIA: return (int)std::ceil(k.radius);
+    case LENIA_SHAPE_SL_INNER:
+    case LENIA_SHAPE_SL_OUTER: return (int)std::ceil(k.radius) + 2;
+    case LENIA_SHAPE_RING: return (int)std::ceil(k.ring_hi);
+    }
+    return 0;
+}
+
+// Real, even kernel spectrum in FP64, rounded to f32, with 1/(W*H) folded in:
+//   khat[kx][ky] = sum_{dx,dy} K(dx,dy) cos(2 pi kx dx / W) cos(2 pi ky dy / H) / (sum K * W * H)
+// for kx in [0, W/2], ky in [0, H/2].  The kernel is even in dx and in dy (min-image
+// placement), so this is its exact DFT; the reference computes the same spectrum with an f32
+// FFT on the GPU (spectral.rs:150-181).
+void compute_khat(const LeniaKernel& k, int W, int H, int HQ, float* out) {
+    const int reach = guard_reach(k) + 1;
+    const int nR = reach + 1;
+    std::vector<double> v((size_t)nR * nR);
+    double sum = 0.0;
+    for (int dy = 0; dy <= reach; dy++)
+        for (int dx = 0; dx <= reach; dx++) {
+            double val = shape64(k, std::sqrt((double)dx * dx + (double)dy * dy));
+            v[(size_t)dy * nR + dx] = val;
+            sum += val * (dx ? 2.0 : 1.0) * (dy ? 2.0 : 1.0);
+        }
+    std::vector<double> cw(W), ch(H);
+    for (int t = 0; t < W; t++) cw[t] = std::cos(2.0 * M_PI * t / W);
+    for (int t = 0; t < H; t++) ch[t] = std::cos(2.0 * M_PI * t / H);
+    const int KX = W / 2 + 1, KY = H / 2 + 1;
+    std::vector<double> rw((size_t)nR * KX);
+    for (int dy = 0; dy <= reach; dy++)
+        for (int kx = 0; kx < KX; kx++) {
+            double a = v[(size_t)dy * nR];
+            for (int dx = 1; dx <= reach; dx++) a += 2.0 * v[(size_t)dy * nR + dx] * cw[((size_t)kx * dx) % W];
+            rw[(size_t)dy * KX + kx] = a;
+        }
+    const double norm = 1.0 / (sum * (double)W * (double)H);
+    unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    auto work = [&](unsigned t) {
+        for (int kx = (int)t; kx < KX; kx += (int)nth)
+            for (int ky = 0; ky < KY; ky++) {
+                double a = rw[kx];
+                for (int dy = 1; dy <= reach; dy++) a += 2.0 * rw[(size_t)dy * KX + kx] * ch[((size_t)ky * dy) % H];
+                out[(size_t)kx * HQ + ky] = (float)(a * norm);
+            }
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < nth; t++) th.emplace_back(work, t);
+    work(0);
+    for (auto& t : th) t.join();
+}
+
+// f64 sum of f32 shape values over [-reach, reach]^2 as f32 (spectral.rs:75-83), for the radix-2 path.
+float kernel_sum_f32(const LeniaKernel& k) {
+    int reach;
+    switch (k.shape) {
+    case LENIA_SHAPE_LENIA: reach = (int)std::ceil(k.radius) + 1; break;
+    case LENIA_SHAPE_RING: reach = (int)std::ceil(k.ring_hi) + 1; break;
+    default: reach = (int)std::ceil(k.radius) + 2;
+    }
+    double s = 0.0;
+    for (int y = -reach; y <= reach; y++)
+        for (int x = -reach; x <= reach; x++) s += (double)(float)shape64(k, (double)std::sqrt((float)(x * x + y * y)));
+    return (float)s;
+}
+
+int validate(const LeniaWorldDesc& d, int i, int path) {
+    if (!supported_side(d.width) || !supported_side(d.height))
+        return fail(nullptr, LENIA_ESIZE, "world %d: %ux%u is not supported (sides 2^a or 3*2^a, 32..4096)", i, d.width,
+                    d.height);
+    if (path == LENIA_PATH_RADIX2 && (!is_pow2(d.width) || !is_pow2(d.height)))
+        return fail(nullptr, LENIA_ESIZE, "world %d: FFT grids must be powers of two on the radix-2 path", i);
+    if (d.channels < 1 || d.channels > LENIA_MAX_CHANNELS)
+        return fail(nullptr, LENIA_EINVAL, "world %d: channels must be 1..%d", i, LENIA_MAX_CHANNELS);
+    if (d.nkernels < 1 || d.nkernels > LENIA_MAX_KERNELS)
+        return fail(nullptr, LENIA_EINVAL, "world %d: nkernels must be 1..%d", i, LENIA_MAX_KERNELS);
+    if (d.rule < 0 || d.rule > 2) return fail(nullptr, LENIA_EINVAL, "world %d: unknown rule %d", i, d.rule);
+    if (d.rule != LENIA_RULE_LENIA && (d.channels != 1 || d.nkernels != 2))
+        return fail(nullptr, LENIA_EINVAL, "world %d: SmoothLife and MNCA need one channel and two kernels", i);
+    if (path == LENIA_PATH_RADIX2 && (d.channels != 1 || d.nkernels > 3))
+        return fail(nullptr, LENIA_EINVAL, "world %d: the radix-2 path runs one channel and 1-3 kernels", i);
+    if (!(d.dt > 0.0f) && d.rule == LENIA_RULE_LENIA) return fail(nullptr, LENIA_EINVAL, "world %d: dt must be > 0", i);
+    for (uint32_t k = 0; k < d.nkernels; k++) {
+        const LeniaKernel& kk = d.kernels[k];
+        if (kk.shape < 0 || kk.shape > 3) return fail(nullptr, LENIA_EINVAL, "world %d kernel %u: unknown shape", i, k);
+        if (kk.src < 0 || kk.src >= (int)d.channels || kk.dst < 0 || kk.dst >= (int)d.channels)
+            return fail(nullptr, LENIA_EINVAL, "world %d kernel %u: src/dst channel out of range", i, k);
+        if (kk.shape == LENIA_SHAPE_LENIA && (kk.nshells < 1 || kk.nshells > 3 || !(kk.radius > 0.0f)))
+            return fail(nullptr, LENIA_EINVAL, "world %d kernel %u: need R > 0 and 1..3 shells", i, k);
+        if (kk.shape == LENIA_SHAPE_RING && !(kk.ring_hi > kk.ring_lo && kk.ring_lo >= 0.0f))
+            return fail(nullptr, LENIA_EINVAL, "world %d kernel %u: ring needs 0 <= lo < hi", i, k);
+        if (d.rule == LENIA_RULE_LENIA && !(kk.sigma > 0.0f))
+            return fail(nullptr, LENIA_EINVAL, "world %d kernel %u: sigma must be > 0", i, k);
+        // spectral.rs:111-116: the kernel is stored once per torus position, so it must fit.
+        if (2 * guard_reach(kk) >= (int)std::min(d.width, d.height))
+            return fail(nullptr, LENIA_ESIZE, "world %d kernel %u: world smaller than its kernel", i, k);
+    }
+    return 0;
+}
+
+int world_from_ctx(const LeniaCtx* ctx, int32_t w) { return (w >= 0 && w < (int)ctx->desc.size()) ? 0 : -1; }
+
+size_t state_count(const LeniaWorldDesc& d) { return (size_t)d.channels * d.width * d.height; }
+
+// Forward row transform of one world (state -> spectrum), after its state changed.
+int refresh_spectrum(LeniaCtx* ctx, int w) {
+    if (ctx->path == LENIA_PATH_RADIX2) return 0;
+    const WorldBuffers& b = ctx->wb[w];
+    const SizeClass& cl = ctx->classes[b.cls];
+    if (!launch_row_fp32(cl.W, cl.nt_row, MODE_FORWARD, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw,
+                         ctx->stream))
+        return fail(ctx, LENIA_ECUDA, "row transform launch failed for %dx%d", cl.W, cl.H);
+    CK(cudaGetLastError());
+    return 0;
+}
+
+// Enqueue `steps` steps of every world on the context's streams (captured into graphs).
+int enqueue_steps(LeniaCtx* ctx, int steps) {
+    if (ctx->path == LENIA_PATH_RADIX2) {
+        for (int s = 0; s < steps; s++)
+            for (auto& r : ctx->r2) r2_enqueue_step(r, ctx->stream);
+        CK(cudaGetLastError());
+        return 0;
+    }
+    const bool fork = ctx->classes.size() > 1;
+    if (fork) CK(cudaEventRecord(ctx->fork, ctx->stream));
+    for (auto& cl : ctx->classes) {
+        cudaStream_t s = fork ? cl.stream : ctx->stream;
+        if (fork) CK(cudaStreamWaitEvent(s, ctx->fork, 0));
+        for (int st = 0; st < steps; st++) {
+            bool ok;
+            if (ctx->path == LENIA_PATH_FP32)
+                ok = launch_col_fp32(cl.H, cl.nt_col, cl.nbuf, ctx->d_worlds, cl.d_col, cl.ncol, ctx->d_tw, s);
+            else
+                ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_col, cl.ncol, s);
+            if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
+            ok = launch_row_fp32(cl.W, cl.nt_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+                                 ctx->d_tw, s);
+            if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
+        }
+        if (fork) {
+            CK(cudaEventRecord(cl.done, s));
+            CK(cudaStreamWaitEvent(ctx->stream, cl.done, 0));
+        }
+    }
+    CK(cudaGetLastError());
+    return 0;
+}
+
+int capture(LeniaCtx* ctx, int steps, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_steps(ctx, steps);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return fail(ctx, LENIA_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ctx, LENIA_ECUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int rebuild_graphs(LeniaCtx* ctx) {
+    if (ctx->graph_big) cudaGraphExecDestroy(ctx->graph_big);
+    if (ctx->graph_one) cudaGraphExecDestroy(ctx->graph_one);
+    ctx->graph_big = ctx->graph_one = nullptr;
+    int rc = capture(ctx, ctx->graph_steps, &ctx->graph_big);
+    if (!rc) rc = capture(ctx, 1, &ctx->graph_one);
+    return rc;
+}
+
+int setup_fused(LeniaCtx* ctx) {
+    const int nw = (int)ctx->desc.size();
+    ctx->hw.resize(nw);
+    ctx->wb.resize(nw);
+    // size classes by (W, H)
+    for (int i = 0; i < nw; i++) {
+        const LeniaWorldDesc& d = ctx->desc[i];
+        int found = -1;
+        for (size_t c = 0; c < ctx->classes.size(); c++)
+            if (ctx->classes[c].W == (int)d.width && ctx->classes[c].H == (int)d.height) found = (int)c;
+        if (found < 0) {
+            SizeClass cl;
+            cl.W = d.width;
+            cl.H = d.height;
+            ctx->classes.push_back(cl);
+            found = (int)ctx->classes.size() - 1;
+        }
+        ctx->classes[found].worlds.push_back(i);
+        ctx->wb[i].cls = found;
+    }
+    const int smem_max = max_smem_optin();
+    for (int i = 0; i < nw; i++) {
+        const LeniaWorldDesc& d = ctx->desc[i];
+        DevWorld& w = ctx->hw[i];
+        memset(&w, 0, sizeof(w));
+        w.W = d.width;
+        w.H = d.height;
+        w.C = d.channels;
+        w.K = d.nkernels;
+        w.rule = d.rule;
+        w.dt = d.dt;
+        w.HQ = d.height / 2 + 1;
+        const size_t cells = (size_t)w.W * w.H;
+        int rc;
+        if ((rc = dalloc(ctx, &w.state, cells * w.C))) return rc;
+        if ((rc = dalloc(ctx, &w.spec, spec_elems(w.W, w.H) * w.C))) return rc;
+        if (w.C == 1 && w.K == 1) w.conv = w.spec;
+        else if ((rc = dalloc(ctx, &w.conv, spec_elems(w.W, w.H) * w.K))) return rc;
+        float* kh;
+        const size_t khn = (size_t)(w.W / 2 + 1) * w.HQ;
+        if ((rc = dalloc(ctx, &kh, khn * w.K))) return rc;
+        std::vector<float> host(khn * w.K, 0.0f);
+        for (int k = 0; k < w.K; k++) {
+            const LeniaKernel& kk = d.kernels[k];
+            w.kern[k].src = kk.src;
+            w.kern[k].dst = kk.dst;
+            w.kern[k].mu = kk.mu;
+            w.kern[k].sigma = kk.sigma;
+            w.kern[k].weight = kk.weight;
+            compute_khat(kk, w.W, w.H, w.HQ, host.data() + k * khn);
+        }
+        CK(cudaMemcpy(kh, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice));
+        w.khat = kh;
+        CK(cudaMemset(w.state, 0, cells * w.C * sizeof(float)));
+        CK(cudaMemset(w.spec, 0, spec_elems(w.W, w.H) * w.C * sizeof(float2)));
+    }
+    int rc;
+    if ((rc = dalloc(ctx, &ctx->d_worlds, nw))) return rc;
+    CK(cudaMemcpy(ctx->d_worlds, ctx->hw.data(), nw * sizeof(DevWorld), cudaMemcpyHostToDevice));
+    // work lists
+    for (auto& cl : ctx->classes) {
+        std::vector<ColItem> col;
+        std::vector<RowItem> row;
+        int nbuf = 1, general = 0, planes = 0;
+        for (int wi : cl.worlds) {
+            const LeniaWorldDesc& d = ctx->desc[wi];
+            const int first_col = (int)col.size(), first_row = (int)row.size();
+            for (uint32_t c = 0; c < d.channels; c++) {
+                int nsrc = 0;
+                for (uint32_t k = 0; k < d.nkernels; k++) nsrc += d.kernels[k].src == (int)c;
+                if (nsrc == 0) continue;
+                if (nsrc > 1) nbuf = 2;
+                for (uint32_t t = 0; t < d.width / 8; t++) col.push_back(ColItem{wi, (int)c, (int)t, 0});
+            }
+            for (uint32_t r = 0; r < d.height; r += 4) row.push_back(RowItem{wi, (int)r});
+            const bool simple = d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA;
+            if (!simple) general = 1;
+            planes = std::max(planes, (int)(simple ? 0 : (d.rule == LENIA_RULE_LENIA ? d.channels : d.nkernels)));
+            WorldBuffers& b = ctx->wb[wi];
+            b.ncol = (int)col.size() - first_col;
+            b.nrow = (int)row.size() - first_row;
+            (void)first_col;
+        }
+        if ((int)col_smem_bytes(cl.H, nbuf) > smem_max) nbuf = 1;
+        if ((int)col_smem_bytes(cl.H, 1) > smem_max || (int)row_smem_bytes(cl.W, planes) > smem_max)
+            return fail(ctx, LENIA_ESIZE, "%dx%d with %d planes needs more shared memory than a CTA has", cl.W, cl.H,
+                        planes);
+        cl.nbuf = nbuf;
+        cl.general = general;
+        cl.planes = planes;
+        cl.nt_col = nt_choice(cl.H, cl.H >= 1024 ? 1 : 0);
+        cl.nt_row = nt_choice(cl.W, cl.W >= 1536 ? 1 : 0);
+        cl.ncol = (int)col.size();
+        cl.nrow = (int)row.size();
+        if ((rc = dalloc(ctx, &cl.d_col, col.size()))) return rc;
+        if ((rc = dalloc(ctx, &cl.d_row, row.size()))) return rc;
+        CK(cudaMemcpy(cl.d_col, col.data(), col.size() * sizeof(ColItem), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(cl.d_row, row.data(), row.size() * sizeof(RowItem), cudaMemcpyHostToDevice));
+        // per-world slices of the class lists
+        size_t co = 0, ro = 0;
+        for (int wi : cl.worlds) {
+            WorldBuffers& b = ctx->wb[wi];
+            b.d_col = cl.d_col + co;
+            b.d_row = cl.d_row + ro;
+            co += b.ncol;
+            ro += b.nrow;
+        }
+        CK(cudaStreamCreateWithFlags(&cl.stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&cl.done, cudaEventDisableTiming));
+        // zero-item launches only set each kernel's shared-memory limit, outside any capture
+        for (int which = 0; which < 2; which++) {
+            if (!launch_col_fp32(cl.H, nt_choice(cl.H, which), cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
+                !launch_row_fp32(cl.W, nt_choice(cl.W, which), MODE_STEP, 0, ctx->d_worlds, cl.d_row, 0, cl.planes,
+                                 ctx->d_tw, ctx->stream))
+                return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
+        }
+    }
+    return 0;
+}
+
+int setup_radix2(LeniaCtx* ctx) {
+    const int nw = (int)ctx->desc.size();
+    ctx->r2.resize(nw);
+    for (int i = 0; i < nw; i++) {
+        const LeniaWorldDesc& d = ctx->desc[i];
+        R2World& r = ctx->r2[i];
+        memset(&r, 0, sizeof(r));
+        r.w = d.width;
+        r.h = d.height;
+        r.k = d.nkernels;
+        r.rule = d.rule;
+        r.mu = d.kernels[0].mu;
+        r.sigma = d.kernels[0].sigma;
+        r.dt = d.dt;
+        const size_t n = (size_t)r.w * r.h;
+        int rc;
+        if ((rc = dalloc(ctx, &r.state, n))) return rc;
+        if ((rc = dalloc(ctx, &r.work[0], n))) return rc;
+        if ((rc = dalloc(ctx, &r.work[1], n))) return rc;
+        if ((rc = dalloc(ctx, &r.spec, n))) return rc;
+        R2Shape shapes[3];
+        float sums[3];
+        for (int k = 0; k < r.k; k++) {
+            if ((rc = dalloc(ctx, &r.kern[k], n))) return rc;
+            if ((rc = dalloc(ctx, &r.conv[k], n))) return rc;
+            const LeniaKernel& kk = d.kernels[k];
+            shapes[k] = R2Shape{kk.shape, kk.radius, kk.nshells, {kk.beta[0], kk.beta[1], kk.beta[2]}, kk.ring_lo, kk.ring_hi};
+            sums[k] = kernel_sum_f32(kk);
+        }
+        CK(cudaMemset(r.state, 0, n * sizeof(float)));
+        r2_enqueue_kernel_spectra(r, shapes, sums, ctx->stream);
+        CK(cudaGetLastError());
+    }
+    // the stats kernel reads states through a world table
+    ctx->hw.resize(nw);
+    for (int i = 0; i < nw; i++) {
+        DevWorld& w = ctx->hw[i];
+        memset(&w, 0, sizeof(w));
+        w.W = ctx->r2[i].w;
+        w.H = ctx->r2[i].h;
+        w.C = 1;
+        w.K = ctx->r2[i].k;
+        w.state = ctx->r2[i].state;
+    }
+    int rc;
+    if ((rc = dalloc(ctx, &ctx->d_worlds, nw))) return rc;
+    CK(cudaMemcpy(ctx->d_worlds, ctx->hw.data(), nw * sizeof(DevWorld), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+float* state_ptr(LeniaCtx* ctx, int w) { return ctx->path == LENIA_PATH_RADIX2 ? ctx->r2[w].state : ctx->hw[w].state; }
+
+}  // namespace
+
+extern "C" {
+
+const char* lenia_last_error(const LeniaCtx* ctx) {
+    if (!ctx) return g_create_error.c_str();
+    return ctx->err.c_str();
+}
+
+int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, LeniaCtx** out) {
+    if (!out) return fail(nullptr, LENIA_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (!worlds || nworlds < 1) return fail(nullptr, LENIA_EINVAL, "need at least one world");
+    if (path < LENIA_PATH_FP32 || path > LENIA_PATH_RADIX2) return fail(nullptr, LENIA_EINVAL, "unknown path %d", path);
+    for (int i = 0; i < nworlds; i++) {
+        int rc = validate(worlds[i], i, path);
+        if (rc) return rc;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(nullptr, LENIA_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return fail(nullptr, LENIA_ENODEV, "cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    if (prop.major != 10 || prop.minor != 3)
+        return fail(nullptr, LENIA_ENODEV, "built for sm_103a (GB300); device is sm_%d%d", prop.major, prop.minor);
+
+    LeniaCtx* ctx = new LeniaCtx();
+    ctx->device = dev;
+    ctx->path = path;
+    ctx->desc.assign(worlds, worlds + nworlds);
+    int rc = 0;
+    auto bail = [&](int code) {
+        std::string msg = ctx->err;
+        lenia_destroy(ctx);
+        g_create_error = msg;
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) != cudaSuccess) {
+        fail(ctx, LENIA_ECUDA, "stream creation failed");
+        return bail(LENIA_ECUDA);
+    }
+    // twiddles exp(-2 pi i t / TWN) from FP64
+    {
+        std::vector<float2> tw(lfft::TWN);
+        for (int t = 0; t < lfft::TWN; t++) {
+            double a = -2.0 * M_PI * (double)t / (double)lfft::TWN;
+            tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        if ((rc = dalloc(ctx, &ctx->d_tw, tw.size()))) return bail(rc);
+        if (cudaMemcpy(ctx->d_tw, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice) != cudaSuccess) {
+            fail(ctx, LENIA_ECUDA, "twiddle upload failed");
+            return bail(LENIA_ECUDA);
+        }
+    }
+    rc = (path == LENIA_PATH_RADIX2) ? setup_radix2(ctx) : setup_fused(ctx);
+    if (rc) return bail(rc);
+    if (path == LENIA_PATH_TF32 || path == LENIA_PATH_BF16X3) {
+        rc = tc_setup(ctx->tc, path, &ctx->err);
+        for (auto& cl : ctx->classes)
+            if (!rc) rc = tc_prepare_size(ctx->tc, path, cl.H, &ctx->err);
+        if (rc) return bail(rc);
+    }
+    if ((rc = dalloc(ctx, &ctx->d_stats, 3 * (size_t)nworlds))) return bail(rc);
+    if ((rc = rebuild_graphs(ctx))) return bail(rc);
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+        fail(ctx, LENIA_ECUDA, "initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
+        return bail(LENIA_ECUDA);
+    }
+    *out = ctx;
+    return 0;
+}
+
+int lenia_destroy(LeniaCtx* ctx) {
+    if (!ctx) return 0;
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->graph_big) cudaGraphExecDestroy(ctx->graph_big);
+    if (ctx->graph_one) cudaGraphExecDestroy(ctx->graph_one);
+    for (auto& cl : ctx->classes) {
+        if (cl.stream) cudaStreamDestroy(cl.stream);
+        if (cl.done) cudaEventDestroy(cl.done);
+    }
+    tc_release(ctx->tc);
+    for (void* p : ctx->allocs) cudaFree(p);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return 0;
+}
+
+int lenia_write_state(LeniaCtx* ctx, int32_t world, const float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (!host || count != state_count(ctx->desc[world]))
+        return fail(ctx, LENIA_EINVAL, "state of world %d has %zu values, got %zu", world, state_count(ctx->desc[world]),
+                    count);
+    CK(cudaMemcpyAsync(state_ptr(ctx, world), host, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    return refresh_spectrum(ctx, world);
+}
+
+int lenia_write_state_device(LeniaCtx* ctx, int32_t world, const float* dev, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (!dev || count != state_count(ctx->desc[world])) return fail(ctx, LENIA_EINVAL, "bad count for world %d", world);
+    CK(cudaMemcpyAsync(state_ptr(ctx, world), dev, count * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    return refresh_spectrum(ctx, world);
+}
+
+int lenia_read_state(LeniaCtx* ctx, int32_t world, float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (!host || count != state_count(ctx->desc[world])) return fail(ctx, LENIA_EINVAL, "bad count for world %d", world);
+    CK(cudaMemcpyAsync(host, state_ptr(ctx, world), count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (!dev || count != state_count(ctx->desc[world])) return fail(ctx, LENIA_EINVAL, "bad count for world %d", world);
+    CK(cudaMemcpyAsync(dev, state_ptr(ctx, world), count * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    return 0;
+}
+
+int lenia_step(LeniaCtx* ctx, uint32_t steps) {
+    if (!ctx) return LENIA_EINVAL;
+    uint32_t full = steps / ctx->graph_steps, rem = steps % ctx->graph_steps;
+    for (uint32_t i = 0; i < full; i++) CK(cudaGraphLaunch(ctx->graph_big, ctx->stream));
+    for (uint32_t i = 0; i < rem; i++) CK(cudaGraphLaunch(ctx->graph_one, ctx->stream));
+    ctx->tick += steps;
+    return 0;
+}
+
+int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms) {
+    if (!ctx || !ms) return LENIA_EINVAL;
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    CK(cudaEventRecord(a, ctx->stream));
+    int rc = lenia_step(ctx, steps);
+    CK(cudaEventRecord(b, ctx->stream));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(ms, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    return rc;
+}
+
+int lenia_sync(LeniaCtx* ctx) {
+    if (!ctx) return LENIA_EINVAL;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_tick(const LeniaCtx* ctx, uint64_t* tick) {
+    if (!ctx || !tick) return LENIA_EINVAL;
+    *tick = ctx->tick;
+    return 0;
+}
+
+int lenia_seed_patches(LeniaCtx* ctx, int32_t world, uint32_t seed, const int32_t* patches, int32_t npatches) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (npatches < 0 || npatches > 4096 || (npatches > 0 && !patches))
+        return fail(ctx, LENIA_EINVAL, "npatches must be 0..4096");
+    const LeniaWorldDesc& d = ctx->desc[world];
+    int4* dp = nullptr;
+    CK(cudaMallocAsync((void**)&dp, std::max(1, npatches) * sizeof(int4), ctx->stream));
+    if (npatches) CK(cudaMemcpyAsync(dp, patches, npatches * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+    for (uint32_t c = 0; c < d.channels; c++)
+        launch_seed_patches(state_ptr(ctx, world) + (size_t)c * d.width * d.height, d.width, d.height, seed + c, dp,
+                            npatches, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaFreeAsync(dp, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return refresh_spectrum(ctx, world);
+}
+
+int lenia_seed_tiles(LeniaCtx* ctx, int32_t world, uint32_t seed, const float* pattern, int32_t pw, int32_t ph,
+                     int32_t spacing) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (!pattern || pw < 1 || ph < 1 || pw != ph || spacing < pw || pw > 1024)
+        return fail(ctx, LENIA_EINVAL, "pattern must be square, 1..1024 cells, and fit in its tile");
+    const LeniaWorldDesc& d = ctx->desc[world];
+    float* dp = nullptr;
+    CK(cudaMallocAsync((void**)&dp, (size_t)pw * ph * sizeof(float), ctx->stream));
+    CK(cudaMemcpyAsync(dp, pattern, (size_t)pw * ph * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    for (uint32_t c = 0; c < d.channels; c++)
+        launch_seed_tiles(state_ptr(ctx, world) + (size_t)c * d.width * d.height, d.width, d.height, seed + c, dp, pw, ph,
+                          spacing, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaFreeAsync(dp, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return refresh_spectrum(ctx, world);
+}
+
+int lenia_cells_per_step(const LeniaCtx* ctx, uint64_t* cells) {
+    if (!ctx || !cells) return LENIA_EINVAL;
+    uint64_t n = 0;
+    for (const auto& d : ctx->desc) n += (uint64_t)d.width * d.height * d.channels;
+    *cells = n;
+    return 0;
+}
+
+int lenia_memory_bytes(const LeniaCtx* ctx, uint64_t* bytes) {
+    if (!ctx || !bytes) return LENIA_EINVAL;
+    *bytes = ctx->bytes;
+    return 0;
+}
+
+int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    const LeniaWorldDesc& d = ctx->desc[world];
+    if (kernel < 0 || kernel >= (int)d.nkernels) return fail(ctx, LENIA_EINVAL, "no kernel %d", kernel);
+    const size_t cells = (size_t)d.width * d.height;
+    if (!host || count != cells) return fail(ctx, LENIA_EINVAL, "U field has %zu values", cells);
+    if (ctx->path == LENIA_PATH_RADIX2) {
+        r2_enqueue_convolve(ctx->r2[world], ctx->stream);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(host, ctx->r2[world].conv[kernel], cells * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        return 0;
+    }
+    DevWorld& w = ctx->hw[world];
+    if (!w.u_out) {
+        int rc = dalloc(ctx, &w.u_out, cells * d.nkernels);
+        if (rc) return rc;
+        CK(cudaMemcpy(ctx->d_worlds + world, &w, sizeof(DevWorld), cudaMemcpyHostToDevice));
+    }
+    const WorldBuffers& b = ctx->wb[world];
+    const SizeClass& cl = ctx->classes[b.cls];
+    bool ok = (ctx->path == LENIA_PATH_FP32)
+                  ? launch_col_fp32(cl.H, cl.nt_col, cl.nbuf, ctx->d_worlds, b.d_col, b.ncol, ctx->d_tw, ctx->stream)
+                  : launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, b.d_col, b.ncol, ctx->stream);
+    ok = ok && launch_row_fp32(cl.W, cl.nt_row, MODE_U, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw, ctx->stream);
+    if (!ok) return fail(ctx, LENIA_ECUDA, "U launch failed");
+    CK(cudaGetLastError());
+    int rc = refresh_spectrum(ctx, world);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(host, w.u_out + (size_t)kernel * cells, cells * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel, float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (ctx->path == LENIA_PATH_RADIX2) return fail(ctx, LENIA_ESTATE, "the radix-2 path keeps no half-spectrum");
+    const LeniaWorldDesc& d = ctx->desc[world];
+    if (channel < 0 || channel >= (int)d.channels) return fail(ctx, LENIA_EINVAL, "no channel %d", channel);
+    const int W = d.width, H = d.height, KX = W / 2 + 1;
+    if (!host || count != (size_t)H * KX * 2) return fail(ctx, LENIA_EINVAL, "spectrum has %d values", H * KX * 2);
+    std::vector<float2> tiles(spec_elems(W, H));
+    CK(cudaMemcpyAsync(tiles.data(), ctx->hw[world].spec + (size_t)channel * spec_elems(W, H), tiles.size() * sizeof(float2),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int y = 0; y < H; y++)
+        for (int kx = 0; kx < W / 2; kx++) {
+            const float2 v = tiles[((size_t)(kx / 4) * H + y) * 4 + (kx % 4)];
+            float* o = host + ((size_t)y * KX + kx) * 2;
+            if (kx == 0) {
+                o[0] = v.x;
+                o[1] = 0.0f;
+                float* n = host + ((size_t)y * KX + W / 2) * 2;
+                n[0] = v.y;
+                n[1] = 0.0f;
+            } else {
+                o[0] = v.x;
+                o[1] = v.y;
+            }
+        }
+    return 0;
+}
+
+int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    if (!host_out || count != 3 * ctx->desc.size()) return fail(ctx, LENIA_EINVAL, "need 3 floats per world");
+    launch_world_stats(ctx->d_worlds, (int)ctx->desc.size(), ctx->d_stats, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host_out, ctx->d_stats, count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
+    if (!ctx || !out3 || steps == 0) return LENIA_EINVAL;
+    if (ctx->path == LENIA_PATH_RADIX2) {
+        cudaEvent_t a, b;
+        CK(cudaEventCreate(&a));
+        CK(cudaEventCreate(&b));
+        CK(cudaEventRecord(a, ctx->stream));
+        for (uint32_t s = 0; s < steps; s++) CK(cudaGraphLaunch(ctx->graph_one, ctx->stream));
+        CK(cudaEventRecord(b, ctx->stream));
+        CK(cudaEventSynchronize(b));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+        out3[0] = out3[1] = 0.0f;
+        out3[2] = ms / steps;
+        ctx->tick += steps;
+        return 0;
+    }
+    // time every class's column and row launches on the context stream, serially
+    std::vector<cudaEvent_t> ev(3);
+    for (auto& e : ev) CK(cudaEventCreate(&e));
+    double col_ms = 0, row_ms = 0;
+    for (uint32_t s = 0; s < steps; s++) {
+        for (auto& cl : ctx->classes) {
+            CK(cudaEventRecord(ev[0], ctx->stream));
+            bool ok = (ctx->path == LENIA_PATH_FP32)
+                          ? launch_col_fp32(cl.H, cl.nt_col, cl.nbuf, ctx->d_worlds, cl.d_col, cl.ncol, ctx->d_tw, ctx->stream)
+                          : launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_col, cl.ncol, ctx->stream);
+            CK(cudaEventRecord(ev[1], ctx->stream));
+            ok = ok && launch_row_fp32(cl.W, cl.nt_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+                                       ctx->d_tw, ctx->stream);
+            CK(cudaEventRecord(ev[2], ctx->stream));
+            if (!ok) return fail(ctx, LENIA_ECUDA, "profile launch failed");
+            CK(cudaEventSynchronize(ev[2]));
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, ev[0], ev[1]);
+            cudaEventElapsedTime(&b, ev[1], ev[2]);
+            col_ms += a;
+            row_ms += b;
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    out3[0] = (float)(col_ms / steps);
+    out3[1] = (float)(row_ms / steps);
+    out3[2] = (float)((col_ms + row_ms) / steps);
+    ctx->tick += steps;
+    return 0;
+}
+
+int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, uint32_t height, float* out, size_t count) {
+    if (!kernel || !out) return fail(nullptr, LENIA_EINVAL, "NULL argument");
+    LeniaWorldDesc d;
+    memset(&d, 0, sizeof(d));
+    d.width = width;
+    d.height = height;
+    d.channels = 1;
+    d.nkernels = 1;
+    d.rule = LENIA_RULE_LENIA;
+    d.dt = 1.0f;
+    d.kernels[0] = *kernel;
+    d.kernels[0].src = d.kernels[0].dst = 0;
+    if (!(d.kernels[0].sigma > 0.0f)) d.kernels[0].sigma = 1.0f;
+    int rc = validate(d, 0, LENIA_PATH_FP32);
+    if (rc) return rc;
+    const size_t need = (size_t)(width / 2 + 1) * (height / 2 + 1);
+    if (count != need) return fail(nullptr, LENIA_EINVAL, "spectrum has %zu values, got %zu", need, count);
+    compute_khat(*kernel, (int)width, (int)height, (int)(height / 2 + 1), out);
+    return 0;
+}
+
+int lenia_autotune(LeniaCtx* ctx) {
+    if (!ctx) return LENIA_EINVAL;
+    if (ctx->path == LENIA_PATH_RADIX2) return 0;
+    // Try both built thread counts for each class's column and row launches; keep the fastest.
+    // The trial steps advance the worlds, so save and restore every state.
+    std::vector<std::vector<float>> saved(ctx->desc.size());
+    for (size_t w = 0; w < ctx->desc.size(); w++) {
+        saved[w].resize(state_count(ctx->desc[w]));
+        int rc = lenia_read_state(ctx, (int)w, saved[w].data(), saved[w].size());
+        if (rc) return rc;
+    }
+    cudaEvent_t a, b;
+    CK(cudaEventCreate(&a));
+    CK(cudaEventCreate(&b));
+    const int reps = 5;
+    for (auto& cl : ctx->classes) {
+        float best_col = 1e30f, best_row = 1e30f;
+        int pick_col = cl.nt_col, pick_row = cl.nt_row;
+        for (int which = 0; which < 2; which++) {
+            const int ntc = nt_choice(cl.H, which), ntr = nt_choice(cl.W, which);
+            float t_col = 0, t_row = 0;
+            for (int r = 0; r < reps + 1; r++) {
+                CK(cudaEventRecord(a, ctx->stream));
+                bool ok = (ctx->path == LENIA_PATH_FP32)
+                              ? launch_col_fp32(cl.H, ntc, cl.nbuf, ctx->d_worlds, cl.d_col, cl.ncol, ctx->d_tw, ctx->stream)
+                              : launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_col, cl.ncol, ctx->stream);
+                CK(cudaEventRecord(b, ctx->stream));
+                CK(cudaEventSynchronize(b));
+                float ms = 0;
+                cudaEventElapsedTime(&ms, a, b);
+                if (r) t_col += ms;
+                CK(cudaEventRecord(a, ctx->stream));
+                ok = ok && launch_row_fp32(cl.W, ntr, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+                                           ctx->d_tw, ctx->stream);
+                CK(cudaEventRecord(b, ctx->stream));
+                CK(cudaEventSynchronize(b));
+                cudaEventElapsedTime(&ms, a, b);
+                if (r) t_row += ms;
+                if (!ok) {
+                    cudaGetLastError();
+                    t_col = t_row = 1e30f;
+                    break;
+                }
+            }
+            if (t_col < best_col) { best_col = t_col; pick_col = ntc; }
+            if (t_row < best_row) { best_row = t_row; pick_row = ntr; }
+        }
+        cl.nt_col = pick_col;
+        cl.nt_row = pick_row;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    for (size_t w = 0; w < ctx->desc.size(); w++) {
+        int rc = lenia_write_state(ctx, (int)w, saved[w].data(), saved[w].size());
+        if (rc) return rc;
+    }
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+}  // extern "C"

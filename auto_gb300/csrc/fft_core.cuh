@@ -1,0 +1,180 @@
+// Shared-memory Stockham FFT building blocks (mixed radix 2/3/4/8/16), FP32.
+//
+// The reference runs one radix-2 Stockham stage per dispatch over global memory
+// (crates/auto-core/src/automata/spectral.rs:14-64: src p and p+n/2, dst 2p-k and 2p-k+m,
+// twiddle exp(sign*i*pi*k/m)).  Here the same autosort formulation is generalised to radix R:
+// with L the length of the sub-transforms already done,
+//     butterfly j in [0, N/R), k = j mod L
+//     v[m]   = x[j + m*N/R] * exp(sign*2*pi*i*k*m/(L*R))     m = 0..R-1
+//     v      = DFT_R(v)
+//     y[(j-k)*R + k + m*L] = v[m]
+// which is the reference's stage for R = 2 (m there is L here).  Whole sequences live in
+// shared memory and each thread keeps its butterflies in registers across a barrier, so a
+// 4096-point transform costs 3 radix-16 passes over shared memory instead of 12 over HBM.
+//
+// Everything here is plain C++ on float2 so that the same templates compile for the host
+// unit test (tests compile this header with g++ and compare against numpy's FFT).
+#pragma once
+
+#if defined(__CUDACC__)
+#define FFT_HD __host__ __device__ __forceinline__
+#define FFT_CHD __host__ __device__
+#else
+#define FFT_HD inline
+#define FFT_CHD
+#ifndef FFT_HOST_FLOAT2
+#define FFT_HOST_FLOAT2
+struct float2 { float x, y; };
+static inline float2 make_float2(float x, float y) { float2 r; r.x = x; r.y = y; return r; }
+#endif
+#endif
+
+namespace lfft {
+
+// Twiddle table length: exp(-2*pi*i*t/TWN) for t in [0, TWN).  Every supported transform
+// length (2^a * 3^b, a <= 13, b <= 1) divides TWN.
+constexpr int TWN = 24576;
+
+// cos/sin(2*pi*t/16), t = 0..15 (exact values rounded to float); folds to a constant when t is.
+FFT_CHD constexpr float c16(int t) {
+    return t == 0 ? 1.0f : t == 1 ? 0.92387953251128674f : t == 2 ? 0.70710678118654752f
+         : t == 3 ? 0.38268343236508978f : t == 4 ? 0.0f : t == 5 ? -0.38268343236508978f
+         : t == 6 ? -0.70710678118654752f : t == 7 ? -0.92387953251128674f : t == 8 ? -1.0f
+         : t == 9 ? -0.92387953251128674f : t == 10 ? -0.70710678118654752f : t == 11 ? -0.38268343236508978f
+         : t == 12 ? 0.0f : t == 13 ? 0.38268343236508978f : t == 14 ? 0.70710678118654752f
+         : 0.92387953251128674f;
+}
+FFT_CHD constexpr float s16(int t) { return c16((t + 12) & 15); }  // sin(x) = cos(x - pi/2)
+constexpr float SQRT3_2 = 0.86602540378443865f;
+
+FFT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+FFT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+FFT_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+FFT_HD float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); } // a*conj(b)
+FFT_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+FFT_HD float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+// multiply by exp(sign * i * pi/2): -i for the forward transform, +i for the inverse
+template <bool INV> FFT_HD float2 rot90(float2 z) { return INV ? make_float2(-z.y, z.x) : make_float2(z.y, -z.x); }
+
+// exp(sign*2*pi*i*j/R) for compile-time R in {2,4,8,16} and j, via the 16-entry table
+template <int R, bool INV> FFT_HD float2 wR(int j) {
+    int t = (j * (16 / R)) & 15;
+    return make_float2(c16(t), INV ? s16(t) : -s16(t));
+}
+
+// ------------------------------------------------------------------ register DFTs
+template <int R, bool INV> struct Dft;
+
+template <bool INV> struct Dft<2, INV> {
+    FFT_HD static void run(float2* v) {
+        float2 a = v[0], b = v[1];
+        v[0] = cadd(a, b); v[1] = csub(a, b);
+    }
+};
+
+template <bool INV> struct Dft<3, INV> {
+    FFT_HD static void run(float2* v) {
+        float2 s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+        float2 t = make_float2(v[0].x - 0.5f * s.x, v[0].y - 0.5f * s.y);
+        // sign*i*(sqrt(3)/2)*d
+        float2 r = INV ? make_float2(-SQRT3_2 * d.y, SQRT3_2 * d.x) : make_float2(SQRT3_2 * d.y, -SQRT3_2 * d.x);
+        v[0] = cadd(v[0], s);
+        v[1] = cadd(t, r);
+        v[2] = csub(t, r);
+    }
+};
+
+template <bool INV> struct Dft<4, INV> {
+    FFT_HD static void run(float2* v) {
+        float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        float2 t2 = cadd(v[1], v[3]), t3 = rot90<INV>(csub(v[1], v[3]));
+        v[0] = cadd(t0, t2); v[2] = csub(t0, t2);
+        v[1] = cadd(t1, t3); v[3] = csub(t1, t3);
+    }
+};
+
+// R = R1 * R2 with m = R2*m1 + m2 and q = q1 + R1*q2:
+//   u[m2][q1] = DFT_R1 over m1 of v[R2*m1 + m2];  u *= w_R^(m2*q1);  y[q1 + R1*q2] = DFT_R2 over m2.
+template <int R1, int R2, bool INV> FFT_HD void dft_split(float2* v) {
+    constexpr int R = R1 * R2;
+    float2 u[R];
+#pragma unroll
+    for (int m2 = 0; m2 < R2; m2++) {
+        float2 a[R1];
+#pragma unroll
+        for (int m1 = 0; m1 < R1; m1++) a[m1] = v[R2 * m1 + m2];
+        Dft<R1, INV>::run(a);
+#pragma unroll
+        for (int q1 = 0; q1 < R1; q1++) u[m2 * R1 + q1] = (m2 * q1 == 0) ? a[q1] : cmul(a[q1], wR<R, INV>(m2 * q1));
+    }
+#pragma unroll
+    for (int q1 = 0; q1 < R1; q1++) {
+        float2 b[R2];
+#pragma unroll
+        for (int m2 = 0; m2 < R2; m2++) b[m2] = u[m2 * R1 + q1];
+        Dft<R2, INV>::run(b);
+#pragma unroll
+        for (int q2 = 0; q2 < R2; q2++) v[q1 + R1 * q2] = b[q2];
+    }
+}
+
+template <bool INV> struct Dft<8, INV> { FFT_HD static void run(float2* v) { dft_split<4, 2, INV>(v); } };
+template <bool INV> struct Dft<16, INV> { FFT_HD static void run(float2* v) { dft_split<4, 4, INV>(v); } };
+
+// ------------------------------------------------------------------ radix plans
+// N = 2^a * 3^b (b <= 1): radix 3 first, then 16s, then the remaining 2, 4 or 8.
+FFT_CHD constexpr int plan_len(int n) {
+    int c = 0;
+    if (n % 3 == 0) { c++; n /= 3; }
+    while (n % 16 == 0 && n >= 16) { c++; n /= 16; }
+    if (n > 1) c++;
+    return c;
+}
+FFT_CHD constexpr int plan_radix(int n, int i) {
+    int c = 0;
+    if (n % 3 == 0) { if (c == i) return 3; c++; n /= 3; }
+    while (n % 16 == 0 && n >= 16) { if (c == i) return 16; c++; n /= 16; }
+    return n;
+}
+FFT_CHD constexpr int plan_L(int n, int i) {  // product of the radices before stage i
+    int l = 1;
+    for (int s = 0; s < i; s++) l *= plan_radix(n, s);
+    return l;
+}
+FFT_CHD constexpr bool size_ok(int n) {
+    if (n % 3 == 0) n /= 3;
+    return n >= 2 && (n & (n - 1)) == 0 && n <= 8192;
+}
+
+// padded shared-memory index: one float2 of padding per 16 keeps radix-16 stores conflict-free
+FFT_HD int pad(int i) { return i + (i >> 4); }
+// stride between sequences held in one shared buffer: padded length, +4 so that loads of
+// 4 interleaved columns fall into different banks
+FFT_CHD constexpr int seq_stride(int n) { return n + n / 16 + 4; }
+
+// Load butterfly j of a stage (with its inter-stage twiddle) from one sequence.
+template <int N, int R, int L, bool INV>
+FFT_HD void stage_load(const float2* seq, int j, float2* v, const float2* tw) {
+    constexpr int NB = N / R;
+    const int k = j % L;
+#pragma unroll
+    for (int m = 0; m < R; m++) v[m] = seq[pad(j + m * NB)];
+    if (L > 1) {
+#pragma unroll
+        for (int m = 1; m < R; m++) {
+            float2 w = tw[(k * m) * (TWN / (L * R))];
+            v[m] = INV ? cmulc(v[m], w) : cmul(v[m], w);
+        }
+    }
+    Dft<R, INV>::run(v);
+}
+
+template <int N, int R, int L>
+FFT_HD void stage_store(float2* seq, int j, const float2* v) {
+    const int k = j % L;
+    const int base = (j - k) * R + k;
+#pragma unroll
+    for (int m = 0; m < R; m++) seq[pad(base + m * L)] = v[m];
+}
+
+}  // namespace lfft

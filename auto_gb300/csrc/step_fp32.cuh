@@ -1,0 +1,341 @@
+// Fused FP32 Lenia step on the CUDA cores: two launches per step.
+//
+// The reference's step is 4*log2(n)+5 full-grid dispatches (spectral.rs:199-264): load, log2 W
+// x-stages, log2 H y-stages, spectrum copy, and per kernel multiply, inverse y, inverse x,
+// convolved, then update.  Here the same mathematics is regrouped so that each grid sweep
+// does as much as it can in shared memory:
+//
+//   column pass (per world, channel, tile of 4 spectrum columns):
+//       forward FFT along y  ->  x khat_k (real, even; includes 1/(W*H))  ->  inverse FFT along y
+//   row pass (per world, block of 4 rows):
+//       inverse real FFT along x of U_k  ->  growth, dt, clamp (spectral.rs:337-345)  ->
+//       write state  ->  forward real FFT along x of the new rows  ->  write spectrum
+//
+// so one step reads and writes the half-spectrum twice and the state once.  Two real rows
+// share one complex FFT (z = a + i b), and the real DC and Nyquist columns share spectrum
+// column 0, so the half-spectrum takes exactly W*H*4 bytes per channel.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "engine.cuh"
+#include "fft_core.cuh"
+
+namespace lenia {
+using namespace lfft;
+
+// S sequences of length N in shared memory (stride seq_stride(N)), transformed in place by NT
+// threads.  Starts after the caller's barrier; ends with a barrier.
+template <int N, int S, int NT, bool INV, int I = 0>
+__device__ __forceinline__ void fft_seqs(float2* buf, const float2* __restrict__ tw) {
+    if constexpr (I < plan_len(N)) {
+        constexpr int R = plan_radix(N, I);
+        constexpr int L = plan_L(N, I);
+        constexpr int NB = N / R;
+        constexpr int TOT = NB * S;
+        constexpr int PER = (TOT + NT - 1) / NT;
+        constexpr int SEQ = seq_stride(N);
+        float2 v[PER][R];
+#pragma unroll
+        for (int p = 0; p < PER; p++) {
+            const int b = threadIdx.x + p * NT;
+            if ((TOT % NT) == 0 || b < TOT) {
+                const int s = b / NB, j = b - s * NB;
+                stage_load<N, R, L, INV>(buf + s * SEQ, j, v[p], tw);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int p = 0; p < PER; p++) {
+            const int b = threadIdx.x + p * NT;
+            if ((TOT % NT) == 0 || b < TOT) {
+                const int s = b / NB, j = b - s * NB;
+                stage_store<N, R, L>(buf + s * SEQ, j, v[p]);
+            }
+        }
+        __syncthreads();
+        fft_seqs<N, S, NT, INV, I + 1>(buf, tw);
+    }
+}
+
+__device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+
+// Gaussian growth mapped to [-1, 1] (spectral.rs:341-344).
+__device__ __forceinline__ float growth(float u, float mu, float sigma) {
+    float d = (u - mu) / sigma;
+    return 2.0f * expf(-0.5f * d * d) - 1.0f;
+}
+
+// SmoothLife update (spectral.rs:396-407).
+__device__ __forceinline__ float smoothlife_update(float s, float c0, float c1) {
+    const float B1 = 0.278f, B2 = 0.365f, D1 = 0.267f, D2 = 0.445f, AN = 0.028f, AM = 0.147f, DT = 0.1f;
+    float m = 1.0f / (1.0f + expf((0.5f - c0) * 4.0f / AM));
+    float lo = B1 * (1.0f - m) + D1 * m, hi = B2 * (1.0f - m) + D2 * m;
+    float target = (1.0f / (1.0f + expf((lo - c1) * 4.0f / AN))) * (1.0f - 1.0f / (1.0f + expf((hi - c1) * 4.0f / AN)));
+    return clamp01(s + DT * (2.0f * target - 1.0f));
+}
+
+// MNCA update (spectral.rs:461-472).
+__device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
+    float o = s;
+    if (c0 >= 0.210f && c0 <= 0.220f) o = 1.0f;
+    if (c0 >= 0.350f && c0 <= 0.500f) o = 0.0f;
+    if (c0 >= 0.750f && c0 <= 0.850f) o = 0.0f;
+    if (c0 >= 0.120f && c0 <= 0.150f) o = 0.0f;
+    if (c1 >= 0.100f && c1 <= 0.280f) o = 0.0f;
+    if (c1 >= 0.430f && c1 <= 0.550f) o = 1.0f;
+    return o;
+}
+
+// ---------------------------------------------------------------------------- row pass
+
+// Half-spectra of rows r0..r0+3 (tile layout) -> two packed complex sequences
+// Z_p = A + iB with A = row r0+2p, B = row r0+2p+1, using Hermitian symmetry for k > W/2.
+template <int W, int NT>
+__device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __restrict__ sp, int H, int r0) {
+    constexpr int SEQ = seq_stride(W);
+    for (int e = threadIdx.x; e < (W / 8) * 8; e += NT) {
+        const int t = e >> 3, p = (e >> 2) & 1, c = e & 3, kx = 4 * t + c;
+        const float2* src = sp + ((size_t)t * H + r0 + 2 * p) * 4 + c;
+        const float2 A = src[0], B = src[4];
+        float2* z = Z + p * SEQ;
+        if (kx == 0) {
+            z[pad(0)] = make_float2(A.x, B.x);
+            z[pad(W / 2)] = make_float2(A.y, B.y);
+        } else {
+            z[pad(kx)] = make_float2(A.x - B.y, A.y + B.x);
+            z[pad(W - kx)] = make_float2(A.x + B.y, B.x - A.y);
+        }
+    }
+}
+
+// Two packed complex spectra Z_p = FFT(a + ib) -> half-spectra of rows r0+2p (A) and r0+2p+1 (B).
+template <int W, int NT>
+__device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __restrict__ sp, int H, int r0) {
+    constexpr int SEQ = seq_stride(W);
+    for (int e = threadIdx.x; e < (W / 8) * 8; e += NT) {
+        const int t = e >> 3, p = (e >> 2) & 1, c = e & 3, kx = 4 * t + c;
+        const float2* z = Z + p * SEQ;
+        float2 A, B;
+        if (kx == 0) {
+            const float2 z0 = z[pad(0)], zn = z[pad(W / 2)];
+            A = make_float2(z0.x, zn.x);
+            B = make_float2(z0.y, zn.y);
+        } else {
+            const float2 a = z[pad(kx)], b = z[pad(W - kx)];
+            A = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
+            B = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+        }
+        float2* dst = sp + ((size_t)t * H + r0 + 2 * p) * 4 + c;
+        dst[0] = A;
+        dst[4] = B;
+    }
+}
+
+template <int W, int NT>
+__global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items,
+                                                int mode, int general, const float2* __restrict__ tw) {
+    extern __shared__ float4 smem_raw[];
+    constexpr int SEQ = seq_stride(W);
+    float2* Z = reinterpret_cast<float2*>(smem_raw);
+    float* acc = reinterpret_cast<float*>(Z + 2 * SEQ);  // [planes][4][W]
+    const RowItem it = items[blockIdx.x];
+    const DevWorld& wd = worlds[it.world];
+    const int H = wd.H, C = wd.C, K = wd.K, r0 = it.row0;
+    const size_t plane = (size_t)W * H, cplane = (size_t)(W / 2) * H;
+
+    if (mode == MODE_FORWARD) {
+        for (int d = 0; d < C; d++) {
+            const float* st = wd.state + d * plane + (size_t)r0 * W;
+            for (int e = threadIdx.x; e < 2 * W; e += NT) {
+                const int p = e / W, x = e - p * W;
+                Z[p * SEQ + pad(x)] = make_float2(st[(2 * p) * W + x], st[(2 * p + 1) * W + x]);
+            }
+            __syncthreads();
+            fft_seqs<W, 2, NT, false>(Z, tw);
+            store_rows_spectrum<W, NT>(Z, wd.spec + d * cplane, H, r0);
+            __syncthreads();
+        }
+        return;
+    }
+
+    if (mode == MODE_U) {
+        for (int k = 0; k < K; k++) {
+            load_rows_spectrum<W, NT>(Z, wd.conv + k * cplane, H, r0);
+            __syncthreads();
+            fft_seqs<W, 2, NT, true>(Z, tw);
+            float* u = wd.u_out + k * plane + (size_t)r0 * W;
+            for (int e = threadIdx.x; e < 2 * W; e += NT) {
+                const int p = e / W, x = e - p * W;
+                const float2 z = Z[p * SEQ + pad(x)];
+                u[(2 * p) * W + x] = z.x;
+                u[(2 * p + 1) * W + x] = z.y;
+            }
+            __syncthreads();
+        }
+        return;
+    }
+
+    if (!general) {
+        // one channel, one kernel, Lenia growth: U -> state -> spectrum without a staging buffer
+        const DevKernel kp = wd.kern[0];
+        const float dtw = wd.dt * kp.weight;
+        load_rows_spectrum<W, NT>(Z, wd.conv, H, r0);
+        __syncthreads();
+        fft_seqs<W, 2, NT, true>(Z, tw);
+        float* st = wd.state + (size_t)r0 * W;
+        for (int e = threadIdx.x; e < 2 * W; e += NT) {
+            const int p = e / W, x = e - p * W;
+            const float2 u = Z[p * SEQ + pad(x)];
+            float* s0 = st + (2 * p) * W + x;
+            float* s1 = s0 + W;
+            const float n0 = clamp01(*s0 + dtw * growth(u.x, kp.mu, kp.sigma));
+            const float n1 = clamp01(*s1 + dtw * growth(u.y, kp.mu, kp.sigma));
+            *s0 = n0;
+            *s1 = n1;
+            Z[p * SEQ + pad(x)] = make_float2(n0, n1);
+        }
+        __syncthreads();
+        fft_seqs<W, 2, NT, false>(Z, tw);
+        store_rows_spectrum<W, NT>(Z, wd.spec, H, r0);
+        return;
+    }
+
+    // General: several channels and/or kernels, or a rule that needs every U at once.
+    const int rule = wd.rule;
+    const int planes = (rule == LENIA_RULE_LENIA) ? C : K;
+    for (int e = threadIdx.x; e < planes * 4 * W; e += NT) acc[e] = 0.0f;
+    for (int k = 0; k < K; k++) {
+        const DevKernel kp = wd.kern[k];
+        load_rows_spectrum<W, NT>(Z, wd.conv + k * cplane, H, r0);
+        __syncthreads();
+        fft_seqs<W, 2, NT, true>(Z, tw);
+        for (int e = threadIdx.x; e < 2 * W; e += NT) {
+            const int p = e / W, x = e - p * W;
+            const float2 u = Z[p * SEQ + pad(x)];
+            if (rule == LENIA_RULE_LENIA) {
+                float* a = acc + (size_t)kp.dst * 4 * W;
+                a[(2 * p) * W + x] += kp.weight * growth(u.x, kp.mu, kp.sigma);
+                a[(2 * p + 1) * W + x] += kp.weight * growth(u.y, kp.mu, kp.sigma);
+            } else {
+                float* a = acc + (size_t)k * 4 * W;
+                a[(2 * p) * W + x] = u.x;
+                a[(2 * p + 1) * W + x] = u.y;
+            }
+        }
+        __syncthreads();
+    }
+    for (int d = 0; d < C; d++) {
+        float* st = wd.state + d * plane + (size_t)r0 * W;
+        for (int e = threadIdx.x; e < 2 * W; e += NT) {
+            const int p = e / W, x = e - p * W;
+            float n[2];
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int r = 2 * p + q;
+                const float s = st[r * W + x];
+                if (rule == LENIA_RULE_LENIA) n[q] = clamp01(s + wd.dt * acc[(size_t)d * 4 * W + r * W + x]);
+                else if (rule == LENIA_RULE_SMOOTHLIFE) n[q] = smoothlife_update(s, acc[r * W + x], acc[4 * W + r * W + x]);
+                else n[q] = mnca_update(s, acc[r * W + x], acc[4 * W + r * W + x]);
+                st[r * W + x] = n[q];
+            }
+            Z[p * SEQ + pad(x)] = make_float2(n[0], n[1]);
+        }
+        __syncthreads();
+        fft_seqs<W, 2, NT, false>(Z, tw);
+        store_rows_spectrum<W, NT>(Z, wd.spec + d * cplane, H, r0);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------- column pass
+
+// X (4 sequences of length H, forward spectrum of tile `t`) times khat -> T.  Column 0 of
+// tile 0 packs the DC column (real part) and the Nyquist column (imaginary part): both are
+// real sequences, so with Z = FFT_y(packed), Z' = Z*(K0+KN)/2 + conj(Z[-ky])*(K0-KN)/2.
+template <int H, int NT>
+__device__ __forceinline__ void multiply_khat(const float2* X, float2* T, const float* __restrict__ kh, int HQ,
+                                              int W, int t) {
+    constexpr int SEQ = seq_stride(H);
+    for (int e = threadIdx.x; e < 4 * H; e += NT) {
+        const int col = e / H, ky = e - col * H;
+        if (t == 0 && col == 0) continue;
+        const int kx = 4 * t + col;
+        const float kv = kh[(size_t)kx * HQ + (ky <= H / 2 ? ky : H - ky)];
+        T[col * SEQ + pad(ky)] = cscale(X[col * SEQ + pad(ky)], kv);
+    }
+    if (t == 0) {
+        for (int ky = threadIdx.x; ky <= H / 2; ky += NT) {
+            const float K0 = kh[ky], KN = kh[(size_t)(W / 2) * HQ + ky];
+            const float a = 0.5f * (K0 + KN), b = 0.5f * (K0 - KN);
+            const int km = (H - ky) % H;
+            const float2 z = X[pad(ky)], zm = X[pad(km)];
+            T[pad(ky)] = make_float2(z.x * a + zm.x * b, z.y * a - zm.y * b);
+            if (km != ky) T[pad(km)] = make_float2(zm.x * a + z.x * b, zm.y * a - z.y * b);
+        }
+    }
+}
+
+template <int H, int NT>
+__device__ __forceinline__ void load_tile(float2* X, const float2* __restrict__ src) {
+    constexpr int SEQ = seq_stride(H);
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    for (int e = threadIdx.x; e < 2 * H; e += NT) {
+        const int y = e >> 1, h = e & 1;
+        const float4 v = s4[e];
+        X[(2 * h) * SEQ + pad(y)] = make_float2(v.x, v.y);
+        X[(2 * h + 1) * SEQ + pad(y)] = make_float2(v.z, v.w);
+    }
+}
+
+template <int H, int NT>
+__device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__ dst) {
+    constexpr int SEQ = seq_stride(H);
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    for (int e = threadIdx.x; e < 2 * H; e += NT) {
+        const int y = e >> 1, h = e & 1;
+        const float2 a = X[(2 * h) * SEQ + pad(y)], b = X[(2 * h + 1) * SEQ + pad(y)];
+        d4[e] = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+template <int H, int NT>
+__global__ void __launch_bounds__(NT, 1) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
+                                                int nbuf, const float2* __restrict__ tw) {
+    extern __shared__ float4 smem_raw[];
+    constexpr int SEQ = seq_stride(H);
+    float2* X = reinterpret_cast<float2*>(smem_raw);
+    float2* Y = X + 4 * SEQ;
+    const ColItem it = items[blockIdx.x];
+    const DevWorld& wd = worlds[it.world];
+    const int W = wd.W, c = it.chan, t = it.tile, K = wd.K, HQ = wd.HQ;
+    const size_t cplane = (size_t)(W / 2) * H;
+    const float2* src = wd.spec + c * cplane + (size_t)t * H * 4;
+    int nsrc = 0;
+    for (int k = 0; k < K; k++) nsrc += (wd.kern[k].src == c);
+    if (nsrc == 0) return;
+    const bool reload = (nsrc > 1 && nbuf < 2);
+    bool have = false;
+    for (int k = 0; k < K; k++) {
+        if (wd.kern[k].src != c) continue;
+        if (!have || reload) {
+            load_tile<H, NT>(X, src);
+            __syncthreads();
+            fft_seqs<H, 4, NT, false>(X, tw);
+            have = true;
+        }
+        float2* T = (nsrc > 1 && !reload) ? Y : X;
+        const float* kh = wd.khat + (size_t)k * (W / 2 + 1) * HQ;
+        multiply_khat<H, NT>(X, T, kh, HQ, W, t);
+        __syncthreads();
+        fft_seqs<H, 4, NT, true>(T, tw);
+        store_tile<H, NT>(T, wd.conv + k * cplane + (size_t)t * H * 4);
+        __syncthreads();
+    }
+}
+
+// Sizes built, and the two thread counts each size is built with.
+#define LENIA_SIZES(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(1536) X(2048) X(3072) X(4096)
+template <int N> constexpr int nt_lo() { return N <= 128 ? 64 : (N <= 512 ? 128 : 256); }
+template <int N> constexpr int nt_hi() { return N <= 128 ? 128 : (N <= 512 ? 256 : 512); }
+
+}  // namespace lenia

@@ -1,0 +1,154 @@
+"""Sim: the engine context behind the reference's ``Sim`` interface (crates/auto-core/src/sim.rs).
+
+``Sim(world_or_worlds, seed)`` mirrors ``Sim::new(&gpu, program, seed)`` (sim.rs:202-282),
+``step(steps)`` mirrors ``Sim::step`` (sim.rs:297-309), ``read_field("state")`` and
+``write_field("state", bytes)`` mirror sim.rs:560-595.  Several worlds may share one Sim; they
+advance together in one set of launches.
+"""
+import ctypes
+from typing import List, Sequence, Union
+
+import numpy as np
+
+from . import _lib
+from ._lib import check, fptr
+from .program import World
+
+
+class Sim:
+    def __init__(self, worlds: Union[World, Sequence[World]], seed: int = 1, path: Union[str, int] = "fp32"):
+        self.worlds: List[World] = [worlds] if isinstance(worlds, World) else list(worlds)
+        if not self.worlds:
+            raise ValueError("need at least one world")
+        self.path = _lib.PATHS[path] if isinstance(path, str) else int(path)
+        self.seed = seed
+        L = _lib.load()
+        descs = (_lib.LeniaWorldDesc * len(self.worlds))(*[w.to_desc() for w in self.worlds])
+        ctx = ctypes.c_void_p()
+        check(L.lenia_create(descs, len(self.worlds), self.path, ctypes.byref(ctx)), None)
+        self._ctx = ctx
+        self._L = L
+        self.run_init()
+
+    # ------------------------------------------------------------------ lifecycle
+    def close(self):
+        if getattr(self, "_ctx", None):
+            self._L.lenia_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        return check(rc, self._ctx)
+
+    # ------------------------------------------------------------------ the reference API
+    def run_init(self):
+        """Seed every world from its program's seed spec (sim.rs:286-294)."""
+        for i, w in enumerate(self.worlds):
+            s = w.seed
+            if s.kind == "patches":
+                self.seed_patches(i, self.seed, s.patches)
+            elif s.kind == "tiles" and s.pattern is not None:
+                self.seed_tiles(i, self.seed, s.pattern, s.spacing)
+
+    @property
+    def tick(self) -> int:
+        t = ctypes.c_uint64()
+        self._check(self._L.lenia_tick(self._ctx, ctypes.byref(t)))
+        return int(t.value)
+
+    def step(self, steps: int) -> int:
+        """Advance every world by ``steps``; returns generations advanced (asynchronous)."""
+        self._check(self._L.lenia_step(self._ctx, int(steps)))
+        return int(steps)
+
+    def step_timed(self, steps: int) -> float:
+        """Advance and block; device milliseconds of the steps (CUDA events on the engine stream)."""
+        ms = ctypes.c_float()
+        self._check(self._L.lenia_step_timed(self._ctx, int(steps), ctypes.byref(ms)))
+        return float(ms.value)
+
+    def wait(self):
+        self._check(self._L.lenia_sync(self._ctx))
+
+    def read_field(self, name: str, world: int = 0) -> bytes:
+        if name != "state":
+            raise KeyError("known field: state")
+        return self.read_state(world).tobytes()
+
+    def write_field(self, name: str, data: bytes, world: int = 0):
+        if name != "state":
+            raise KeyError("known field: state")
+        w = self.worlds[world]
+        self.write_state(world, np.frombuffer(data, np.float32).reshape(w.channels, w.height, w.width))
+
+    # ------------------------------------------------------------------ arrays
+    def read_state(self, world: int = 0) -> np.ndarray:
+        w = self.worlds[world]
+        out = np.empty((w.channels, w.height, w.width), np.float32)
+        self._check(self._L.lenia_read_state(self._ctx, world, fptr(out), out.size))
+        return out
+
+    def write_state(self, world: int, state: np.ndarray):
+        w = self.worlds[world]
+        a = np.ascontiguousarray(state, np.float32).reshape(w.channels, w.height, w.width)
+        self._check(self._L.lenia_write_state(self._ctx, world, fptr(a), a.size))
+        self.wait()
+
+    def seed_patches(self, world: int, seed: int, patches):
+        p = np.ascontiguousarray(np.asarray(patches, np.int32).reshape(-1, 4))
+        self._check(self._L.lenia_seed_patches(self._ctx, world, seed,
+                                               p.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), len(p)))
+
+    def seed_tiles(self, world: int, seed: int, pattern, spacing: int = 64):
+        pat = np.ascontiguousarray(pattern, np.float32)
+        self._check(self._L.lenia_seed_tiles(self._ctx, world, seed, fptr(pat), pat.shape[1], pat.shape[0], spacing))
+
+    def u_field(self, world: int = 0, kernel: int = 0) -> np.ndarray:
+        w = self.worlds[world]
+        out = np.empty((w.height, w.width), np.float32)
+        self._check(self._L.lenia_read_field_u(self._ctx, world, kernel, fptr(out), out.size))
+        return out
+
+    def spectrum(self, world: int = 0, channel: int = 0) -> np.ndarray:
+        w = self.worlds[world]
+        out = np.empty((w.height, w.width // 2 + 1, 2), np.float32)
+        self._check(self._L.lenia_read_spectrum(self._ctx, world, channel, fptr(out), out.size))
+        return out[..., 0] + 1j * out[..., 1]
+
+    def stats(self) -> np.ndarray:
+        """(mass, centroid x, centroid y) per world."""
+        out = np.empty((len(self.worlds), 3), np.float32)
+        self._check(self._L.lenia_world_stats(self._ctx, fptr(out), out.size))
+        return out
+
+    @property
+    def cells_per_step(self) -> int:
+        v = ctypes.c_uint64()
+        self._check(self._L.lenia_cells_per_step(self._ctx, ctypes.byref(v)))
+        return int(v.value)
+
+    @property
+    def memory_bytes(self) -> int:
+        v = ctypes.c_uint64()
+        self._check(self._L.lenia_memory_bytes(self._ctx, ctypes.byref(v)))
+        return int(v.value)
+
+    def autotune(self):
+        self._check(self._L.lenia_autotune(self._ctx))
+
+    def profile(self, steps: int = 10):
+        """Event-timed (column ms, row ms, step ms) per step."""
+        out = np.zeros(3, np.float32)
+        self._check(self._L.lenia_profile_step(self._ctx, int(steps), fptr(out)))
+        return out

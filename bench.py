@@ -1,0 +1,365 @@
+"""Lenia cell-updates/s on one GB300 (and N independent replicas under torchrun).
+
+One bench step = one ``lenia_step(ctx, G)`` call: G generations (default 64, one CUDA-graph replay)
+of every world in the workload.  The default workload is the single 4096x4096 world with a
+three-shell R=52 kernel; ``--config batched`` runs the 384 uneven worlds in one context.
+
+Printed JSON (one line, rank 0):
+  value   cell-updates/s with the state resident in HBM, from CUDA events on the engine stream
+          around the K timed bench steps, max over ranks
+  e2e     the same metric through the public C ABI with host buffers: every bench step writes
+          each world's state from pinned host memory, runs G generations and reads the state back
+  roofline, cpu_baseline, clocks, gpu_launches: see the design doc
+
+``--impl reference`` times the reference's step as restated on the CPU (the reference itself is
+Rust + WGSL on Vulkan and cannot run here) on all host cores, on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Lenia cell-updates/s on 1 GB300, batched TC vs plain FP32, at ≤1e-4 vs FP64"
+UNIT = "cell-updates/s"
+ALG_BYTES_PER_UPDATE = 12.0  # state read + write (8 B) + one f32 complex half-spectrum of the kernel (4 B)
+PUBLISHED_REF = {"lenia_4096x4096_R13": 3.174e8, "hardware": "AMD RX 7900 XT (wgpu/Vulkan)",
+                 "source": "results/gpu.jsonl:81"}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default="single_4096", choices=["single_4096", "batched", "single_256", "multichannel"])
+    p.add_argument("--path", default="fp32", choices=["fp32", "tf32", "bf16x3", "radix2"])
+    p.add_argument("--gens", type=int, default=64, help="generations per bench step")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--autotune", action="store_true")
+    return p.parse_args()
+
+
+# ----------------------------------------------------------------------------- distributed plumbing
+
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.torch = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            self.torch = torch
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl")
+
+    def barrier(self):
+        if self.world > 1:
+            self.torch.distributed.barrier()
+
+    def max(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64, device="cuda")
+        self.torch.distributed.all_reduce(t, op=self.torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.torch.distributed.destroy_process_group()
+
+
+def device_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except Exception:
+        pass
+
+
+# ----------------------------------------------------------------------------- clocks
+
+REASONS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
+
+class Clocks:
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(REASONS, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------- workloads
+
+def workload(name):
+    import auto_gb300 as ag
+    from auto_gb300 import configs
+    if name == "single_4096":
+        w = configs.single_4096()
+        return [w], [configs.SEED_4096], {"workload": "single 4096x4096 world, R=52, beta=[1,.5,.25], mu=.26, "
+                                                       "sigma=.036, dt=.05, 16 U[0,1] 256^2 patches (seed 1)"}
+    if name == "single_256":
+        return [configs.single_256()], [configs.SEED_256], {"workload": "single 256x256 world, R=13 (seed 0)"}
+    if name == "multichannel":
+        return [configs.multichannel()], [configs.SEED_MULTI], {"workload": "3 channels x 1024^2, 9 kernels"}
+    ws = configs.batched(384)
+    return ws, list(range(len(ws))), {"workload": "384 uneven worlds, sides 128..1024, per-world R/mu/sigma/dt"}
+
+
+def seed_all(sim, worlds, seeds):
+    for i, (w, s) in enumerate(zip(worlds, seeds)):
+        sim.seed_patches(i, s, w.seed.patches)
+
+
+# ----------------------------------------------------------------------------- CPU leg
+
+def cpu_leg(worlds, seeds, max_seconds=20.0, min_steps=1):
+    """The reference's f32 step restated in C (oracle/lenia_oracle.c) on all host cores: a bounded
+    sample of the workload.  Returns (cell-updates/s, cores, sample description)."""
+    from oracle.oracle import RefF32
+    cores = os.cpu_count() or 1
+    ref = RefF32(threads=cores)
+    todo = [(w, s) for w, s in zip(worlds, seeds)
+            if w.channels == 1 and (w.width & (w.width - 1)) == 0 and (w.height & (w.height - 1)) == 0]
+    cells = 0
+    t_total = 0.0
+    steps_done = 0
+    for w, s in todo:
+        st = ref.seed_patches(w.width, w.height, s, w.seed.patches)
+        spectra = ref.spectra(w)
+        t0 = time.perf_counter()
+        st = ref.step(w, st, steps=min_steps, spectra=spectra)
+        t_total += time.perf_counter() - t0
+        cells += w.width * w.height * min_steps
+        steps_done += min_steps
+        if t_total > max_seconds:
+            break
+    sample = "%d world-step(s) of the restated reference step (%d power-of-two worlds available), %d threads" % (
+        steps_done, len(todo), cores)
+    return (cells / t_total if t_total > 0 else None), cores, sample
+
+
+def run_reference(args, dist):
+    worlds, seeds, cfg = workload(args.config)
+    if dist.rank != 0:
+        return
+    from oracle.oracle import RefF32
+    cores = os.cpu_count() or 1
+    ref = RefF32(threads=cores)
+    pot = [(w, s) for w, s in zip(worlds, seeds) if w.channels == 1 and (w.width & (w.width - 1)) == 0]
+    # one bench step = one generation of as many worlds as fit in ~2 s of CPU work
+    prepared = []
+    for w, s in pot:
+        prepared.append((w, ref.seed_patches(w.width, w.height, s, w.seed.patches), ref.spectra(w)))
+        if sum(x[0].width * x[0].height for x in prepared) >= 4096 * 4096:
+            break
+
+    def one():
+        cells = 0
+        for i, (w, st, sp) in enumerate(prepared):
+            prepared[i] = (w, ref.step(w, st, steps=1, spectra=sp), sp)
+            cells += w.width * w.height
+        return cells
+
+    for _ in range(args.warmup):
+        one()
+    t0 = time.perf_counter()
+    cells = 0
+    for _ in range(args.steps):
+        cells += one()
+    dt = time.perf_counter() - t0
+    value = cells / dt
+    cfg.update({"path": "cpu restatement of spectral.rs (radix-2 Stockham, f32)", "gens_per_step": 1})
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+           "config": cfg,
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": "%d world(s) one generation per step, %d threads; the reference (Rust + WGSL "
+                                      "on Vulkan) cannot build or run on this box" % (len(prepared), cores)},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ----------------------------------------------------------------------------- our arm
+
+def read_traffic():
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        return json.load(open(p))
+    except Exception:
+        return {}
+
+
+def run_ours(args, dist):
+    import auto_gb300 as ag
+    from auto_gb300 import Sim
+
+    worlds, seeds, cfg = workload(args.config)
+    sim = Sim(worlds, seed=0, path=args.path)
+    seed_all(sim, worlds, seeds)
+    if args.autotune:
+        sim.autotune()
+    G = args.gens
+    cells = sim.cells_per_step
+    for _ in range(args.warmup):
+        sim.step(G)
+    sim.wait()
+    device_sync()
+    dist.barrier()
+    device_sync()
+    clocks = Clocks(dist.local)
+    clocks.start()
+    ms = sim.step_timed(args.steps * G)
+    device_sync()
+    dist.barrier()
+    device_sync()
+    clk = clocks.stop()
+    ms = dist.max(ms)
+    value = dist.world * cells * G * args.steps / (ms * 1e-3)
+    ms_per_gen = ms / (args.steps * G)
+
+    # per-kernel breakdown (event-timed launches on the engine stream, right after the timed region)
+    prof = sim.profile(5)
+    col_ms, row_ms, step_ms = [float(x) for x in prof]
+    nclasses = len({(w.width, w.height) for w in worlds})
+    launches_per_gen = 2 * nclasses
+    if args.path == "radix2":
+        n = worlds[0].width
+        lg = int(np.log2(n))
+        launches_per_gen = len(worlds) * (1 + 2 * lg + 1 + len(worlds[0].kernels) * (2 + 2 * lg) + 1)
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs")
+    peak_src = "measured" if hbm else "fallback"
+    hbm = hbm or 6800.0
+    achieved = cells * ALG_BYTES_PER_UPDATE / (ms_per_gen * 1e-3) / 1e9
+    traffic = read_traffic().get("%s/%s" % (args.config, args.path))
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": traffic, "peak_source": peak_src,
+                "what": "whole step (column + row launch) as the unit: 12 B per cell-update over the event-timed "
+                        "generation time",
+                "kernels": {"column_ms": col_ms, "row_ms": row_ms, "step_ms_serial": step_ms,
+                            "column_share": col_ms / step_ms if step_ms else None,
+                            "column_own_bytes_per_cell": 8.0 + 1.0, "row_own_bytes_per_cell": 16.0,
+                            "column_gbs": cells * 9.0 / (col_ms * 1e-3) / 1e9 if col_ms else None,
+                            "row_gbs": cells * 16.0 / (row_ms * 1e-3) / 1e9 if row_ms else None}}
+
+    e2e = None
+    if not args.no_e2e:
+        import torch
+        host = []
+        for w in worlds:
+            t = torch.empty(w.channels * w.height * w.width, dtype=torch.float32, pin_memory=True)
+            a = t.numpy()
+            a[:] = sim.read_state(worlds.index(w)).ravel()
+            host.append((t, a))
+        L = sim._L
+        from auto_gb300._lib import check, fptr
+        device_sync()
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for i, (_, a) in enumerate(host):
+                check(L.lenia_write_state(sim._ctx, i, fptr(a), a.size), sim._ctx)
+            check(L.lenia_step(sim._ctx, G), sim._ctx)
+            for i, (_, a) in enumerate(host):
+                check(L.lenia_read_state(sim._ctx, i, fptr(a), a.size), sim._ctx)
+        device_sync()
+        t_e2e = dist.max(time.perf_counter() - t0)
+        nbytes = sum(a.nbytes for _, a in host)
+        e2e = {"value": dist.world * cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+               "d2h_bytes_per_step": nbytes, "gens_per_step": G}
+
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
+        v, cores, sample = cpu_leg(worlds, seeds)
+        cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    if dist.rank == 0:
+        cfg.update({"path": args.path, "gens_per_step": G, "cells_per_generation": cells, "worlds": len(worlds),
+                    "l2": "no flush: per-generation working set (state + half-spectrum + kernel spectrum) "
+                          "exceeds the 129 MB L2" if cells >= 4096 * 4096 else "no flush",
+                    "parallelism": "replicas" if dist.world > 1 else "single"})
+        out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
+               "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches_per_gen * G * args.steps,
+               "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
+        print(json.dumps(out))
+    sim.close()
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

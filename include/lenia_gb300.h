@@ -1,0 +1,163 @@
+/*
+ * lenia_gb300 -- Lenia-family FFT stepping engine for one NVIDIA GB300 (sm_103a).
+ *
+ * C ABI of the drop-in for the reference's continuous-CA step.  In the reference
+ * (ErikFrankling/auto, Rust + WGSL) an automaton is an `Entry` whose `build(w, h)` returns a
+ * `Program` (crates/auto-core/src/automata/mod.rs:14-27, program.rs:102-129) that a `Sim`
+ * runs on a `Gpu` (crates/auto-core/src/sim.rs:202-595).  This header replaces that stack for
+ * the spectral automata (crates/auto-core/src/automata/spectral.rs): a context owns every
+ * device buffer of one or more worlds, and the functions below mirror Sim::new, Sim::step,
+ * Sim::write_field / read_field and Sim::tick.
+ *
+ * Conventions
+ *   - Every function returns 0 on success or a negative LENIA_E* code; lenia_last_error()
+ *     gives the message (the reference returns Err(String) or panics; nothing here aborts).
+ *   - Plain pointers and sizes only.  Host buffers are float32, channel-major then row-major
+ *     (c*H*W + y*W + x), the layout of the reference's `state` field.
+ *   - One context per host thread; a context uses one CUDA stream on one GPU.
+ */
+#ifndef LENIA_GB300_H
+#define LENIA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define LENIA_API
+#else
+#define LENIA_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LENIA_MAX_KERNELS 16
+#define LENIA_MAX_CHANNELS 4
+
+/* status codes */
+#define LENIA_OK 0
+#define LENIA_EINVAL (-1)     /* bad argument: size, index, parameter */
+#define LENIA_ESIZE (-2)      /* grid size not supported / world smaller than its kernel */
+#define LENIA_ENOMEM (-3)     /* device or host allocation failed */
+#define LENIA_ECUDA (-4)      /* a CUDA call failed */
+#define LENIA_ENODEV (-5)     /* no usable sm_103 device */
+#define LENIA_ESTATE (-6)     /* call not valid in the context's current state */
+
+/* kernel shapes (spectral.rs:288-303, 356-383, 427-433) */
+#define LENIA_SHAPE_LENIA 0     /* exp(4 - 1/(q(1-q))) core, q = r/R, with beta shells */
+#define LENIA_SHAPE_SL_INNER 1  /* SmoothLife inner disc of radius ra/3, anti-aliased 0.5 */
+#define LENIA_SHAPE_SL_OUTER 2  /* SmoothLife outer ring ra/3..ra */
+#define LENIA_SHAPE_RING 3      /* MNCA hard ring lo <= r < hi */
+
+/* update rules (spectral.rs:337-345, 396-407, 461-472) */
+#define LENIA_RULE_LENIA 0      /* s_d += dt * sum_k w_k * (2 exp(-(U_k-mu_k)^2 / (2 sigma_k^2)) - 1) */
+#define LENIA_RULE_SMOOTHLIFE 1 /* Rafler's sigmoid bands on (inner, outer); needs 2 kernels */
+#define LENIA_RULE_MNCA 2       /* threshold bands on two neighbourhoods; needs 2 kernels */
+
+/* step implementations */
+#define LENIA_PATH_FP32 0       /* fused shared-memory FP32 FFT on the CUDA cores */
+#define LENIA_PATH_TF32 1       /* DFT-as-GEMM on tcgen05 tensor cores, TF32 operands */
+#define LENIA_PATH_BF16X3 2     /* DFT-as-GEMM on tcgen05, split BF16 (hi*hi + hi*lo + lo*hi) */
+#define LENIA_PATH_RADIX2 3     /* the reference's pass structure (radix-2 Stockham, one launch
+                                   per stage, spectral.rs:199-264) in FP32 CUDA */
+
+typedef struct LeniaKernel {
+    int32_t shape;      /* LENIA_SHAPE_* */
+    float radius;       /* R in cells (Lenia), ra (SmoothLife) */
+    int32_t nshells;    /* 1..3 beta shells (Lenia) */
+    float beta[3];      /* shell peak heights */
+    float ring_lo;      /* ring inner radius (MNCA) */
+    float ring_hi;      /* ring outer radius (MNCA) */
+    int32_t src;        /* source channel */
+    int32_t dst;        /* destination channel */
+    float mu, sigma;    /* Gaussian growth centre and width (LENIA_RULE_LENIA) */
+    float weight;       /* growth weight; weights into one channel should sum to 1 */
+} LeniaKernel;
+
+typedef struct LeniaWorldDesc {
+    uint32_t width, height;   /* 2^a * 3^b (b <= 1), 32..4096 */
+    uint32_t channels;        /* 1..LENIA_MAX_CHANNELS */
+    uint32_t nkernels;        /* 1..LENIA_MAX_KERNELS */
+    int32_t rule;             /* LENIA_RULE_* */
+    float dt;                 /* time step (LENIA_RULE_LENIA) */
+    LeniaKernel kernels[LENIA_MAX_KERNELS];
+} LeniaWorldDesc;
+
+typedef struct LeniaCtx LeniaCtx;
+
+/* Message for the last failure on this context; with ctx == NULL, the last failure of a
+ * call that had no context yet (lenia_create) on this thread.  Never NULL. */
+LENIA_API const char* lenia_last_error(const LeniaCtx* ctx);
+
+/* Sim::new (sim.rs:202-282): validate the worlds, allocate every buffer, precompute each
+ * kernel spectrum in FP64 on the host (spectral.rs:150-181 does it in f32 on the GPU), zero the
+ * states.  `path` is a LENIA_PATH_*.  Sizes the reference would reject with a panic
+ * (spectral.rs:103-116) return LENIA_ESIZE. */
+LENIA_API int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, LeniaCtx** out);
+LENIA_API int lenia_destroy(LeniaCtx* ctx);
+
+/* Sim::write_field("state") / read_field("state") (sim.rs:560-595) for one world.
+ * count must equal channels*height*width.  Writes are stream-ordered; reads block. */
+LENIA_API int lenia_write_state(LeniaCtx* ctx, int32_t world, const float* host, size_t count);
+LENIA_API int lenia_read_state(LeniaCtx* ctx, int32_t world, float* host, size_t count);
+/* Same with a device pointer on the caller's side (no host staging). */
+LENIA_API int lenia_write_state_device(LeniaCtx* ctx, int32_t world, const float* dev, size_t count);
+LENIA_API int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, size_t count);
+
+/* Sim::step (sim.rs:297-309): advance every world by `steps`, asynchronously.  Steps are
+ * replayed from CUDA graphs of up to 64 steps each. */
+LENIA_API int lenia_step(LeniaCtx* ctx, uint32_t steps);
+/* lenia_step, then block, and return the device time of those steps in milliseconds from CUDA
+ * events recorded on the context's stream around the graph launches. */
+LENIA_API int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms);
+/* Gpu::wait (gpu.rs:131-137). */
+LENIA_API int lenia_sync(LeniaCtx* ctx);
+/* Sim::tick. */
+LENIA_API int lenia_tick(const LeniaCtx* ctx, uint64_t* tick);
+
+/* On-device initial states (the reference's init passes, spectral.rs:183-197, 313-335).
+ * Tiles: every `spacing` x `spacing` tile whose rand3(tx, ty, seed) is even gets the pw x ph
+ * pattern with a quarter turn chosen by (r >> 8) & 3.  Patches: unit_f(rand3(x, y, seed)) in
+ * each (x0, y0, w, h) rectangle (torus-wrapped), zero elsewhere.  Channel c of a multichannel
+ * world uses seed + c. */
+LENIA_API int lenia_seed_tiles(LeniaCtx* ctx, int32_t world, uint32_t seed, const float* pattern, int32_t pw,
+                     int32_t ph, int32_t spacing);
+LENIA_API int lenia_seed_patches(LeniaCtx* ctx, int32_t world, uint32_t seed, const int32_t* patches_xywh,
+                       int32_t npatches);
+
+/* Program::cells_per_step (program.rs:116-119) summed over worlds and channels. */
+LENIA_API int lenia_cells_per_step(const LeniaCtx* ctx, uint64_t* cells);
+/* Program::total_bytes (program.rs:122-129): device bytes this context holds. */
+LENIA_API int lenia_memory_bytes(const LeniaCtx* ctx, uint64_t* bytes);
+
+/* Inspection: U_k of the current state (the convolution of kernel k's source channel that the
+ * next step will use) as float32 (height x width), and the forward half-spectrum of channel c as
+ * complex float32 (height x (width/2+1) x 2).  For tests and analysis; they do not advance time. */
+LENIA_API int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host, size_t count);
+LENIA_API int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel, float* host, size_t count);
+
+/* Per-world statistics on the device: mass (sum of channel 0) and toroidal centroid (circular
+ * mean per axis, in cells).  out: 3 floats per world (mass, cx, cy). */
+LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
+
+/* Autotuner: times the candidate launch shapes of every size class on this context's worlds
+ * and keeps the fastest.  Rebuilds the step graphs.  Optional; defaults are reasonable. */
+LENIA_API int lenia_autotune(LeniaCtx* ctx);
+
+/* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
+ * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.
+ * out[kx * (height/2+1) + ky] for kx in [0, width/2], ky in [0, height/2]; count must be
+ * (width/2+1)*(height/2+1).  The reference builds the same spectrum with an f32 FFT of the
+ * kernel on the GPU (spectral.rs:150-181). */
+LENIA_API int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, uint32_t height, float* out,
+                                    size_t count);
+
+/* Event-timed average device time of the dominant launches of one step, in milliseconds:
+ * out[0] = column passes, out[1] = row passes, out[2] = whole step.  Runs `steps` steps. */
+LENIA_API int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LENIA_GB300_H */

@@ -1,0 +1,49 @@
+// Host build of auto_gb300/csrc/fft_core.cuh: runs every Stockham stage of a plan serially
+// (all butterfly loads of a stage, then all stores, as the GPU does across its barrier) so the
+// radix plans, register DFTs, twiddle indexing and padding can be checked against numpy on a
+// machine without a GPU.
+#include <cmath>
+#include <vector>
+#include "../../auto_gb300/csrc/fft_core.cuh"
+
+using namespace lfft;
+
+template <int N, int I, bool INV>
+static void run_stage(float2* seq, const float2* tw) {
+    if constexpr (I < plan_len(N)) {
+        constexpr int R = plan_radix(N, I);
+        constexpr int L = plan_L(N, I);
+        std::vector<float2> v((N / R) * R);
+        for (int j = 0; j < N / R; j++) stage_load<N, R, L, INV>(seq, j, &v[j * R], tw);
+        for (int j = 0; j < N / R; j++) stage_store<N, R, L>(seq, j, &v[j * R]);
+        run_stage<N, I + 1, INV>(seq, tw);
+    }
+}
+
+template <int N>
+static int fft_n(int inverse, const float* in, float* out, const float2* tw) {
+    std::vector<float2> seq(seq_stride(N));
+    for (int i = 0; i < N; i++) seq[pad(i)] = make_float2(in[2 * i], in[2 * i + 1]);
+    if (inverse) run_stage<N, 0, true>(seq.data(), tw);
+    else run_stage<N, 0, false>(seq.data(), tw);
+    for (int i = 0; i < N; i++) { out[2 * i] = seq[pad(i)].x; out[2 * i + 1] = seq[pad(i)].y; }
+    return 0;
+}
+
+extern "C" int fft_host(int n, int inverse, const float* in, float* out) {
+    static std::vector<float2> tw;
+    if (tw.empty()) {
+        tw.resize(TWN);
+        for (int t = 0; t < TWN; t++) {
+            double a = -2.0 * M_PI * (double)t / (double)TWN;
+            tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+    }
+    switch (n) {
+#define CASE(N) case N: return fft_n<N>(inverse, in, out, tw.data());
+        CASE(16) CASE(32) CASE(48) CASE(64) CASE(96) CASE(128) CASE(192) CASE(256) CASE(384) CASE(512)
+        CASE(768) CASE(1024) CASE(1536) CASE(2048) CASE(3072) CASE(4096) CASE(8192)
+#undef CASE
+    }
+    return -1;
+}

@@ -1,0 +1,35 @@
+"""The shared-memory FFT templates (auto_gb300/csrc/fft_core.cuh), built for the host with g++
+and run stage by stage as the GPU does, against numpy's FFT."""
+import ctypes
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+SIZES = [16, 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096, 8192]
+
+
+@pytest.fixture(scope="module")
+def fft_host(tmp_path_factory):
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    out = str(tmp_path_factory.mktemp("fft") / "fft_host.so")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-shared", "-fPIC",
+                           os.path.join(ROOT, "tests", "cpp", "fft_core_host.cpp"), "-o", out])
+    return ctypes.CDLL(out)
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_stockham_plan_matches_numpy(fft_host, n, inverse):
+    rng = np.random.default_rng(n + inverse)
+    x = (rng.random(n) + 1j * rng.random(n)).astype(np.complex64)
+    out = np.zeros(n, np.complex64)
+    assert fft_host.fft_host(n, inverse, x.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p)) == 0
+    x64 = x.astype(np.complex128)
+    want = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
+    assert np.abs(out - want).max() / np.abs(want).max() < 2e-7
