@@ -30,11 +30,13 @@ thread_local std::string g_create_error;
 struct SizeClass {
     int W = 0, H = 0;
     std::vector<int> worlds;
-    ColItem* d_col = nullptr;
+    ColItem* d_col = nullptr;  // FP32 column items (tiles)
     int ncol = 0;
+    ColItem* d_tcg = nullptr;  // tensor-core column groups (TF32 / BF16X3 paths)
+    int ntcg = 0;
     RowItem* d_row = nullptr;
     int nrow = 0;
-    int nt_col = 0, nt_row = 0;
+    int var_col = 0, var_row = 0;  // launch variants (see launch_col_fp32)
     int nbuf = 1, general = 0, planes = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t done = nullptr;
@@ -43,6 +45,8 @@ struct SizeClass {
 struct WorldBuffers {
     ColItem* d_col = nullptr;  // this world's column items (inspection, U fields)
     int ncol = 0;
+    ColItem* d_tcg = nullptr;
+    int ntcg = 0;
     RowItem* d_row = nullptr;  // this world's row items (forward transform after writes)
     int nrow = 0;
     int cls = 0;
@@ -251,11 +255,19 @@ int refresh_spectrum(LeniaCtx* ctx, int w) {
     if (ctx->path == LENIA_PATH_RADIX2) return 0;
     const WorldBuffers& b = ctx->wb[w];
     const SizeClass& cl = ctx->classes[b.cls];
-    if (!launch_row_fp32(cl.W, cl.nt_row, MODE_FORWARD, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw,
+    if (!launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw,
                          ctx->stream))
         return fail(ctx, LENIA_ECUDA, "row transform launch failed for %dx%d", cl.W, cl.H);
     CK(cudaGetLastError());
     return 0;
+}
+
+// The column pass of one class (or one world's slice of it).
+bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int ncol, const ColItem* tcg, int ntcg,
+                    int variant, cudaStream_t s) {
+    bool ok = true;
+    if (ntcg > 0) ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
+    return ok && launch_col_fp32(cl.H, variant, cl.nbuf, ctx->d_worlds, col, ncol, ctx->d_tw, s);
 }
 
 // Enqueue `steps` steps of every world on the context's streams (captured into graphs).
@@ -272,13 +284,9 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
         cudaStream_t s = fork ? cl.stream : ctx->stream;
         if (fork) CK(cudaStreamWaitEvent(s, ctx->fork, 0));
         for (int st = 0; st < steps; st++) {
-            bool ok;
-            if (ctx->path == LENIA_PATH_FP32)
-                ok = launch_col_fp32(cl.H, cl.nt_col, cl.nbuf, ctx->d_worlds, cl.d_col, cl.ncol, ctx->d_tw, s);
-            else
-                ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_col, cl.ncol, s);
+            bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, cl.var_col, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
-            ok = launch_row_fp32(cl.W, cl.nt_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+            ok = launch_row_fp32(cl.W, cl.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
                                  ctx->d_tw, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
         }
@@ -376,19 +384,30 @@ int setup_fused(LeniaCtx* ctx) {
     if ((rc = dalloc(ctx, &ctx->d_worlds, nw))) return rc;
     CK(cudaMemcpy(ctx->d_worlds, ctx->hw.data(), nw * sizeof(DevWorld), cudaMemcpyHostToDevice));
     // work lists
+    const bool tc_path = ctx->path == LENIA_PATH_TF32 || ctx->path == LENIA_PATH_BF16X3;
     for (auto& cl : ctx->classes) {
-        std::vector<ColItem> col;
+        std::vector<ColItem> col, tcg;
         std::vector<RowItem> row;
         int nbuf = 1, general = 0, planes = 0;
+        // tensor-core groups of CT columns, except the first group of every channel: column 0
+        // packs the DC and Nyquist columns, which the FP32 pass pairs up (ky with H - ky)
+        const bool use_tc = tc_path && tc_supports(cl.H);
+        const int tpg = use_tc ? tc_columns_per_group(cl.H) / TC : 0;
         for (int wi : cl.worlds) {
             const LeniaWorldDesc& d = ctx->desc[wi];
-            const int first_col = (int)col.size(), first_row = (int)row.size();
+            const int first_col = (int)col.size(), first_row = (int)row.size(), first_tcg = (int)tcg.size();
             for (uint32_t c = 0; c < d.channels; c++) {
                 int nsrc = 0;
                 for (uint32_t k = 0; k < d.nkernels; k++) nsrc += d.kernels[k].src == (int)c;
                 if (nsrc == 0) continue;
                 if (nsrc > 1) nbuf = 2;
-                for (uint32_t t = 0; t < d.width / 8; t++) col.push_back(ColItem{wi, (int)c, (int)t, 0});
+                const int ntiles = spec_tiles(d.width);
+                if (use_tc && ntiles % tpg == 0) {
+                    for (int t = 0; t < tpg; t++) col.push_back(ColItem{wi, (int)c, t, 0});
+                    for (int t = tpg; t < ntiles; t += tpg) tcg.push_back(ColItem{wi, (int)c, t, 0});
+                } else {
+                    for (int t = 0; t < ntiles; t++) col.push_back(ColItem{wi, (int)c, t, 0});
+                }
             }
             for (uint32_t r = 0; r < d.height; r += 4) row.push_back(RowItem{wi, (int)r});
             const bool simple = d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA;
@@ -397,7 +416,7 @@ int setup_fused(LeniaCtx* ctx) {
             WorldBuffers& b = ctx->wb[wi];
             b.ncol = (int)col.size() - first_col;
             b.nrow = (int)row.size() - first_row;
-            (void)first_col;
+            b.ntcg = (int)tcg.size() - first_tcg;
         }
         if ((int)col_smem_bytes(cl.H, nbuf) > smem_max) nbuf = 1;
         if ((int)col_smem_bytes(cl.H, 1) > smem_max || (int)row_smem_bytes(cl.W, planes) > smem_max)
@@ -406,32 +425,42 @@ int setup_fused(LeniaCtx* ctx) {
         cl.nbuf = nbuf;
         cl.general = general;
         cl.planes = planes;
-        cl.nt_col = nt_choice(cl.H, cl.H >= 1024 ? 1 : 0);
-        cl.nt_row = nt_choice(cl.W, cl.W >= 1536 ? 1 : 0);
+        cl.var_col = 0;
+        cl.var_row = 0;
         cl.ncol = (int)col.size();
         cl.nrow = (int)row.size();
+        cl.ntcg = (int)tcg.size();
         if ((rc = dalloc(ctx, &cl.d_col, col.size()))) return rc;
         if ((rc = dalloc(ctx, &cl.d_row, row.size()))) return rc;
+        if ((rc = dalloc(ctx, &cl.d_tcg, tcg.size()))) return rc;
         CK(cudaMemcpy(cl.d_col, col.data(), col.size() * sizeof(ColItem), cudaMemcpyHostToDevice));
         CK(cudaMemcpy(cl.d_row, row.data(), row.size() * sizeof(RowItem), cudaMemcpyHostToDevice));
+        if (!tcg.empty()) CK(cudaMemcpy(cl.d_tcg, tcg.data(), tcg.size() * sizeof(ColItem), cudaMemcpyHostToDevice));
+        if (use_tc) {
+            int trc = tc_prepare_size(ctx->tc, ctx->path, cl.H, &ctx->err);
+            if (trc) return trc;
+        }
         // per-world slices of the class lists
-        size_t co = 0, ro = 0;
+        size_t co = 0, ro = 0, go = 0;
         for (int wi : cl.worlds) {
             WorldBuffers& b = ctx->wb[wi];
             b.d_col = cl.d_col + co;
             b.d_row = cl.d_row + ro;
+            b.d_tcg = cl.d_tcg + go;
             co += b.ncol;
             ro += b.nrow;
+            go += b.ntcg;
         }
         CK(cudaStreamCreateWithFlags(&cl.stream, cudaStreamNonBlocking));
         CK(cudaEventCreateWithFlags(&cl.done, cudaEventDisableTiming));
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
-        for (int which = 0; which < 2; which++) {
-            if (!launch_col_fp32(cl.H, nt_choice(cl.H, which), cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
-                !launch_row_fp32(cl.W, nt_choice(cl.W, which), MODE_STEP, 0, ctx->d_worlds, cl.d_row, 0, cl.planes,
-                                 ctx->d_tw, ctx->stream))
+        for (int v = 0; v < 2; v++) {
+            if (!launch_col_fp32(cl.H, v, cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
+                !launch_row_fp32(cl.W, v, MODE_STEP, 0, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw, ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
         }
+        if (cl.ntcg > 0 && !launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_tcg, 0, ctx->d_tw, ctx->stream))
+            return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core pass for H=%d", cl.H);
     }
     return 0;
 }
@@ -544,14 +573,12 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
             return bail(LENIA_ECUDA);
         }
     }
-    rc = (path == LENIA_PATH_RADIX2) ? setup_radix2(ctx) : setup_fused(ctx);
-    if (rc) return bail(rc);
     if (path == LENIA_PATH_TF32 || path == LENIA_PATH_BF16X3) {
         rc = tc_setup(ctx->tc, path, &ctx->err);
-        for (auto& cl : ctx->classes)
-            if (!rc) rc = tc_prepare_size(ctx->tc, path, cl.H, &ctx->err);
         if (rc) return bail(rc);
     }
+    rc = (path == LENIA_PATH_RADIX2) ? setup_radix2(ctx) : setup_fused(ctx);
+    if (rc) return bail(rc);
     if ((rc = dalloc(ctx, &ctx->d_stats, 3 * (size_t)nworlds))) return bail(rc);
     if ((rc = rebuild_graphs(ctx))) return bail(rc);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
@@ -603,7 +630,7 @@ int lenia_read_state(LeniaCtx* ctx, int32_t world, float* host, size_t count) {
     if (!host || count != state_count(ctx->desc[world])) return fail(ctx, LENIA_EINVAL, "bad count for world %d", world);
     CK(cudaMemcpyAsync(host, state_ptr(ctx, world), count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    return 0;
+    return tc_check_error(ctx->tc, &ctx->err);
 }
 
 int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, size_t count) {
@@ -635,13 +662,15 @@ int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms) {
     CK(cudaEventElapsedTime(ms, a, b));
     cudaEventDestroy(a);
     cudaEventDestroy(b);
+    if (!rc) rc = tc_check_error(ctx->tc, &ctx->err);
     return rc;
 }
 
 int lenia_sync(LeniaCtx* ctx) {
     if (!ctx) return LENIA_EINVAL;
     CK(cudaStreamSynchronize(ctx->stream));
-    return 0;
+    int rc = tc_check_error(ctx->tc, &ctx->err);
+    return rc;
 }
 
 int lenia_tick(const LeniaCtx* ctx, uint64_t* tick) {
@@ -723,10 +752,8 @@ int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host
     }
     const WorldBuffers& b = ctx->wb[world];
     const SizeClass& cl = ctx->classes[b.cls];
-    bool ok = (ctx->path == LENIA_PATH_FP32)
-                  ? launch_col_fp32(cl.H, cl.nt_col, cl.nbuf, ctx->d_worlds, b.d_col, b.ncol, ctx->d_tw, ctx->stream)
-                  : launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, b.d_col, b.ncol, ctx->stream);
-    ok = ok && launch_row_fp32(cl.W, cl.nt_row, MODE_U, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw, ctx->stream);
+    bool ok = launch_columns(ctx, cl, b.d_col, b.ncol, b.d_tcg, b.ntcg, cl.var_col, ctx->stream);
+    ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_U, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw, ctx->stream);
     if (!ok) return fail(ctx, LENIA_ECUDA, "U launch failed");
     CK(cudaGetLastError());
     int rc = refresh_spectrum(ctx, world);
@@ -750,7 +777,7 @@ int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel, float* ho
     CK(cudaStreamSynchronize(ctx->stream));
     for (int y = 0; y < H; y++)
         for (int kx = 0; kx < W / 2; kx++) {
-            const float2 v = tiles[((size_t)(kx / 4) * H + y) * 4 + (kx % 4)];
+            const float2 v = tiles[((size_t)(kx / TC) * H + y) * TC + (kx % TC)];
             float* o = host + ((size_t)y * KX + kx) * 2;
             if (kx == 0) {
                 o[0] = v.x;
@@ -802,11 +829,9 @@ int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
     for (uint32_t s = 0; s < steps; s++) {
         for (auto& cl : ctx->classes) {
             CK(cudaEventRecord(ev[0], ctx->stream));
-            bool ok = (ctx->path == LENIA_PATH_FP32)
-                          ? launch_col_fp32(cl.H, cl.nt_col, cl.nbuf, ctx->d_worlds, cl.d_col, cl.ncol, ctx->d_tw, ctx->stream)
-                          : launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_col, cl.ncol, ctx->stream);
+            bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, cl.var_col, ctx->stream);
             CK(cudaEventRecord(ev[1], ctx->stream));
-            ok = ok && launch_row_fp32(cl.W, cl.nt_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+            ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
                                        ctx->d_tw, ctx->stream);
             CK(cudaEventRecord(ev[2], ctx->stream));
             if (!ok) return fail(ctx, LENIA_ECUDA, "profile launch failed");
@@ -847,6 +872,14 @@ int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, uint32_t he
     return 0;
 }
 
+int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const float* b, float* d) {
+    if (!a || !b || !d) return fail(nullptr, LENIA_EINVAL, "NULL argument");
+    std::string err;
+    int rc = tc_selftest(path, n, k, a, b, d, &err);
+    if (rc) return fail(nullptr, rc, "%s", err.c_str());
+    return 0;
+}
+
 int lenia_autotune(LeniaCtx* ctx) {
     if (!ctx) return LENIA_EINVAL;
     if (ctx->path == LENIA_PATH_RADIX2) return 0;
@@ -864,15 +897,13 @@ int lenia_autotune(LeniaCtx* ctx) {
     const int reps = 5;
     for (auto& cl : ctx->classes) {
         float best_col = 1e30f, best_row = 1e30f;
-        int pick_col = cl.nt_col, pick_row = cl.nt_row;
+        int pick_col = cl.var_col, pick_row = cl.var_row;
         for (int which = 0; which < 2; which++) {
-            const int ntc = nt_choice(cl.H, which), ntr = nt_choice(cl.W, which);
+            const int ntc = which, ntr = which;
             float t_col = 0, t_row = 0;
             for (int r = 0; r < reps + 1; r++) {
                 CK(cudaEventRecord(a, ctx->stream));
-                bool ok = (ctx->path == LENIA_PATH_FP32)
-                              ? launch_col_fp32(cl.H, ntc, cl.nbuf, ctx->d_worlds, cl.d_col, cl.ncol, ctx->d_tw, ctx->stream)
-                              : launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_col, cl.ncol, ctx->stream);
+                bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, ntc, ctx->stream);
                 CK(cudaEventRecord(b, ctx->stream));
                 CK(cudaEventSynchronize(b));
                 float ms = 0;
@@ -894,8 +925,8 @@ int lenia_autotune(LeniaCtx* ctx) {
             if (t_col < best_col) { best_col = t_col; pick_col = ntc; }
             if (t_row < best_row) { best_row = t_row; pick_row = ntr; }
         }
-        cl.nt_col = pick_col;
-        cl.nt_row = pick_row;
+        cl.var_col = pick_col;
+        cl.var_row = pick_row;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);

@@ -15,10 +15,11 @@ struct DevKernel {
 
 // One world on the device.  Layouts (HBM):
 //   state [C][H][W] float                               channel-major, row-major (reference layout)
-//   spec  [C][W/8][H][4] float2   forward half-spectrum, tiles of 4 columns so that a column
-//                                 pass reads one contiguous block; column 0 packs the DC column
-//                                 (real part) with the Nyquist column W/2 (imaginary part)
-//   conv  [K][W/8][H][4] float2   per-kernel convolved spectrum (aliases spec when C = K = 1)
+//   spec  [C][W/(2*TC)][H][TC] float2   half-spectrum along x of every row, in tiles of TC
+//                                 columns so that a column pass reads one contiguous block;
+//                                 column 0 packs the DC column (real part) with the Nyquist
+//                                 column W/2 (imaginary part)
+//   conv  [K][W/(2*TC)][H][TC] float2   per-kernel convolved spectrum (aliases spec when C = K = 1)
 //   khat  [K][W/2+1][HQ] float    real, even kernel spectrum for ky in [0, H/2], times 1/(W*H)
 struct DevWorld {
     int W, H, C, K, rule;
@@ -32,24 +33,26 @@ struct DevWorld {
     DevKernel kern[LENIA_MAX_KERNELS];
 };
 
-// Work items.  Column pass: (world, channel, tile of 4 columns).  Row pass: (world, first of 4 rows).
+// Spectrum columns per tile: a column pass CTA transforms TC columns of length H.
+constexpr int TC = 2;
+
+// Work items.  Column pass: (world, channel, tile of TC columns).  Row pass: (world, first of 4 rows).
 struct ColItem { int world, chan, tile, pad; };
 struct RowItem { int world, row0; };
 
 enum RowMode { MODE_STEP = 0, MODE_FORWARD = 1, MODE_U = 2 };
 
-// Launch shapes a size class can use (threads per CTA); the autotuner picks among them.
-constexpr int NT_CHOICES[3] = {128, 256, 512};
-
-// Fused FP32 path (step_fp32.cu).  Return false if the size/thread combination is not built.
-bool launch_col_fp32(int H, int nt, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+// Fused FP32 path (step_fp32_*.cu).  Every size is built in two launch variants with the same
+// threads per CTA: variant 0 caps registers at 64 per thread (more resident CTAs), variant 1 at
+// 128.  The autotuner picks per size class.  Launchers return false if the size is not built.
+bool launch_col_fp32(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
                      const float2* tw, cudaStream_t s);
-bool launch_row_fp32(int W, int nt, int mode, int general, const DevWorld* worlds, const RowItem* items,
+bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* worlds, const RowItem* items,
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s);
 size_t col_smem_bytes(int H, int nbuf);
 size_t row_smem_bytes(int W, int acc_planes);
 int max_smem_optin();
-int nt_choice(int n, int which);  // threads per CTA built for transform length n (which = 0 or 1)
+int threads_for(int n);  // threads per CTA of the transforms of length n
 
 // Seeding and statistics (seed.cu).
 void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* patches, int npatch,
@@ -60,5 +63,6 @@ void launch_world_stats(const DevWorld* worlds, int nworlds, float* out, cudaStr
 
 // Tile-layout helpers on the host.
 inline size_t spec_elems(int W, int H) { return (size_t)(W / 2) * H; }
+inline int spec_tiles(int W) { return W / (2 * TC); }
 
 }  // namespace lenia

@@ -146,25 +146,75 @@ FFT_CHD constexpr bool size_ok(int n) {
     return n >= 2 && (n & (n - 1)) == 0 && n <= 8192;
 }
 
+// Per-stage twiddle tables.  A stage with L > 1 needs w = exp(-2 pi i k / (L R)) for k < L and,
+// when R >= 8, w^4; they are copied once per CTA from the global table into shared memory.
+FFT_CHD constexpr int stage_tw_count(int n, int i) {
+    return plan_L(n, i) > 1 ? (plan_radix(n, i) >= 8 ? 2 : 1) * plan_L(n, i) : 0;
+}
+FFT_CHD constexpr int stage_tw_offset(int n, int i) {
+    int o = 0;
+    for (int s = 0; s < i; s++) o += stage_tw_count(n, s);
+    return o;
+}
+FFT_CHD constexpr int tw_table_size(int n) { return stage_tw_offset(n, plan_len(n)); }
+
+// Fill the per-stage tables of transform length N from the global table (threads tid of nth).
+template <int N>
+FFT_HD void fill_stage_twiddles(float2* stw, const float2* tw, int tid, int nth) {
+    for (int i = 0; i < plan_len(N); i++) {
+        const int L = plan_L(N, i), R = plan_radix(N, i), off = stage_tw_offset(N, i);
+        if (L == 1) continue;
+        const int step = TWN / (L * R);
+        for (int k = tid; k < L; k += nth) {
+            stw[off + k] = tw[k * step];
+            if (R >= 8) stw[off + L + k] = tw[4 * k * step];
+        }
+    }
+}
+
 // padded shared-memory index: one float2 of padding per 16 keeps radix-16 stores conflict-free
 FFT_HD int pad(int i) { return i + (i >> 4); }
 // stride between sequences held in one shared buffer: padded length, +4 so that loads of
 // 4 interleaved columns fall into different banks
 FFT_CHD constexpr int seq_stride(int n) { return n + n / 16 + 4; }
 
-// Load butterfly j of a stage (with its inter-stage twiddle) from one sequence.
+// Twiddles w^m, m = 1..R-1, of one butterfly from w and (R >= 8) w^4; the other powers are
+// products of at most three factors, so each stays within a few float ulps of the exactly rounded
+// value (checked against numpy by the host test).
+template <int R>
+FFT_HD void twiddle_powers(float2 w1, float2 w4, float2* w) {
+    w[1] = w1;
+    if (R >= 3) w[2] = cmul(w[1], w[1]);
+    if (R >= 4) w[3] = cmul(w[2], w[1]);
+    if (R >= 8) {
+        w[4] = w4;
+        w[5] = cmul(w[4], w[1]);
+        w[6] = cmul(w[4], w[2]);
+        w[7] = cmul(w[4], w[3]);
+    }
+    if (R >= 16) {
+        w[8] = cmul(w[4], w[4]);
+#pragma unroll
+        for (int m = 9; m < 12; m++) w[m] = cmul(w[8], w[m - 8]);
+        w[12] = cmul(w[8], w[4]);
+#pragma unroll
+        for (int m = 13; m < 16; m++) w[m] = cmul(w[12], w[m - 12]);
+    }
+}
+
+// Load butterfly j of a stage (with its inter-stage twiddle) from one sequence; stw is the
+// stage's twiddle table (see fill_stage_twiddles).
 template <int N, int R, int L, bool INV>
-FFT_HD void stage_load(const float2* seq, int j, float2* v, const float2* tw) {
+FFT_HD void stage_load(const float2* seq, int j, float2* v, const float2* stw) {
     constexpr int NB = N / R;
     const int k = j % L;
 #pragma unroll
     for (int m = 0; m < R; m++) v[m] = seq[pad(j + m * NB)];
     if (L > 1) {
+        float2 w[R];
+        twiddle_powers<R>(stw[k], R >= 8 ? stw[L + k] : stw[k], w);
 #pragma unroll
-        for (int m = 1; m < R; m++) {
-            float2 w = tw[(k * m) * (TWN / (L * R))];
-            v[m] = INV ? cmulc(v[m], w) : cmul(v[m], w);
-        }
+        for (int m = 1; m < R; m++) v[m] = INV ? cmulc(v[m], w[m]) : cmul(v[m], w[m]);
     }
     Dft<R, INV>::run(v);
 }

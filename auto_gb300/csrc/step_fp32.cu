@@ -1,0 +1,42 @@
+// Dispatch of the fused FP32 step's launches to the per-size instantiations.
+#include "step_fp32.cuh"
+
+namespace lenia {
+
+size_t col_smem_bytes(int H, int nbuf) {
+    return (size_t)nbuf * TC * lfft::seq_stride(H) * sizeof(float2) + (lfft::tw_table_size(H) + 1) * sizeof(float2);
+}
+size_t row_smem_bytes(int W, int acc_planes) {
+    return (size_t)2 * lfft::seq_stride(W) * sizeof(float2) + (lfft::tw_table_size(W) + 1) * sizeof(float2) +
+           (size_t)acc_planes * 4 * W * sizeof(float);
+}
+
+int max_smem_optin() {
+    int dev = 0, v = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    return v;
+}
+
+int threads_for(int n) {
+    switch (n) {
+#define NT_CASE(N) case N: return nt_of<N>();
+        LENIA_SIZES_SMALL(NT_CASE) LENIA_SIZES_LARGE(NT_CASE)
+#undef NT_CASE
+    }
+    return 0;
+}
+
+bool launch_col_fp32(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+                     const float2* tw, cudaStream_t s) {
+    return launch_col_group_small(H, variant, nbuf, worlds, items, nitems, tw, s) ||
+           launch_col_group_large(H, variant, nbuf, worlds, items, nitems, tw, s);
+}
+
+bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* worlds, const RowItem* items,
+                     int nitems, int acc_planes, const float2* tw, cudaStream_t s) {
+    return launch_row_group_small(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s) ||
+           launch_row_group_large(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s);
+}
+
+}  // namespace lenia

@@ -24,9 +24,10 @@ namespace lenia {
 using namespace lfft;
 
 // S sequences of length N in shared memory (stride seq_stride(N)), transformed in place by NT
-// threads.  Starts after the caller's barrier; ends with a barrier.
+// threads; stw holds the per-stage twiddle tables (fill_stage_twiddles).  Starts after the
+// caller's barrier; ends with a barrier.
 template <int N, int S, int NT, bool INV, int I = 0>
-__device__ __forceinline__ void fft_seqs(float2* buf, const float2* __restrict__ tw) {
+__device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
     if constexpr (I < plan_len(N)) {
         constexpr int R = plan_radix(N, I);
         constexpr int L = plan_L(N, I);
@@ -40,7 +41,7 @@ __device__ __forceinline__ void fft_seqs(float2* buf, const float2* __restrict__
             const int b = threadIdx.x + p * NT;
             if ((TOT % NT) == 0 || b < TOT) {
                 const int s = b / NB, j = b - s * NB;
-                stage_load<N, R, L, INV>(buf + s * SEQ, j, v[p], tw);
+                stage_load<N, R, L, INV>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, I));
             }
         }
         __syncthreads();
@@ -53,9 +54,13 @@ __device__ __forceinline__ void fft_seqs(float2* buf, const float2* __restrict__
             }
         }
         __syncthreads();
-        fft_seqs<N, S, NT, INV, I + 1>(buf, tw);
+        fft_seqs<N, S, NT, INV, I + 1>(buf, stw);
     }
 }
+
+// Shared memory of a pass: the sequences, then (float2-aligned) the stage twiddle tables.
+template <int N>
+constexpr size_t stage_table_bytes() { return (size_t)(tw_table_size(N) + 1) * sizeof(float2); }
 
 __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
 
@@ -90,20 +95,35 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 
 // Half-spectra of rows r0..r0+3 (tile layout) -> two packed complex sequences
 // Z_p = A + iB with A = row r0+2p, B = row r0+2p+1, using Hermitian symmetry for k > W/2.
+// Consecutive threads cover whole tiles: 4 rows x TC columns = one contiguous chunk.
 template <int W, int NT>
 __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __restrict__ sp, int H, int r0) {
     constexpr int SEQ = seq_stride(W);
-    for (int e = threadIdx.x; e < (W / 8) * 8; e += NT) {
-        const int t = e >> 3, p = (e >> 2) & 1, c = e & 3, kx = 4 * t + c;
-        const float2* src = sp + ((size_t)t * H + r0 + 2 * p) * 4 + c;
-        const float2 A = src[0], B = src[4];
-        float2* z = Z + p * SEQ;
-        if (kx == 0) {
-            z[pad(0)] = make_float2(A.x, B.x);
-            z[pad(W / 2)] = make_float2(A.y, B.y);
-        } else {
-            z[pad(kx)] = make_float2(A.x - B.y, A.y + B.x);
-            z[pad(W - kx)] = make_float2(A.x + B.y, B.x - A.y);
+    constexpr int IT = (W + NT - 1) / NT;  // W/(2 TC) tiles x 2 pairs x TC columns, over NT threads
+    float2 A[IT], B[IT];
+#pragma unroll
+    for (int i = 0; i < IT; i++) {  // every load in flight before the first use
+        const int e = threadIdx.x + i * NT;
+        if (IT * NT == W || e < W) {
+            const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC;
+            const float2* src = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
+            A[i] = src[0];
+            B[i] = src[TC];
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < IT; i++) {
+        const int e = threadIdx.x + i * NT;
+        if (IT * NT == W || e < W) {
+            const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC, kx = TC * t + c;
+            float2* z = Z + p * SEQ;
+            if (kx == 0) {
+                z[pad(0)] = make_float2(A[i].x, B[i].x);
+                z[pad(W / 2)] = make_float2(A[i].y, B[i].y);
+            } else {
+                z[pad(kx)] = make_float2(A[i].x - B[i].y, A[i].y + B[i].x);
+                z[pad(W - kx)] = make_float2(A[i].x + B[i].y, B[i].x - A[i].y);
+            }
         }
     }
 }
@@ -112,8 +132,8 @@ __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __re
 template <int W, int NT>
 __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __restrict__ sp, int H, int r0) {
     constexpr int SEQ = seq_stride(W);
-    for (int e = threadIdx.x; e < (W / 8) * 8; e += NT) {
-        const int t = e >> 3, p = (e >> 2) & 1, c = e & 3, kx = 4 * t + c;
+    for (int e = threadIdx.x; e < W; e += NT) {
+        const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC, kx = TC * t + c;
         const float2* z = Z + p * SEQ;
         float2 A, B;
         if (kx == 0) {
@@ -125,19 +145,21 @@ __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __r
             A = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
             B = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
         }
-        float2* dst = sp + ((size_t)t * H + r0 + 2 * p) * 4 + c;
+        float2* dst = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
         dst[0] = A;
-        dst[4] = B;
+        dst[TC] = B;
     }
 }
 
-template <int W, int NT>
-__global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items,
+template <int W, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items,
                                                 int mode, int general, const float2* __restrict__ tw) {
     extern __shared__ float4 smem_raw[];
     constexpr int SEQ = seq_stride(W);
     float2* Z = reinterpret_cast<float2*>(smem_raw);
-    float* acc = reinterpret_cast<float*>(Z + 2 * SEQ);  // [planes][4][W]
+    float2* stw = Z + 2 * SEQ;
+    float* acc = reinterpret_cast<float*>(stw + tw_table_size(W) + 1);  // [planes][4][W]
+    fill_stage_twiddles<W>(stw, tw, threadIdx.x, NT);
     const RowItem it = items[blockIdx.x];
     const DevWorld& wd = worlds[it.world];
     const int H = wd.H, C = wd.C, K = wd.K, r0 = it.row0;
@@ -146,12 +168,23 @@ __global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ w
     if (mode == MODE_FORWARD) {
         for (int d = 0; d < C; d++) {
             const float* st = wd.state + d * plane + (size_t)r0 * W;
-            for (int e = threadIdx.x; e < 2 * W; e += NT) {
-                const int p = e / W, x = e - p * W;
-                Z[p * SEQ + pad(x)] = make_float2(st[(2 * p) * W + x], st[(2 * p + 1) * W + x]);
+            constexpr int IT = (2 * W + NT - 1) / NT;
+            float a[IT], b[IT];
+#pragma unroll
+            for (int i = 0; i < IT; i++) {
+                const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
+                if (IT * NT == 2 * W || e < 2 * W) {
+                    a[i] = st[(2 * p) * W + x];
+                    b[i] = st[(2 * p + 1) * W + x];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < IT; i++) {
+                const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
+                if (IT * NT == 2 * W || e < 2 * W) Z[p * SEQ + pad(x)] = make_float2(a[i], b[i]);
             }
             __syncthreads();
-            fft_seqs<W, 2, NT, false>(Z, tw);
+            fft_seqs<W, 2, NT, false>(Z, stw);
             store_rows_spectrum<W, NT>(Z, wd.spec + d * cplane, H, r0);
             __syncthreads();
         }
@@ -162,7 +195,7 @@ __global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ w
         for (int k = 0; k < K; k++) {
             load_rows_spectrum<W, NT>(Z, wd.conv + k * cplane, H, r0);
             __syncthreads();
-            fft_seqs<W, 2, NT, true>(Z, tw);
+            fft_seqs<W, 2, NT, true>(Z, stw);
             float* u = wd.u_out + k * plane + (size_t)r0 * W;
             for (int e = threadIdx.x; e < 2 * W; e += NT) {
                 const int p = e / W, x = e - p * W;
@@ -181,21 +214,37 @@ __global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ w
         const float dtw = wd.dt * kp.weight;
         load_rows_spectrum<W, NT>(Z, wd.conv, H, r0);
         __syncthreads();
-        fft_seqs<W, 2, NT, true>(Z, tw);
+        fft_seqs<W, 2, NT, true>(Z, stw);
         float* st = wd.state + (size_t)r0 * W;
-        for (int e = threadIdx.x; e < 2 * W; e += NT) {
-            const int p = e / W, x = e - p * W;
-            const float2 u = Z[p * SEQ + pad(x)];
-            float* s0 = st + (2 * p) * W + x;
-            float* s1 = s0 + W;
-            const float n0 = clamp01(*s0 + dtw * growth(u.x, kp.mu, kp.sigma));
-            const float n1 = clamp01(*s1 + dtw * growth(u.y, kp.mu, kp.sigma));
-            *s0 = n0;
-            *s1 = n1;
-            Z[p * SEQ + pad(x)] = make_float2(n0, n1);
+        // state values for this thread's cells, in chunks of up to 8 loads per row pair
+        constexpr int IT = (2 * W + NT - 1) / NT;
+        constexpr int CH = IT < 8 ? IT : 8;
+#pragma unroll
+        for (int i0 = 0; i0 < IT; i0 += CH) {
+            float a[CH], b[CH];
+#pragma unroll
+            for (int i = 0; i < CH; i++) {
+                const int e = threadIdx.x + (i0 + i) * NT, p = e / W, x = e - p * W;
+                if (i0 + i < IT && (IT * NT == 2 * W || e < 2 * W)) {
+                    a[i] = st[(2 * p) * W + x];
+                    b[i] = st[(2 * p + 1) * W + x];
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < CH; i++) {
+                const int e = threadIdx.x + (i0 + i) * NT, p = e / W, x = e - p * W;
+                if (i0 + i < IT && (IT * NT == 2 * W || e < 2 * W)) {
+                    const float2 u = Z[p * SEQ + pad(x)];
+                    const float n0 = clamp01(a[i] + dtw * growth(u.x, kp.mu, kp.sigma));
+                    const float n1 = clamp01(b[i] + dtw * growth(u.y, kp.mu, kp.sigma));
+                    st[(2 * p) * W + x] = n0;
+                    st[(2 * p + 1) * W + x] = n1;
+                    Z[p * SEQ + pad(x)] = make_float2(n0, n1);
+                }
+            }
         }
         __syncthreads();
-        fft_seqs<W, 2, NT, false>(Z, tw);
+        fft_seqs<W, 2, NT, false>(Z, stw);
         store_rows_spectrum<W, NT>(Z, wd.spec, H, r0);
         return;
     }
@@ -208,7 +257,7 @@ __global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ w
         const DevKernel kp = wd.kern[k];
         load_rows_spectrum<W, NT>(Z, wd.conv + k * cplane, H, r0);
         __syncthreads();
-        fft_seqs<W, 2, NT, true>(Z, tw);
+        fft_seqs<W, 2, NT, true>(Z, stw);
         for (int e = threadIdx.x; e < 2 * W; e += NT) {
             const int p = e / W, x = e - p * W;
             const float2 u = Z[p * SEQ + pad(x)];
@@ -241,7 +290,7 @@ __global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ w
             Z[p * SEQ + pad(x)] = make_float2(n[0], n[1]);
         }
         __syncthreads();
-        fft_seqs<W, 2, NT, false>(Z, tw);
+        fft_seqs<W, 2, NT, false>(Z, stw);
         store_rows_spectrum<W, NT>(Z, wd.spec + d * cplane, H, r0);
         __syncthreads();
     }
@@ -249,17 +298,17 @@ __global__ void __launch_bounds__(NT, 1) row_pass(const DevWorld* __restrict__ w
 
 // ---------------------------------------------------------------------------- column pass
 
-// X (4 sequences of length H, forward spectrum of tile `t`) times khat -> T.  Column 0 of
+// X (TC sequences of length H, forward spectrum of tile `t`) times khat -> T.  Column 0 of
 // tile 0 packs the DC column (real part) and the Nyquist column (imaginary part): both are
 // real sequences, so with Z = FFT_y(packed), Z' = Z*(K0+KN)/2 + conj(Z[-ky])*(K0-KN)/2.
 template <int H, int NT>
 __device__ __forceinline__ void multiply_khat(const float2* X, float2* T, const float* __restrict__ kh, int HQ,
                                               int W, int t) {
     constexpr int SEQ = seq_stride(H);
-    for (int e = threadIdx.x; e < 4 * H; e += NT) {
+    for (int e = threadIdx.x; e < TC * H; e += NT) {
         const int col = e / H, ky = e - col * H;
         if (t == 0 && col == 0) continue;
-        const int kx = 4 * t + col;
+        const int kx = TC * t + col;
         const float kv = kh[(size_t)kx * HQ + (ky <= H / 2 ? ky : H - ky)];
         T[col * SEQ + pad(ky)] = cscale(X[col * SEQ + pad(ky)], kv);
     }
@@ -275,15 +324,26 @@ __device__ __forceinline__ void multiply_khat(const float2* X, float2* T, const 
     }
 }
 
+// One tile (H rows x TC columns, contiguous) <-> TC sequences in shared memory.
 template <int H, int NT>
 __device__ __forceinline__ void load_tile(float2* X, const float2* __restrict__ src) {
+    static_assert(TC == 2, "tile loads move one float4 (two columns) per row");
     constexpr int SEQ = seq_stride(H);
+    constexpr int IT = (H + NT - 1) / NT;
     const float4* s4 = reinterpret_cast<const float4*>(src);
-    for (int e = threadIdx.x; e < 2 * H; e += NT) {
-        const int y = e >> 1, h = e & 1;
-        const float4 v = s4[e];
-        X[(2 * h) * SEQ + pad(y)] = make_float2(v.x, v.y);
-        X[(2 * h + 1) * SEQ + pad(y)] = make_float2(v.z, v.w);
+    float4 v[IT];
+#pragma unroll
+    for (int i = 0; i < IT; i++) {
+        const int y = threadIdx.x + i * NT;
+        if (IT * NT == H || y < H) v[i] = s4[y];
+    }
+#pragma unroll
+    for (int i = 0; i < IT; i++) {
+        const int y = threadIdx.x + i * NT;
+        if (IT * NT == H || y < H) {
+            X[pad(y)] = make_float2(v[i].x, v[i].y);
+            X[SEQ + pad(y)] = make_float2(v[i].z, v[i].w);
+        }
     }
 }
 
@@ -291,25 +351,26 @@ template <int H, int NT>
 __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__ dst) {
     constexpr int SEQ = seq_stride(H);
     float4* d4 = reinterpret_cast<float4*>(dst);
-    for (int e = threadIdx.x; e < 2 * H; e += NT) {
-        const int y = e >> 1, h = e & 1;
-        const float2 a = X[(2 * h) * SEQ + pad(y)], b = X[(2 * h + 1) * SEQ + pad(y)];
-        d4[e] = make_float4(a.x, a.y, b.x, b.y);
+    for (int y = threadIdx.x; y < H; y += NT) {
+        const float2 a = X[pad(y)], b = X[SEQ + pad(y)];
+        d4[y] = make_float4(a.x, a.y, b.x, b.y);
     }
 }
 
-template <int H, int NT>
-__global__ void __launch_bounds__(NT, 1) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
+template <int H, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
                                                 int nbuf, const float2* __restrict__ tw) {
     extern __shared__ float4 smem_raw[];
     constexpr int SEQ = seq_stride(H);
     float2* X = reinterpret_cast<float2*>(smem_raw);
-    float2* Y = X + 4 * SEQ;
+    float2* Y = X + TC * SEQ;
+    float2* stw = X + nbuf * TC * SEQ;
+    fill_stage_twiddles<H>(stw, tw, threadIdx.x, NT);
     const ColItem it = items[blockIdx.x];
     const DevWorld& wd = worlds[it.world];
     const int W = wd.W, c = it.chan, t = it.tile, K = wd.K, HQ = wd.HQ;
     const size_t cplane = (size_t)(W / 2) * H;
-    const float2* src = wd.spec + c * cplane + (size_t)t * H * 4;
+    const float2* src = wd.spec + c * cplane + (size_t)t * H * TC;
     int nsrc = 0;
     for (int k = 0; k < K; k++) nsrc += (wd.kern[k].src == c);
     if (nsrc == 0) return;
@@ -320,22 +381,76 @@ __global__ void __launch_bounds__(NT, 1) col_pass(const DevWorld* __restrict__ w
         if (!have || reload) {
             load_tile<H, NT>(X, src);
             __syncthreads();
-            fft_seqs<H, 4, NT, false>(X, tw);
+            fft_seqs<H, TC, NT, false>(X, stw);
             have = true;
         }
         float2* T = (nsrc > 1 && !reload) ? Y : X;
         const float* kh = wd.khat + (size_t)k * (W / 2 + 1) * HQ;
         multiply_khat<H, NT>(X, T, kh, HQ, W, t);
         __syncthreads();
-        fft_seqs<H, 4, NT, true>(T, tw);
-        store_tile<H, NT>(T, wd.conv + k * cplane + (size_t)t * H * 4);
+        fft_seqs<H, TC, NT, true>(T, stw);
+        store_tile<H, NT>(T, wd.conv + k * cplane + (size_t)t * H * TC);
         __syncthreads();
     }
 }
 
-// Sizes built, and the two thread counts each size is built with.
-#define LENIA_SIZES(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768) X(1024) X(1536) X(2048) X(3072) X(4096)
-template <int N> constexpr int nt_lo() { return N <= 128 ? 64 : (N <= 512 ? 128 : 256); }
-template <int N> constexpr int nt_hi() { return N <= 128 ? 128 : (N <= 512 ? 256 : 512); }
+// Sizes built: each TU instantiates one group.  Threads per CTA: one radix-16 butterfly per
+// thread for the two sequences a CTA holds (2N/16), between 64 and 512.
+#define LENIA_SIZES_SMALL(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768)
+#define LENIA_SIZES_LARGE(X) X(1024) X(1536) X(2048) X(3072) X(4096)
+template <int N> constexpr int nt_of() { return N / 8 < 64 ? 64 : (N / 8 > 512 ? 512 : N / 8); }
+// variant 0: at most 64 registers per thread; variant 1: at most 128
+template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) / nt_of<N>() < 1 ? 1 : (V == 0 ? 1024 : 512) / nt_of<N>(); }
+
+// Launch one instantiation.  Dynamic shared memory above 48 KB must be enabled per kernel before
+// its first launch and before any stream capture that contains it; a zero-item call does just that.
+template <int H, int NT, int MINB>
+bool col_go(int nbuf, const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
+    const size_t smem = (size_t)nbuf * TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>();
+    static int attr_max = 0;
+    if ((int)smem > attr_max) {
+        if (cudaFuncSetAttribute(col_pass<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return false;
+        attr_max = (int)smem;
+    }
+    if (nitems > 0) col_pass<H, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, nbuf, tw);
+    return true;
+}
+
+template <int W, int NT, int MINB>
+bool row_go(int mode, int general, int planes, const DevWorld* worlds, const RowItem* items, int nitems,
+            const float2* tw, cudaStream_t s) {
+    const size_t smem = (size_t)2 * seq_stride(W) * sizeof(float2) + stage_table_bytes<W>() +
+                        (size_t)planes * 4 * W * sizeof(float);
+    static int attr_max = 0;
+    if ((int)smem > attr_max) {
+        if (cudaFuncSetAttribute(row_pass<W, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return false;
+        attr_max = (int)smem;
+    }
+    if (nitems > 0) row_pass<W, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, mode, general, tw);
+    return true;
+}
+
+#define LENIA_COL_CASE(N)                                                                                   \
+    case N:                                                                                                 \
+        return variant == 0 ? col_go<N, nt_of<N>(), minb_of<N, 0>()>(nbuf, worlds, items, nitems, tw, s)    \
+                            : col_go<N, nt_of<N>(), minb_of<N, 1>()>(nbuf, worlds, items, nitems, tw, s);
+#define LENIA_ROW_CASE(N)                                                                                   \
+    case N:                                                                                                 \
+        return variant == 0                                                                                 \
+                   ? row_go<N, nt_of<N>(), minb_of<N, 0>()>(mode, general, planes, worlds, items, nitems, tw, s) \
+                   : row_go<N, nt_of<N>(), minb_of<N, 1>()>(mode, general, planes, worlds, items, nitems, tw, s);
+
+bool launch_col_group_small(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+                            const float2* tw, cudaStream_t s);
+bool launch_col_group_large(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+                            const float2* tw, cudaStream_t s);
+bool launch_row_group_small(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
+                            const RowItem* items, int nitems, const float2* tw, cudaStream_t s);
+bool launch_row_group_large(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
+                            const RowItem* items, int nitems, const float2* tw, cudaStream_t s);
 
 }  // namespace lenia

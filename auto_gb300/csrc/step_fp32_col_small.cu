@@ -1,0 +1,12 @@
+// Column-pass instantiations of the fused FP32 step, small sizes (templates in step_fp32.cuh).
+#include "step_fp32.cuh"
+
+namespace lenia {
+
+bool launch_col_group_small(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+                            const float2* tw, cudaStream_t s) {
+    switch (H) { LENIA_SIZES_SMALL(LENIA_COL_CASE) }
+    return false;
+}
+
+}  // namespace lenia

@@ -1,0 +1,12 @@
+// Row-pass instantiations of the fused FP32 step, small sizes (templates in step_fp32.cuh).
+#include "step_fp32.cuh"
+
+namespace lenia {
+
+bool launch_row_group_small(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
+                            const RowItem* items, int nitems, const float2* tw, cudaStream_t s) {
+    switch (W) { LENIA_SIZES_SMALL(LENIA_ROW_CASE) }
+    return false;
+}
+
+}  // namespace lenia

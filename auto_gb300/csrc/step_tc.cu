@@ -1,18 +1,641 @@
-// Tensor-core (tcgen05) DFT-as-GEMM column pass.
+// Column pass as DFT-as-GEMM on the 5th-generation tensor cores (tcgen05): LENIA_PATH_TF32 and
+// LENIA_PATH_BF16X3.
+//
+// The column pass transforms every spectrum column along y, multiplies by the kernel spectrum
+// and transforms back (the FP32 path does this with shared-memory butterflies).  Here a column
+// of length H = H1*H2 (y = y1 + H1*y2) is transformed by the four-step method as two real GEMMs
+// against small DFT matrices, with the twiddle exp(-2 pi i y1 k2 / H) applied between them:
+//
+//   GEMM A  rows (c, y1)  x  K (re/im, y2)  ->  N (k2, re/im)      DFT over y2, length H2
+//   GEMM B  rows (c, k2)  x  K (re/im, y1)  ->  N (k1, re/im)      DFT over y1, length H1
+//            spectrum X[c][k2 + H2*k1]  *  khat  (real), conjugated
+//   GEMM C  rows (c, k2)  x  K (re/im, k1)  ->  N (y1, re/im)      DFT over k1
+//   GEMM D  rows (c, y1)  x  K (re/im, k2)  ->  N (y2, re/im)      DFT over k2, then conjugated
+//
+// The inverse uses the forward matrices through IDFT(z) = conj(DFT(conj z)).  The data is the A
+// operand (M = 128-row blocks of the CT columns a CTA owns), the DFT matrix is the B operand, both
+// in shared memory in the canonical K-major layout, with FP32 accumulators in TMEM.  BF16X3 splits
+// both operands into bf16 hi + lo and accumulates hi*hi + hi*lo + lo*hi; TF32 rounds both to tf32.
+// Tiles arrive and leave by bulk (TMA) copies; one elected thread issues every MMA.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "fft_core.cuh"
 #include "step_tc.cuh"
+#include "tc_ptx.cuh"
 
 namespace lenia {
+using namespace tc;
+
+template <int H1_, int H2_, int CT_, bool X3_>
+struct TcShape {
+    static constexpr int H1 = H1_, H2 = H2_, CT = CT_, H = H1 * H2;
+    static constexpr bool X3 = X3_;
+    static constexpr int E = X3 ? 2 : 4;              // operand element bytes
+    static constexpr int NOP = X3 ? 2 : 1;            // hi/lo copies
+    static constexpr int MA = CT * H1, KA = 2 * H2, NA = 2 * H2;
+    static constexpr int MB = CT * H2, KB = 2 * H1, NB = 2 * H1;
+    static constexpr int OPND = 2 * CT * H * E;       // one operand copy (MA*KA*E == MB*KB*E)
+    static constexpr int FA = NA * KA * E, FB = NB * KB * E;
+    static constexpr bool SAME = H1 == H2;
+    static constexpr int STG = CT * H * 8;            // fp32 complex tile group
+    static constexpr int OFF_F2 = OPND * NOP;
+    static constexpr int OFF_F1 = OFF_F2 + FA * NOP;
+    static constexpr int OFF_STG = OFF_F1 + (SAME ? 0 : FB * NOP);
+    static constexpr int OFF_BAR = OFF_STG + STG;
+    static constexpr int SMEM = OFF_BAR + 64;
+    static constexpr int COLS_A = (MA / 128) * NA, COLS_B = (MB / 128) * NB;
+    static constexpr int REGION = COLS_A > COLS_B ? COLS_A : COLS_B;
+    static constexpr int TCOLS = 2 * REGION <= 32 ? 32 : (2 * REGION <= 64 ? 64 : (2 * REGION <= 128 ? 128 : (2 * REGION <= 256 ? 256 : 512)));
+    static_assert(OPND * NOP == STG, "the output staging reuses the operand area");
+    static_assert(MA % 128 == 0 && MB % 128 == 0, "row blocks of 128");
+    static_assert(NA % 32 == 0 && NB % 32 == 0, "TMEM loads of 32 columns");
+    static_assert(2 * REGION <= 512, "TMEM");
+};
+
+// ------------------------------------------------------------------ operand stores
+template <bool X3>
+__device__ __forceinline__ void store_elem(uint8_t* op, int opnd_bytes, int r, int k, int K, float v) {
+    if (X3) {
+        const uint32_t off = kmajor_offset(r, k, K, 2);
+        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+        *reinterpret_cast<__nv_bfloat16*>(op + off) = hi;
+        *reinterpret_cast<__nv_bfloat16*>(op + opnd_bytes + off) = lo;
+    } else {
+        *reinterpret_cast<uint32_t*>(op + kmajor_offset(r, k, K, 4)) = to_tf32(v);
+    }
+}
+
+// 16 bytes of consecutive K: 8 values (bf16 hi and lo) or 4 (tf32), starting at k0.
+template <bool X3>
+__device__ __forceinline__ void store_chunk(uint8_t* op, int opnd_bytes, int r, int k0, int K, const float* v) {
+    if (X3) {
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
+            const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
+            const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
+            hi[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
+            lo[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
+        }
+        const uint32_t off = kmajor_offset(r, k0, K, 2);
+        *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(op + opnd_bytes + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+    } else {
+        *reinterpret_cast<uint4*>(op + kmajor_offset(r, k0, K, 4)) =
+            make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+    }
+}
+
+// One GEMM: D[rows of M in blocks of 128] (+)= A (M x K, K-major) * F^T (F: N x K, K-major).
+template <bool X3>
+__device__ __forceinline__ void issue_gemm(uint32_t d_tmem, uint32_t a_saddr, uint32_t a_lo_off, int M, int K,
+                                           uint32_t f_saddr, uint32_t f_lo_off, int N, uint32_t idesc) {
+    constexpr int E = X3 ? 2 : 4;
+    const uint32_t sbo = (uint32_t)(K * E * 8);
+    const int ksteps = K * E / 32;
+    for (int b = 0; b < M / 128; b++) {
+        const uint32_t d = d_tmem + (uint32_t)(b * N);
+        const uint32_t a0 = a_saddr + (uint32_t)b * 16u * sbo;
+        for (int s = 0; s < ksteps; s++) {
+            const uint64_t ad = smem_desc(a0 + 256u * s, 128, sbo);
+            const uint64_t bd = smem_desc(f_saddr + 256u * s, 128, sbo);
+            mma<!X3>(d, ad, bd, idesc, s > 0 ? 1u : 0u);
+            if (X3) {
+                mma<false>(d, ad, smem_desc(f_saddr + f_lo_off + 256u * s, 128, sbo), idesc, 1u);
+                mma<false>(d, smem_desc(a0 + a_lo_off + 256u * s, 128, sbo), bd, idesc, 1u);
+            }
+        }
+    }
+}
+
+// Twiddle exp(-2 pi i a b / H) from the global table (TWN entries).
+template <int H>
+__device__ __forceinline__ float2 twid(const float2* __restrict__ tw, int a, int b) {
+    return tw[((a * b) % H) * (lfft::TWN / H)];
+}
+
+// A group is (world, channel, first tile); it covers CT columns = CT / TC consecutive tiles.
+template <class S>
+__global__ void __launch_bounds__(128, 1)
+    col_pass_tc(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ groups, int ngroups,
+                const uint8_t* __restrict__ fmats, const float2* __restrict__ tw, int* err) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint8_t* op = smem;
+    uint8_t* f2 = smem + S::OFF_F2;
+    uint8_t* f1 = S::SAME ? f2 : smem + S::OFF_F1;
+    float2* stg = reinterpret_cast<float2*>(smem + S::OFF_STG);
+    uint64_t* bar_ld = reinterpret_cast<uint64_t*>(smem + S::OFF_BAR);
+    uint64_t* bar_mma = bar_ld + 1;
+    uint64_t* bar_f = bar_ld + 2;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_ld + 3);
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    constexpr uint32_t IDESC_A = instr_desc(S::X3 ? 1 : 2, 128, S::NA);
+    constexpr uint32_t IDESC_B = instr_desc(S::X3 ? 1 : 2, 128, S::NB);
+
+    if (tid == 0) {
+        mbar_init(bar_ld, 1);
+        mbar_init(bar_mma, 1);
+        mbar_init(bar_f, 1);
+        *abort_flag = 0;
+        fence_barrier_init();
+    }
+    if (warp == 0) tmem_alloc(tmem_slot, S::TCOLS);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tmem_slot;
+    const uint32_t t_b = tbase;                 // D of GEMM B (kept while every kernel of the channel runs)
+    const uint32_t t_x = tbase + S::REGION;     // D of GEMMs A, C, D
+    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+
+    // DFT matrices (hi, lo) once per CTA; first tile group
+    if (tid == 0) {
+        const uint32_t fbytes = (S::FA + (S::SAME ? 0 : S::FB)) * S::NOP;
+        mbar_arrive_expect_tx(bar_f, fbytes);
+        bulk_g2s(f2, fmats, fbytes, bar_f);
+    }
+    auto load_group = [&](int g) {
+        const ColItem it = groups[g];
+        const DevWorld& wd = worlds[it.world];
+        const float2* src = wd.spec + (size_t)it.chan * (wd.W / 2) * S::H + (size_t)it.tile * S::H * TC;
+        mbar_arrive_expect_tx(bar_ld, S::STG);
+        bulk_g2s(stg, src, S::STG, bar_ld);
+    };
+    if (tid == 0 && blockIdx.x < ngroups) load_group(blockIdx.x);
+    bool ok = mbar_wait(bar_f, 0);
+    uint32_t ph_ld = 0, ph_mma = 0;
+
+    for (int g = blockIdx.x; g < ngroups && ok; g += gridDim.x) {
+        const ColItem it = groups[g];
+        const DevWorld& wd = worlds[it.world];
+        const int W = wd.W, HQ = wd.HQ, K = wd.K;
+        const int kx0 = it.tile * TC;
+        if (!mbar_wait(bar_ld, ph_ld)) ok = false;
+        ph_ld ^= 1;
+        if (tid == 0) bulk_wait_read0();  // the previous group's output has left the operand area
+        __syncthreads();
+        if (!ok) *abort_flag = 1;
+        if (*abort_flag) break;
+
+        // ---- stage 0: tile group (fp32, [tile][y][c][re,im]) -> A_A rows (c, y1), K (re/im, y2)
+        for (int b = 0; b < S::MA / 128; b++) {
+            const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
+            const float2* col = stg + (size_t)(c / TC) * S::H * TC + (c % TC);
+            constexpr int CH = S::X3 ? 8 : 4;
+#pragma unroll 2
+            for (int y2 = 0; y2 < S::H2; y2 += CH) {
+                float re[CH], im[CH];
+#pragma unroll
+                for (int u = 0; u < CH; u++) {
+                    const float2 v = col[(size_t)(y1 + S::H1 * (y2 + u)) * TC];
+                    re[u] = v.x;
+                    im[u] = v.y;
+                }
+                store_chunk<S::X3>(op, S::OPND, r, y2, S::KA, re);
+                store_chunk<S::X3>(op, S::OPND, r, S::H2 + y2, S::KA, im);
+            }
+        }
+        fence_async_smem();
+        __syncthreads();
+        // the staging buffer is free: fetch the next group while this one computes
+        if (tid == 0 && g + (int)gridDim.x < ngroups) load_group(g + gridDim.x);
+
+        // ---- GEMM A
+        if (tid == 0) {
+            tc_fence_after();
+            issue_gemm<S::X3>(t_x, smem_u32(op), S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A);
+            mma_commit(bar_mma);
+        }
+        if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
+        ph_mma ^= 1;
+        tc_fence_after();
+
+        // ---- A -> B: twiddle exp(-2 pi i y1 k2 / H), rows (c, k2), K (re/im, y1)
+        for (int b = 0; b < S::MA / 128; b++) {
+            const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
+            for (int q = 0; q < S::NA / 32; q++) {
+                float v[32];
+                tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NA + 32 * q), v);
+#pragma unroll
+                for (int u = 0; u < 16; u++) {
+                    const int k2 = 16 * q + u;
+                    const float2 w = twid<S::H>(tw, y1, k2);
+                    const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
+                    const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
+                    const int rr = c * S::H2 + k2;
+                    store_elem<S::X3>(op, S::OPND, rr, y1, S::KB, re);
+                    store_elem<S::X3>(op, S::OPND, rr, S::H1 + y1, S::KB, im);
+                }
+            }
+        }
+        tc_fence_before();
+        fence_async_smem();
+        __syncthreads();
+
+        // ---- GEMM B -> spectrum of the channel along y, kept in TMEM region t_b
+        if (tid == 0) {
+            tc_fence_after();
+            issue_gemm<S::X3>(t_b, smem_u32(op), S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B);
+            mma_commit(bar_mma);
+        }
+        if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
+        ph_mma ^= 1;
+        tc_fence_after();
+
+        for (int k = 0; k < K; k++) {
+            if (wd.kern[k].src != it.chan) continue;
+            const float* kh = wd.khat + (size_t)k * (W / 2 + 1) * HQ;
+            // ---- B -> C: x khat (real, even), conjugate; rows (c, k2), K (re/im, k1)
+            for (int b = 0; b < S::MB / 128; b++) {
+                const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
+                const float* khrow = kh + (size_t)(kx0 + c) * HQ;
+                for (int q = 0; q < S::NB / 32; q++) {
+                    float v[32];
+                    tmem_ld32(t_b + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
+                    float re[16], im[16];
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const int ky = k2 + S::H2 * (16 * q + u);
+                        const float s = khrow[ky <= S::H / 2 ? ky : S::H - ky];
+                        re[u] = v[2 * u] * s;
+                        im[u] = -v[2 * u + 1] * s;
+                    }
+                    constexpr int CH = S::X3 ? 8 : 4;
+#pragma unroll
+                    for (int u = 0; u < 16; u += CH) {
+                        store_chunk<S::X3>(op, S::OPND, r, 16 * q + u, S::KB, re + u);
+                        store_chunk<S::X3>(op, S::OPND, r, S::H1 + 16 * q + u, S::KB, im + u);
+                    }
+                }
+            }
+            tc_fence_before();
+            fence_async_smem();
+            __syncthreads();
+            // ---- GEMM C
+            if (tid == 0) {
+                tc_fence_after();
+                issue_gemm<S::X3>(t_x, smem_u32(op), S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B);
+                mma_commit(bar_mma);
+            }
+            if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
+            ph_mma ^= 1;
+            tc_fence_after();
+            // ---- C -> D: twiddle exp(-2 pi i k2 y1 / H); rows (c, y1), K (re/im, k2)
+            for (int b = 0; b < S::MB / 128; b++) {
+                const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
+                for (int q = 0; q < S::NB / 32; q++) {
+                    float v[32];
+                    tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const int y1 = 16 * q + u;
+                        const float2 w = twid<S::H>(tw, k2, y1);
+                        const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
+                        const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
+                        const int rr = c * S::H1 + y1;
+                        store_elem<S::X3>(op, S::OPND, rr, k2, S::KA, re);
+                        store_elem<S::X3>(op, S::OPND, rr, S::H2 + k2, S::KA, im);
+                    }
+                }
+            }
+            tc_fence_before();
+            fence_async_smem();
+            __syncthreads();
+            // ---- GEMM D
+            if (tid == 0) {
+                tc_fence_after();
+                issue_gemm<S::X3>(t_x, smem_u32(op), S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A);
+                mma_commit(bar_mma);
+            }
+            if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
+            ph_mma ^= 1;
+            tc_fence_after();
+            // ---- output: conjugate, natural order y = y1 + H1*y2, into the operand area
+            float2* out = reinterpret_cast<float2*>(op);
+            for (int b = 0; b < S::MA / 128; b++) {
+                const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
+                float2* col = out + (size_t)(c / TC) * S::H * TC + (c % TC);
+                for (int q = 0; q < S::NA / 32; q++) {
+                    float v[32];
+                    tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NA + 32 * q), v);
+#pragma unroll
+                    for (int u = 0; u < 16; u++)
+                        col[(size_t)(y1 + S::H1 * (16 * q + u)) * TC] = make_float2(v[2 * u], -v[2 * u + 1]);
+                }
+            }
+            tc_fence_before();
+            fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                float2* dst = wd.conv + (size_t)k * (W / 2) * S::H + (size_t)it.tile * S::H * TC;
+                bulk_s2g(dst, out, S::STG);
+                bulk_commit();
+                bulk_wait_read0();  // the next kernel (if any) rebuilds the operand area
+            }
+            __syncthreads();
+            if (*abort_flag) break;
+        }
+        if (*abort_flag) break;
+    }
+    if (*abort_flag && tid == 0) atomicExch(err, 1);
+    if (tid == 0) {
+        bulk_wait0();
+        // a group load may still be in flight if this CTA stopped early; wait for it (bounded)
+        if (*abort_flag) mbar_wait(bar_ld, ph_ld);
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(tbase, S::TCOLS);
+    }
+}
+
+// ------------------------------------------------------------------ host side
+
+namespace {
+
+// DFT matrix of length n as the B operand: rows (k, re/im out), K (re/im in, y), exp(-2 pi i y k / n),
+// in the K-major layout, as bf16 hi then lo, or tf32 -- rounded from FP64.
+void build_dft_operand(int n, bool x3, std::vector<uint8_t>& out) {
+    const int N = 2 * n, K = 2 * n, E = x3 ? 2 : 4;
+    const size_t bytes = (size_t)N * K * E;
+    const size_t base = out.size();
+    out.resize(base + bytes * (x3 ? 2 : 1), 0);
+    for (int row = 0; row < N; row++)
+        for (int kk = 0; kk < K; kk++) {
+            const int k = row / 2, ro = row % 2, ri = kk / n, y = kk % n;
+            const double th = 2.0 * M_PI * (double)((long)y * k % n) / n, c = std::cos(th), s = std::sin(th);
+            const double v = ro == 0 ? (ri == 0 ? c : s) : (ri == 0 ? -s : c);
+            const uint32_t off = kmajor_offset(row, kk, K, E);
+            if (x3) {
+                const __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
+                const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
+                *reinterpret_cast<__nv_bfloat16*>(&out[base + off]) = hi;
+                *reinterpret_cast<__nv_bfloat16*>(&out[base + bytes + off]) = lo;
+            } else {
+                float f = (float)v;
+                uint32_t u;
+                memcpy(&u, &f, 4);
+                // round to nearest tf32 (10 mantissa bits), ties away from zero
+                u = (u + 0x1000u) & 0xFFFFE000u;
+                memcpy(&out[base + off], &u, 4);
+            }
+        }
+}
+
+struct ShapeInfo {
+    int H, H1, H2, CT;
+};
+constexpr ShapeInfo SHAPES[] = {{4096, 64, 64, 2}, {2048, 64, 32, 4}, {1024, 32, 32, 4}, {512, 32, 16, 8}, {256, 16, 16, 8}};
+
+const ShapeInfo* shape_for(int H) {
+    for (const auto& s : SHAPES)
+        if (s.H == H) return &s;
+    return nullptr;
+}
+
+template <class S>
+bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups, int ngroups, const float2* tw,
+                  int* err, cudaStream_t st) {
+    static int attr = 0;
+    if (!attr) {
+        if (cudaFuncSetAttribute(col_pass_tc<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess)
+            return false;
+        attr = 1;
+    }
+    if (ngroups <= 0) return true;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_pass_tc<S>, 128, S::SMEM) != cudaSuccess || per_sm < 1)
+        return false;
+    // TMEM: co-resident CTAs must fit in 512 columns
+    if (per_sm * S::TCOLS > 512) per_sm = 512 / S::TCOLS;
+    int grid = sms * per_sm;
+    if (grid > ngroups) grid = ngroups;
+    col_pass_tc<S><<<grid, 128, S::SMEM, st>>>(worlds, groups, ngroups, (const uint8_t*)fm, tw, err);
+    return true;
+}
+
+}  // namespace
+
+int tc_columns_per_group(int H) {
+    const ShapeInfo* s = shape_for(H);
+    return s ? s->CT : 0;
+}
 
 int tc_setup(TcPlan& plan, int path, std::string* err) {
-    (void)plan; (void)path;
-    if (err) *err = "the tensor-core paths are not built in this library yet";
-    return LENIA_EINVAL;
+    (void)err;
+    plan.path = path;
+    plan.ready = 1;
+    if (!plan.d_err) {
+        if (cudaMalloc(&plan.d_err, sizeof(int)) != cudaSuccess) {
+            if (err) *err = "tensor-core error flag allocation failed";
+            return LENIA_ENOMEM;
+        }
+        cudaMemset(plan.d_err, 0, sizeof(int));
+    }
+    return 0;
 }
+
 int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
-    (void)plan; (void)path; (void)H; (void)err;
-    return LENIA_EINVAL;
+    const ShapeInfo* s = shape_for(H);
+    if (!s) return 0;  // served by the FP32 column pass
+    for (int i = 0; i < plan.nsizes; i++)
+        if (plan.sizes[i] == H) return 0;
+    if (plan.nsizes >= 16) {
+        if (err) *err = "too many tensor-core sizes";
+        return LENIA_EINVAL;
+    }
+    const bool x3 = path == LENIA_PATH_BF16X3;
+    std::vector<uint8_t> host;
+    build_dft_operand(s->H2, x3, host);                  // F_H2 (hi, lo)
+    if (s->H1 != s->H2) build_dft_operand(s->H1, x3, host);  // F_H1 (hi, lo)
+    void* d = nullptr;
+    if (cudaMalloc(&d, host.size()) != cudaSuccess ||
+        cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (err) *err = "DFT matrix upload failed";
+        return LENIA_ECUDA;
+    }
+    plan.mats[plan.nsizes] = d;
+    plan.sizes[plan.nsizes] = H;
+    plan.nsizes++;
+    return 0;
 }
-bool launch_col_tc(const TcPlan&, int, int, const DevWorld*, const ColItem*, int, cudaStream_t) { return false; }
-void tc_release(TcPlan& plan) { plan.ready = 0; }
+
+bool tc_supports(int H) { return shape_for(H) != nullptr; }
+
+bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
+                   const float2* tw, cudaStream_t s) {
+    const void* fm = nullptr;
+    for (int i = 0; i < plan.nsizes; i++)
+        if (plan.sizes[i] == H) fm = plan.mats[i];
+    if (!fm) return false;
+    const bool x3 = path == LENIA_PATH_BF16X3;
+    int* e = (int*)plan.d_err;
+    switch (H) {
+    case 4096: return x3 ? launch_shape<TcShape<64, 64, 2, true>>(fm, worlds, groups, ngroups, tw, e, s)
+                         : launch_shape<TcShape<64, 64, 2, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s)
+                         : launch_shape<TcShape<64, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s)
+                         : launch_shape<TcShape<32, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    case 512: return x3 ? launch_shape<TcShape<32, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s)
+                        : launch_shape<TcShape<32, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    case 256: return x3 ? launch_shape<TcShape<16, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s)
+                        : launch_shape<TcShape<16, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    }
+    return false;
+}
+
+int tc_check_error(TcPlan& plan, std::string* err) {
+    if (!plan.d_err) return 0;
+    int h = 0;
+    if (cudaMemcpy(&h, plan.d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return LENIA_ECUDA;
+    if (h) {
+        cudaMemset(plan.d_err, 0, sizeof(int));
+        if (err) *err = "a tensor-core column pass gave up waiting on a barrier; results of that step are invalid";
+        return LENIA_ECUDA;
+    }
+    return 0;
+}
+
+void tc_release(TcPlan& plan) {
+    for (int i = 0; i < plan.nsizes; i++) cudaFree(plan.mats[i]);
+    plan.nsizes = 0;
+    if (plan.d_err) cudaFree(plan.d_err);
+    plan.d_err = nullptr;
+    plan.ready = 0;
+}
+
+}  // namespace lenia
+
+// ------------------------------------------------------------------ GEMM self-test
+namespace lenia {
+
+template <bool X3>
+__global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b,
+                                                             int n, int k, float* d, int* err) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    constexpr int E = X3 ? 2 : 4, NOP = X3 ? 2 : 1;
+    const int abytes = 128 * k * E, bbytes = n * k * E;
+    uint8_t* sa = smem;
+    uint8_t* sb = smem + abytes * NOP;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sb + bbytes * NOP);
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    for (int i = tid * 16; i < abytes * NOP; i += 128 * 16) *reinterpret_cast<uint4*>(sa + i) = *reinterpret_cast<const uint4*>(a + i);
+    for (int i = tid * 16; i < bbytes * NOP; i += 128 * 16) *reinterpret_cast<uint4*>(sb + i) = *reinterpret_cast<const uint4*>(b + i);
+    if (tid == 0) {
+        mbar_init(bar, 1);
+        fence_barrier_init();
+    }
+    if (warp == 0) tmem_alloc(slot, 256);
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t t = *slot;
+    if (tid == 0) {
+        issue_gemm<X3>(t, smem_u32(sa), abytes, 128, k, smem_u32(sb), bbytes, n, instr_desc(X3 ? 1 : 2, 128, n));
+        mma_commit(bar);
+    }
+    const bool ok = mbar_wait(bar, 0);
+    tc_fence_after();
+    if (!ok && tid == 0) atomicExch(err, 1);
+    for (int q = 0; q < n / 32 && ok; q++) {
+        float v[32];
+        tmem_ld32(t + ((uint32_t)(warp * 32) << 16) + 32 * q, v);
+        for (int j = 0; j < 32; j++) d[(size_t)tid * n + 32 * q + j] = v[j];
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        tmem_dealloc(t, 256);
+    }
+}
+
+namespace {
+void pack_operand(const float* m, int rows, int k, bool x3, std::vector<uint8_t>& out) {
+    const int E = x3 ? 2 : 4;
+    const size_t bytes = (size_t)rows * k * E;
+    out.assign(bytes * (x3 ? 2 : 1), 0);
+    for (int r = 0; r < rows; r++)
+        for (int c = 0; c < k; c++) {
+            const float v = m[(size_t)r * k + c];
+            const uint32_t off = kmajor_offset(r, c, k, E);
+            if (x3) {
+                const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+                const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+                *reinterpret_cast<__nv_bfloat16*>(&out[off]) = hi;
+                *reinterpret_cast<__nv_bfloat16*>(&out[bytes + off]) = lo;
+            } else {
+                uint32_t u;
+                memcpy(&u, &v, 4);
+                u = (u + 0x1000u) & 0xFFFFE000u;
+                memcpy(&out[off], &u, 4);
+            }
+        }
+}
+}  // namespace
+
+int tc_selftest(int path, int n, int k, const float* a, const float* b, float* d, std::string* err) {
+    const bool x3 = path == LENIA_PATH_BF16X3;
+    if ((path != LENIA_PATH_TF32 && !x3) || n < 32 || n > 256 || n % 32 || k < 16 || k > 256 || k % 16) {
+        if (err) *err = "selftest: path must be TF32 or BF16X3, n in 32..256 (multiple of 32), k in 16..256 (multiple of 16)";
+        return LENIA_EINVAL;
+    }
+    std::vector<uint8_t> ha, hb;
+    pack_operand(a, 128, k, x3, ha);
+    pack_operand(b, n, k, x3, hb);
+    uint8_t *da = nullptr, *db = nullptr;
+    float* dd = nullptr;
+    int* de = nullptr;
+    int rc = 0;
+    const size_t smem = ha.size() + hb.size() + 64;
+    if (cudaMalloc(&da, ha.size()) || cudaMalloc(&db, hb.size()) || cudaMalloc(&dd, (size_t)128 * n * 4) ||
+        cudaMalloc(&de, 4)) {
+        rc = LENIA_ENOMEM;
+    } else {
+        cudaMemcpy(da, ha.data(), ha.size(), cudaMemcpyHostToDevice);
+        cudaMemcpy(db, hb.data(), hb.size(), cudaMemcpyHostToDevice);
+        cudaMemset(de, 0, 4);
+        cudaMemset(dd, 0, (size_t)128 * n * 4);
+        cudaError_t e;
+        if (x3) {
+            cudaFuncSetAttribute(tc_selftest_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            tc_selftest_kernel<true><<<1, 128, smem>>>(da, db, n, k, dd, de);
+        } else {
+            cudaFuncSetAttribute(tc_selftest_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            tc_selftest_kernel<false><<<1, 128, smem>>>(da, db, n, k, dd, de);
+        }
+        e = cudaDeviceSynchronize();
+        int h = 0;
+        if (e == cudaSuccess) e = cudaMemcpy(&h, de, 4, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(d, dd, (size_t)128 * n * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            rc = LENIA_ECUDA;
+            if (err) *err = std::string("selftest: ") + cudaGetErrorString(e);
+        } else if (h) {
+            rc = LENIA_ECUDA;
+            if (err) *err = "selftest: MMA completion wait timed out";
+        }
+    }
+    cudaFree(da);
+    cudaFree(db);
+    cudaFree(dd);
+    cudaFree(de);
+    return rc;
+}
 
 }  // namespace lenia

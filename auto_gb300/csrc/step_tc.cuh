@@ -8,18 +8,29 @@
 
 namespace lenia {
 
-// Per-context device data of the tensor-core path: DFT matrices per column length.
+// Per-context device data of the tensor-core path: the DFT matrices per column length, and a
+// flag a kernel sets if it gives up waiting on a barrier.
 struct TcPlan {
     int ready = 0;
+    int path = 0;
     void* mats[16] = {};
     int sizes[16] = {};
     int nsizes = 0;
+    void* d_err = nullptr;
 };
 
+// Column lengths the tensor-core pass serves (256..4096, powers of two); others use the FP32 pass.
+bool tc_supports(int H);
+// Spectrum columns one tensor-core CTA transforms at a time (a multiple of TC).
+int tc_columns_per_group(int H);
 int tc_setup(TcPlan& plan, int path, std::string* err);
 int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err);
-bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* items, int nitems,
-                   cudaStream_t s);
+// groups: (world, channel, first tile) items, each covering tc_columns_per_group(H) columns.
+bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
+                   const float2* tw, cudaStream_t s);
+int tc_check_error(TcPlan& plan, std::string* err);
 void tc_release(TcPlan& plan);
+// One GEMM through the same operand layouts and descriptors (diagnostic).
+int tc_selftest(int path, int n, int k, const float* a, const float* b, float* d, std::string* err);
 
 }  // namespace lenia

@@ -100,8 +100,7 @@ class Sim:
         return out
 
     def write_state(self, world: int, state: np.ndarray):
-        w = self.worlds[world]
-        a = np.ascontiguousarray(state, np.float32).reshape(w.channels, w.height, w.width)
+        a = np.ascontiguousarray(state, np.float32).ravel()
         self._check(self._L.lenia_write_state(self._ctx, world, fptr(a), a.size))
         self.wait()
 

@@ -132,8 +132,9 @@ LENIA_API int lenia_cells_per_step(const LeniaCtx* ctx, uint64_t* cells);
 LENIA_API int lenia_memory_bytes(const LeniaCtx* ctx, uint64_t* bytes);
 
 /* Inspection: U_k of the current state (the convolution of kernel k's source channel that the
- * next step will use) as float32 (height x width), and the forward half-spectrum of channel c as
- * complex float32 (height x (width/2+1) x 2).  For tests and analysis; they do not advance time. */
+ * next step will use) as float32 (height x width), and the half-spectrum along x of every row of
+ * channel c, which the engine keeps between steps, as complex float32 (height x (width/2+1) x 2).
+ * For tests and analysis; they do not advance time. */
 LENIA_API int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host, size_t count);
 LENIA_API int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel, float* host, size_t count);
 
@@ -152,6 +153,13 @@ LENIA_API int lenia_autotune(LeniaCtx* ctx);
  * kernel on the GPU (spectral.rs:150-181). */
 LENIA_API int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, uint32_t height, float* out,
                                     size_t count);
+
+/* Diagnostic: one tensor-core GEMM, D (128 x n) = A (128 x k) * B^T (B is n x k), through the
+ * shared-memory operand layout, descriptors and TMEM reads the tensor-core column pass uses.
+ * A, B, D are row-major float32 on the host; path is LENIA_PATH_TF32 or LENIA_PATH_BF16X3;
+ * n in 32..256 (multiple of 32), k in 16..256 (multiple of 16).  No counterpart in the
+ * reference (it has no tensor-core code). */
+LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const float* b, float* d);
 
 /* Event-timed average device time of the dominant launches of one step, in milliseconds:
  * out[0] = column passes, out[1] = row passes, out[2] = whole step.  Runs `steps` steps. */

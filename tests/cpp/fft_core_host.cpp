@@ -14,7 +14,7 @@ static void run_stage(float2* seq, const float2* tw) {
         constexpr int R = plan_radix(N, I);
         constexpr int L = plan_L(N, I);
         std::vector<float2> v((N / R) * R);
-        for (int j = 0; j < N / R; j++) stage_load<N, R, L, INV>(seq, j, &v[j * R], tw);
+        for (int j = 0; j < N / R; j++) stage_load<N, R, L, INV>(seq, j, &v[j * R], tw + stage_tw_offset(N, I));
         for (int j = 0; j < N / R; j++) stage_store<N, R, L>(seq, j, &v[j * R]);
         run_stage<N, I + 1, INV>(seq, tw);
     }
@@ -23,9 +23,11 @@ static void run_stage(float2* seq, const float2* tw) {
 template <int N>
 static int fft_n(int inverse, const float* in, float* out, const float2* tw) {
     std::vector<float2> seq(seq_stride(N));
+    std::vector<float2> stw(tw_table_size(N) + 1);
+    fill_stage_twiddles<N>(stw.data(), tw, 0, 1);
     for (int i = 0; i < N; i++) seq[pad(i)] = make_float2(in[2 * i], in[2 * i + 1]);
-    if (inverse) run_stage<N, 0, true>(seq.data(), tw);
-    else run_stage<N, 0, false>(seq.data(), tw);
+    if (inverse) run_stage<N, 0, true>(seq.data(), stw.data());
+    else run_stage<N, 0, false>(seq.data(), stw.data());
     for (int i = 0; i < N; i++) { out[2 * i] = seq[pad(i)].x; out[2 * i + 1] = seq[pad(i)].y; }
     return 0;
 }

@@ -1,0 +1,80 @@
+"""Tensor-core (tcgen05) path on a GB300: the GEMM self-test through the operand layouts and
+descriptors the column pass uses, then the TF32 / BF16x3 step against the FP64 oracle.
+
+Tolerances: the self-test GEMM against float64 (TF32 1e-2 relative, BF16x3 2e-4 relative, as the
+operand roundings allow); the BF16x3 step per step against FP64 within 1e-4 max-abs (the target
+precision of the tensor-core path); TF32 is reported, with a looser bound of 5e-3."""
+import numpy as np
+import pytest
+
+import auto_gb300 as ag
+from auto_gb300 import Sim, configs
+from auto_gb300 import _lib
+from oracle.oracle import fp64_convolve, fp64_step
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def built():
+    from auto_gb300 import native
+    native.build()
+    _lib.load()
+
+
+@pytest.mark.parametrize("path,tol", [(_lib.PATH_BF16X3, 2e-4), (_lib.PATH_TF32, 1e-2)])
+@pytest.mark.parametrize("n,k", [(128, 128), (64, 64), (32, 32), (256, 128)])
+def test_gemm_selftest(path, tol, n, k):
+    rng = np.random.default_rng(n * k + path)
+    a = rng.standard_normal((128, k)).astype(np.float32)
+    b = rng.standard_normal((n, k)).astype(np.float32)
+    d = np.zeros((128, n), np.float32)
+    rc = _lib.load().lenia_tc_selftest(path, n, k, _lib.fptr(a), _lib.fptr(b), _lib.fptr(d))
+    assert rc == 0, _lib.load().lenia_last_error(None)
+    want = a.astype(np.float64) @ b.astype(np.float64).T
+    err = np.abs(d - want).max() / np.abs(want).max()
+    assert err < tol, err
+
+
+@pytest.mark.parametrize("path", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("side", [256, 512, 1024, 2048, 4096])
+def test_tc_u_field_vs_fp64(path, side):
+    rng = np.random.default_rng(side)
+    s = rng.random((side, side), dtype=np.float32)
+    world = ag.World(side, side, [ag.Kernel(radius=min(52.0, side / 4), beta=[1.0, 0.5, 0.25])])
+    with Sim(world, path=path) as sim:
+        sim.write_state(0, s)
+        u = sim.u_field(0, 0)
+    want = fp64_convolve(world, s[None])[0]
+    err = float(np.abs(u - want).max())
+    print("U field %s %d: max|err| = %.3e" % (path, side, err))
+    assert err < (2e-5 if path == "bf16x3" else 2e-3), err
+
+
+@pytest.mark.parametrize("path,tol", [("bf16x3", 1e-4), ("tf32", 5e-3)])
+def test_tc_config2_teacher_forced(path, tol):
+    world = configs.single_4096()
+    with Sim(world, seed=configs.SEED_4096, path=path) as sim:
+        s = sim.read_state(0)
+        worst = 0.0
+        for _ in range(2):
+            sim.step(1)
+            got = sim.read_state(0)
+            worst = max(worst, float(np.abs(got - fp64_step(world, s)).max()))
+            s = got
+    print("config2 %s per-step max|err| vs FP64 = %.3e" % (path, worst))
+    assert worst < tol, worst
+
+
+@pytest.mark.parametrize("path", ["bf16x3", "tf32"])
+def test_tc_batched_and_multichannel_run(path):
+    worlds = configs.batched(24)
+    with Sim(worlds, seed=0, path=path) as sim:
+        for i, w in enumerate(worlds):
+            sim.seed_patches(i, i, w.seed.patches)
+        sim.step(3)
+        before = [sim.read_state(i) for i in range(len(worlds))]
+        sim.step(1)
+        for i, w in enumerate(worlds):
+            err = np.abs(sim.read_state(i) - fp64_step(w, before[i])).max()
+            assert err < (1e-4 if path == "bf16x3" else 1e-2), (i, w.width, err)
