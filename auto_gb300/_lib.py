@@ -23,7 +23,7 @@ EXPORTS = [
     "lenia_write_state_device", "lenia_read_state_device", "lenia_step", "lenia_step_timed", "lenia_sync",
     "lenia_tick", "lenia_seed_tiles", "lenia_seed_patches", "lenia_cells_per_step", "lenia_memory_bytes",
     "lenia_read_field_u", "lenia_read_spectrum", "lenia_world_stats", "lenia_autotune", "lenia_profile_step",
-    "lenia_kernel_spectrum", "lenia_tc_selftest",
+    "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_step_noalloc",
 ]
 
 
@@ -80,6 +80,7 @@ def _declare(L):
         "lenia_profile_step": [vp, u32, _c_float_p],
         "lenia_kernel_spectrum": [ctypes.POINTER(LeniaKernel), u32, u32, _c_float_p, sz],
         "lenia_tc_selftest": [i32, i32, i32, _c_float_p, _c_float_p, _c_float_p],
+        "lenia_step_noalloc": [vp, u32, u32, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, u32, vp],
     }
     for name, args in sig.items():
         f = getattr(L, name)

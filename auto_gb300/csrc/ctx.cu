@@ -519,6 +519,8 @@ float* state_ptr(LeniaCtx* ctx, int w) { return ctx->path == LENIA_PATH_RADIX2 ?
 
 }  // namespace
 
+void lenia::set_thread_error(const std::string& msg) { g_create_error = msg; }
+
 extern "C" {
 
 const char* lenia_last_error(const LeniaCtx* ctx) {

@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/lenia_gb300.h"
 
 namespace lenia {
@@ -60,6 +62,9 @@ void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* 
 void launch_seed_tiles(float* state, int W, int H, uint32_t seed, const float* pattern, int pw, int ph,
                        int spacing, cudaStream_t s);
 void launch_world_stats(const DevWorld* worlds, int nworlds, float* out, cudaStream_t s);
+
+// The message lenia_last_error(NULL) returns on this thread (calls that have no context).
+void set_thread_error(const std::string& msg);
 
 // Tile-layout helpers on the host.
 inline size_t spec_elems(int W, int H) { return (size_t)(W / 2) * H; }

@@ -161,6 +161,22 @@ LENIA_API int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, u
  * reference (it has no tensor-core code). */
 LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const float* b, float* d);
 
+/* Steps one world of one channel and one Lenia kernel `steps` times, in place, without allocating
+ * device memory.  For callers that cannot call cudaMalloc when they step: an application that
+ * has given all device memory to its own pool allocator, or a real-time frame loop where an
+ * allocation (which may synchronize the device) would stall the frame.  No counterpart in the
+ * reference.
+ *   state   device pointer, height*width float32, read and overwritten
+ *   khat    device pointer holding lenia_kernel_spectrum()'s output for this kernel and size
+ *   stream  a cudaStream_t, or NULL for the default stream; the call is asynchronous on it
+ * The scratch it needs (half-spectrum, twiddles, work lists) is a fixed __device__ array of about
+ * 4.2 MiB that every GPU loading this library holds until exit, so width*height is limited to
+ * 1,048,576 cells (larger returns LENIA_ESIZE).  The first call on a device finds the array's
+ * address and fills its twiddle table: make it before any stream capture.  All calls share the
+ * array, so calls that overlap on the GPU race; serialise them.  Errors: lenia_last_error(NULL). */
+LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, const float* khat, float mu,
+                                 float sigma, float dt, uint32_t steps, void* stream);
+
 /* Event-timed average device time of the dominant launches of one step, in milliseconds:
  * out[0] = column passes, out[1] = row passes, out[2] = whole step.  Runs `steps` steps. */
 LENIA_API int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3);
