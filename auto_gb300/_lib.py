@@ -24,6 +24,8 @@ EXPORTS = [
     "lenia_tick", "lenia_seed_tiles", "lenia_seed_patches", "lenia_cells_per_step", "lenia_memory_bytes",
     "lenia_read_field_u", "lenia_read_spectrum", "lenia_world_stats", "lenia_autotune", "lenia_profile_step",
     "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_step_noalloc",
+    "lenia_mlp_create", "lenia_mlp_destroy", "lenia_mlp_param_count", "lenia_mlp_set_params",
+    "lenia_mlp_get_params", "lenia_mlp_gradients", "lenia_mlp_train_step", "lenia_mlp_predict",
 ]
 
 
@@ -81,6 +83,14 @@ def _declare(L):
         "lenia_kernel_spectrum": [ctypes.POINTER(LeniaKernel), u32, u32, _c_float_p, sz],
         "lenia_tc_selftest": [i32, i32, i32, _c_float_p, _c_float_p, _c_float_p],
         "lenia_step_noalloc": [vp, u32, u32, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, u32, vp],
+        "lenia_mlp_create": [u32, u32, ctypes.POINTER(vp)],
+        "lenia_mlp_destroy": [vp],
+        "lenia_mlp_param_count": [ctypes.POINTER(u32)],
+        "lenia_mlp_set_params": [vp, _c_float_p, sz],
+        "lenia_mlp_get_params": [vp, _c_float_p, sz],
+        "lenia_mlp_gradients": [vp, _c_float_p, _c_float_p, u32, _c_float_p, _c_float_p],
+        "lenia_mlp_train_step": [vp, _c_float_p, _c_float_p, u32, ctypes.c_float, _c_float_p],
+        "lenia_mlp_predict": [vp, _c_float_p, u32, _c_float_p],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -71,6 +72,11 @@ struct LeniaCtx {
     std::vector<void*> allocs;
     uint64_t tick = 0;
     uint64_t bytes = 0;
+    // one device arena for all per-world buffers (many small worlds would otherwise cost one
+    // cudaMalloc each): `arena_need` is summed in a sizing pass, then carved in order
+    char* arena = nullptr;
+    size_t arena_need = 0, arena_used = 0;
+    bool sizing = false;
     int graph_steps = 64;
     cudaGraphExec_t graph_big = nullptr, graph_one = nullptr;
     TcPlan tc;
@@ -97,6 +103,18 @@ int fail(LeniaCtx* c, int code, const char* fmt, ...) {
 
 template <typename T>
 int dalloc(LeniaCtx* ctx, T** p, size_t count) {
+    const size_t bytes = (count * sizeof(T) + 255) / 256 * 256;
+    if (ctx->sizing) {
+        ctx->arena_need += bytes;
+        *p = nullptr;
+        return 0;
+    }
+    if (ctx->arena && ctx->arena_used + bytes <= ctx->arena_need) {
+        *p = (T*)(ctx->arena + ctx->arena_used);
+        ctx->arena_used += bytes;
+        ctx->bytes += bytes;
+        return 0;
+    }
     void* v = nullptr;
     cudaError_t e = cudaMalloc(&v, count * sizeof(T) > 0 ? count * sizeof(T) : 16);
     if (e != cudaSuccess) {
@@ -160,7 +178,7 @@ int guard_reach(const LeniaKernel& k) {
 // for kx in [0, W/2], ky in [0, H/2].  The kernel is even in dx and in dy (min-image
 // placement), so this is its exact DFT; the reference computes the same spectrum with an f32
 // FFT on the GPU (spectral.rs:150-181).
-void compute_khat(const LeniaKernel& k, int W, int H, int HQ, float* out) {
+void compute_khat(const LeniaKernel& k, int W, int H, int HQ, float* out, bool threaded = true) {
     const int reach = guard_reach(k) + 1;
     const int nR = reach + 1;
     std::vector<double> v((size_t)nR * nR);
@@ -183,7 +201,7 @@ void compute_khat(const LeniaKernel& k, int W, int H, int HQ, float* out) {
             rw[(size_t)dy * KX + kx] = a;
         }
     const double norm = 1.0 / (sum * (double)W * (double)H);
-    unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    unsigned nth = threaded ? std::max(1u, std::min(16u, std::thread::hardware_concurrency())) : 1u;
     auto work = [&](unsigned t) {
         for (int kx = (int)t; kx < KX; kx += (int)nth)
             for (int ky = 0; ky < KY; ky++) {
@@ -345,10 +363,69 @@ int setup_fused(LeniaCtx* ctx) {
         ctx->wb[i].cls = found;
     }
     const int smem_max = max_smem_optin();
+    // per-world buffers: a sizing pass, one arena, then the same calls carve it
+    auto world_buffers = [&](void) -> int {
+        for (int i = 0; i < nw; i++) {
+            const LeniaWorldDesc& d = ctx->desc[i];
+            DevWorld& w = ctx->hw[i];
+            const size_t cells = (size_t)d.width * d.height;
+            int rc;
+            if ((rc = dalloc(ctx, &w.state, cells * d.channels))) return rc;
+            if ((rc = dalloc(ctx, &w.spec, spec_elems(d.width, d.height) * d.channels))) return rc;
+            if (d.channels == 1 && d.nkernels == 1) w.conv = w.spec;
+            else if ((rc = dalloc(ctx, &w.conv, spec_elems(d.width, d.height) * d.nkernels))) return rc;
+            float* kh;
+            if ((rc = dalloc(ctx, &kh, (size_t)(d.width / 2 + 1) * (d.height / 2 + 1) * d.nkernels))) return rc;
+            w.khat = kh;
+        }
+        return 0;
+    };
+    ctx->sizing = true;
+    int rc0 = world_buffers();
+    ctx->sizing = false;
+    if (rc0) return rc0;
+    {
+        void* a = nullptr;
+        cudaError_t e = cudaMalloc(&a, ctx->arena_need);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(ctx, LENIA_ENOMEM, "device allocation of %zu bytes failed: %s", ctx->arena_need,
+                        cudaGetErrorString(e));
+        }
+        ctx->allocs.push_back(a);
+        ctx->arena = (char*)a;
+    }
+    if ((rc0 = world_buffers())) return rc0;
+    // kernel spectra in FP64 on the host, in parallel across (world, kernel) pairs
+    std::vector<std::pair<int, int>> jobs;
+    size_t khat_total = 0;
+    std::vector<size_t> khat_off(nw + 1, 0);
+    for (int i = 0; i < nw; i++) {
+        const LeniaWorldDesc& d = ctx->desc[i];
+        khat_off[i] = khat_total;
+        khat_total += (size_t)(d.width / 2 + 1) * (d.height / 2 + 1) * d.nkernels;
+        for (uint32_t k = 0; k < d.nkernels; k++) jobs.push_back({i, (int)k});
+    }
+    std::vector<float> khat_host(khat_total, 0.0f);
+    {
+        const unsigned nth = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        std::atomic<size_t> next(0);
+        auto worker = [&]() {
+            for (size_t j = next++; j < jobs.size(); j = next++) {
+                const LeniaWorldDesc& d = ctx->desc[jobs[j].first];
+                const size_t khn = (size_t)(d.width / 2 + 1) * (d.height / 2 + 1);
+                compute_khat(d.kernels[jobs[j].second], d.width, d.height, d.height / 2 + 1,
+                             khat_host.data() + khat_off[jobs[j].first] + khn * jobs[j].second, jobs.size() < nth);
+            }
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nth && t < jobs.size(); t++) th.emplace_back(worker);
+        worker();
+        for (auto& t : th) t.join();
+    }
     for (int i = 0; i < nw; i++) {
         const LeniaWorldDesc& d = ctx->desc[i];
         DevWorld& w = ctx->hw[i];
-        memset(&w, 0, sizeof(w));
         w.W = d.width;
         w.H = d.height;
         w.C = d.channels;
@@ -356,30 +433,24 @@ int setup_fused(LeniaCtx* ctx) {
         w.rule = d.rule;
         w.dt = d.dt;
         w.HQ = d.height / 2 + 1;
-        const size_t cells = (size_t)w.W * w.H;
-        int rc;
-        if ((rc = dalloc(ctx, &w.state, cells * w.C))) return rc;
-        if ((rc = dalloc(ctx, &w.spec, spec_elems(w.W, w.H) * w.C))) return rc;
-        if (w.C == 1 && w.K == 1) w.conv = w.spec;
-        else if ((rc = dalloc(ctx, &w.conv, spec_elems(w.W, w.H) * w.K))) return rc;
-        float* kh;
-        const size_t khn = (size_t)(w.W / 2 + 1) * w.HQ;
-        if ((rc = dalloc(ctx, &kh, khn * w.K))) return rc;
-        std::vector<float> host(khn * w.K, 0.0f);
-        for (int k = 0; k < w.K; k++) {
+        w.u_out = nullptr;
+        for (uint32_t k = 0; k < d.nkernels; k++) {
             const LeniaKernel& kk = d.kernels[k];
             w.kern[k].src = kk.src;
             w.kern[k].dst = kk.dst;
             w.kern[k].mu = kk.mu;
             w.kern[k].sigma = kk.sigma;
             w.kern[k].weight = kk.weight;
-            compute_khat(kk, w.W, w.H, w.HQ, host.data() + k * khn);
         }
-        CK(cudaMemcpy(kh, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice));
-        w.khat = kh;
-        CK(cudaMemset(w.state, 0, cells * w.C * sizeof(float)));
-        CK(cudaMemset(w.spec, 0, spec_elems(w.W, w.H) * w.C * sizeof(float2)));
     }
+    CK(cudaMemsetAsync(ctx->arena, 0, ctx->arena_need, ctx->stream));
+    for (int i = 0; i < nw; i++) {
+        const LeniaWorldDesc& d = ctx->desc[i];
+        const size_t khn = (size_t)(d.width / 2 + 1) * (d.height / 2 + 1) * d.nkernels;
+        CK(cudaMemcpyAsync((float*)ctx->hw[i].khat, khat_host.data() + khat_off[i], khn * sizeof(float),
+                           cudaMemcpyHostToDevice, ctx->stream));
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
     int rc;
     if ((rc = dalloc(ctx, &ctx->d_worlds, nw))) return rc;
     CK(cudaMemcpy(ctx->d_worlds, ctx->hw.data(), nw * sizeof(DevWorld), cudaMemcpyHostToDevice));

@@ -177,6 +177,30 @@ LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float*
 LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, const float* khat, float mu,
                                  float sigma, float dt, uint32_t steps, void* stream);
 
+/* ------------------------------------------------------------------------------------------
+ * Learned screen proposer: an MLP 16 -> 256 -> 256 -> 3 (ReLU) in BF16 with FP32 accumulation,
+ * FP32 master weights and Adam, trained by this library's own forward and backward kernels.
+ * Inputs are 16 features of a world's kernel and growth parameters; outputs are
+ * P(survives), P(moves), P(explodes) as judged by the simulator.  The reference has no learned
+ * component: its world screen samples parameters uniformly (scripts/life_screen.py:143-179).
+ * Parameters are one float32 vector: W1 [256x16], b1 [256], W2 [256x256], b2 [256], W3 [3x256],
+ * b3 [3] (row-major, output index first). */
+typedef struct LeniaMlp LeniaMlp;
+LENIA_API int lenia_mlp_create(uint32_t seed, uint32_t max_batch, LeniaMlp** out);
+LENIA_API int lenia_mlp_destroy(LeniaMlp* mlp);
+LENIA_API int lenia_mlp_param_count(uint32_t* count);
+LENIA_API int lenia_mlp_set_params(LeniaMlp* mlp, const float* host, size_t count);
+LENIA_API int lenia_mlp_get_params(LeniaMlp* mlp, float* host, size_t count);
+/* Gradients of the mean binary cross-entropy over batch x 3 labels (x: batch x 16, y: batch x 3
+ * in {0,1}) into grads (param_count floats), without updating the weights. */
+LENIA_API int lenia_mlp_gradients(LeniaMlp* mlp, const float* x, const float* y, uint32_t batch, float* grads,
+                                  float* loss);
+/* One Adam step (beta 0.9 / 0.999) on one batch; returns the batch's mean loss. */
+LENIA_API int lenia_mlp_train_step(LeniaMlp* mlp, const float* x, const float* y, uint32_t batch, float lr,
+                                   float* loss);
+/* Sigmoid outputs for `count` rows of features (count x 3 floats). */
+LENIA_API int lenia_mlp_predict(LeniaMlp* mlp, const float* x, uint32_t count, float* probs);
+
 /* Event-timed average device time of the dominant launches of one step, in milliseconds:
  * out[0] = column passes, out[1] = row passes, out[2] = whole step.  Runs `steps` steps. */
 LENIA_API int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3);

@@ -20,6 +20,21 @@ import numpy as np
 
 from . import build as _build
 
+try:  # multi-threaded float64 FFTs when scipy is present; numpy's otherwise (same results)
+    import scipy.fft as _sfft
+
+    def _rfft2(a):
+        return _sfft.rfft2(a, workers=-1)
+
+    def _irfft2(a, s):
+        return _sfft.irfft2(a, s=s, workers=-1)
+except ImportError:  # pragma: no cover
+    def _rfft2(a):
+        return np.fft.rfft2(a)
+
+    def _irfft2(a, s):
+        return np.fft.irfft2(a, s=s)
+
 SHAPE_LENIA, SHAPE_SL_INNER, SHAPE_SL_OUTER, SHAPE_RING = 0, 1, 2, 3
 RULE_LENIA, RULE_SMOOTHLIFE, RULE_MNCA = 0, 1, 2
 
@@ -202,7 +217,7 @@ def fp64_kernel_spatial(w, h, k):
 def fp64_khat(w, h, k):
     """Real, even kernel spectrum (h, w//2+1) in float64.  The imaginary part is zero up to
     rounding because the min-image kernel is even in both axes."""
-    return np.fft.rfft2(fp64_kernel_spatial(w, h, k)).real
+    return _rfft2(fp64_kernel_spatial(w, h, k)).real
 
 
 def fp64_khats(world):
@@ -219,8 +234,8 @@ def fp64_convolve(world, state, khats=None):
     w, h = world.width, world.height
     khats = fp64_khats(world) if khats is None else khats
     st = np.asarray(state, np.float64).reshape(world.channels, h, w)
-    specs = [np.fft.rfft2(st[c]) for c in range(world.channels)]
-    return np.stack([np.fft.irfft2(specs[int(k.src)] * khats[i], s=(h, w))
+    specs = [_rfft2(st[c]) for c in range(world.channels)]
+    return np.stack([_irfft2(specs[int(k.src)] * khats[i], s=(h, w))
                      for i, k in enumerate(world.kernels)])
 
 
