@@ -26,7 +26,10 @@ EXPORTS = [
     "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_step_noalloc",
     "lenia_mlp_create", "lenia_mlp_destroy", "lenia_mlp_param_count", "lenia_mlp_set_params",
     "lenia_mlp_get_params", "lenia_mlp_gradients", "lenia_mlp_train_step", "lenia_mlp_predict",
+    "lenia_seed_rule", "lenia_render",
 ]
+SEED_SL_DISCS, SEED_MNCA_BLOCKS = 1, 2
+PALETTE_LENIA, PALETTE_SMOOTHLIFE, PALETTE_MNCA = 0, 1, 2
 
 
 class LeniaKernel(ctypes.Structure):
@@ -83,6 +86,8 @@ def _declare(L):
         "lenia_kernel_spectrum": [ctypes.POINTER(LeniaKernel), u32, u32, _c_float_p, sz],
         "lenia_tc_selftest": [i32, i32, i32, _c_float_p, _c_float_p, _c_float_p],
         "lenia_step_noalloc": [vp, u32, u32, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, u32, vp],
+        "lenia_seed_rule": [vp, i32, u32, i32],
+        "lenia_render": [vp, i32, i32, ctypes.c_float, ctypes.c_float, ctypes.c_float, u32, u32, u32, i32, vp],
         "lenia_mlp_create": [u32, u32, ctypes.POINTER(vp)],
         "lenia_mlp_destroy": [vp],
         "lenia_mlp_param_count": [ctypes.POINTER(u32)],

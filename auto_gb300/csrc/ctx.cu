@@ -789,6 +789,39 @@ int lenia_seed_tiles(LeniaCtx* ctx, int32_t world, uint32_t seed, const float* p
     return refresh_spectrum(ctx, world);
 }
 
+int lenia_seed_rule(LeniaCtx* ctx, int32_t world, uint32_t seed, int32_t kind) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    if (kind != LENIA_SEED_SL_DISCS && kind != LENIA_SEED_MNCA_BLOCKS) return fail(ctx, LENIA_EINVAL, "unknown seed %d", kind);
+    const LeniaWorldDesc& d = ctx->desc[world];
+    for (uint32_t c = 0; c < d.channels; c++)
+        launch_seed_rule(state_ptr(ctx, world) + (size_t)c * d.width * d.height, d.width, d.height, seed + c, kind,
+                         ctx->stream);
+    CK(cudaGetLastError());
+    return refresh_spectrum(ctx, world);
+}
+
+int lenia_render(LeniaCtx* ctx, int32_t world, int32_t channel, float origin_x, float origin_y, float scale,
+                 uint32_t samples, uint32_t out_w, uint32_t out_h, int32_t palette, uint8_t* rgba) {
+    if (!ctx) return LENIA_EINVAL;
+    if (world_from_ctx(ctx, world)) return fail(ctx, LENIA_EINVAL, "no world %d", world);
+    const LeniaWorldDesc& d = ctx->desc[world];
+    if (channel < 0 || channel >= (int)d.channels) return fail(ctx, LENIA_EINVAL, "no channel %d", channel);
+    if (!rgba || out_w < 1 || out_h < 1 || out_w > 16384 || out_h > 16384 || samples < 1 || samples > 16 ||
+        !(scale > 0.0f) || palette < 0 || palette > 2)
+        return fail(ctx, LENIA_EINVAL, "render: bad output size, samples, scale or palette");
+    uchar4* dev = nullptr;
+    const size_t bytes = (size_t)out_w * out_h * 4;
+    CK(cudaMallocAsync((void**)&dev, bytes, ctx->stream));
+    launch_render(state_ptr(ctx, world) + (size_t)channel * d.width * d.height, d.width, d.height, origin_x, origin_y,
+                  scale, (int)samples, (int)out_w, (int)out_h, palette, dev, ctx->stream);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(rgba, dev, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaFreeAsync(dev, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
 int lenia_cells_per_step(const LeniaCtx* ctx, uint64_t* cells) {
     if (!ctx || !cells) return LENIA_EINVAL;
     uint64_t n = 0;

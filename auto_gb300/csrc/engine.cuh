@@ -62,6 +62,9 @@ void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* 
 void launch_seed_tiles(float* state, int W, int H, uint32_t seed, const float* pattern, int pw, int ph,
                        int spacing, cudaStream_t s);
 void launch_world_stats(const DevWorld* worlds, int nworlds, float* out, cudaStream_t s);
+void launch_seed_rule(float* state, int W, int H, uint32_t seed, int kind, cudaStream_t s);
+void launch_render(const float* state, int W, int H, float ox, float oy, float scale, int n, int out_w, int out_h,
+                   int palette, uchar4* out, cudaStream_t s);
 
 // The message lenia_last_error(NULL) returns on this thread (calls that have no context).
 void set_thread_error(const std::string& msg);

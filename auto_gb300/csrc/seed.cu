@@ -58,6 +58,73 @@ __global__ void seed_tiles_kernel(float* state, int W, int H, uint32_t seed, con
     }
 }
 
+// The reference's other seeders: SmoothLife's scattered discs (spectral.rs:385-395) and MNCA's
+// random 3x3 blocks (spectral.rs:456-460).
+__global__ void seed_rule_kernel(float* state, int W, int H, uint32_t seed, int kind) {
+    const size_t n = (size_t)W * H;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t x = (uint32_t)(i % W), y = (uint32_t)(i / W);
+        float v = 0.0f;
+        if (kind == LENIA_SEED_SL_DISCS) {
+            const uint32_t tile = 96u;
+            const uint32_t c = rand3(x / tile, y / tile, seed);
+            if ((c & 1u) != 0u) {
+                const float dx = (float)(x % tile) - (float)tile / 2.0f, dy = (float)(y % tile) - (float)tile / 2.0f;
+                v = (dx * dx + dy * dy < 24.0f * 24.0f) ? 1.0f : 0.0f;
+            }
+        } else {
+            v = unit_f(rand3(x / 3u, y / 3u, seed)) < 0.32f ? 1.0f : 0.0f;
+        }
+        state[i] = v;
+    }
+}
+
+// sim.rs:17-41 (view_main) with the shade functions of spectral.rs:347-349, 410-412, 475-477 and
+// the ramp/mix3 helpers of program.rs:148-157: an n x n supersampled average in light (squares,
+// then the square root) of the state's colours, outside the world black; rgba8 output.
+__device__ __forceinline__ float3 mix3f(float3 a, float3 b, float t) {
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    return make_float3(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t);
+}
+__device__ float3 shade(float t, int palette) {
+    if (palette == LENIA_PALETTE_MNCA) return mix3f(make_float3(0.02f, 0.02f, 0.07f), make_float3(0.75f, 0.95f, 0.85f), t);
+    float3 c[5];
+    if (palette == LENIA_PALETTE_SMOOTHLIFE) {
+        c[0] = make_float3(0.02f, 0.02f, 0.03f); c[1] = make_float3(0.3f, 0.07f, 0.25f); c[2] = make_float3(0.85f, 0.25f, 0.25f);
+        c[3] = make_float3(0.98f, 0.7f, 0.3f); c[4] = make_float3(1.0f, 0.98f, 0.85f);
+    } else {
+        c[0] = make_float3(0.01f, 0.01f, 0.05f); c[1] = make_float3(0.08f, 0.12f, 0.45f); c[2] = make_float3(0.1f, 0.6f, 0.7f);
+        c[3] = make_float3(0.95f, 0.85f, 0.4f); c[4] = make_float3(1.0f, 0.98f, 0.9f);
+    }
+    const float s = fminf(fmaxf(t, 0.0f), 1.0f) * 4.0f;
+    if (s < 1.0f) return mix3f(c[0], c[1], s);
+    if (s < 2.0f) return mix3f(c[1], c[2], s - 1.0f);
+    if (s < 3.0f) return mix3f(c[2], c[3], s - 2.0f);
+    return mix3f(c[3], c[4], s - 3.0f);
+}
+
+__global__ void render_kernel(const float* __restrict__ state, int W, int H, float ox, float oy, float scale, int n,
+                              int out_w, int out_h, int palette, uchar4* __restrict__ out) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= out_w || py >= out_h) return;
+    float ar = 0.f, ag = 0.f, ab = 0.f;
+    for (int sy = 0; sy < n; sy++)
+        for (int sx = 0; sx < n; sx++) {
+            const float subx = ((float)sx + 0.5f) / (float)n, suby = ((float)sy + 0.5f) / (float)n;
+            const float x = ox + ((float)px + subx) * scale, y = oy + ((float)py + suby) * scale;
+            if (x >= 0.0f && y >= 0.0f && x < (float)W && y < (float)H) {
+                const int cx = min((int)x, W - 1), cy = min((int)y, H - 1);
+                const float3 c = shade(state[(size_t)cy * W + cx], palette);
+                ar += c.x * c.x;
+                ag += c.y * c.y;
+                ab += c.z * c.z;
+            }
+        }
+    const float inv = 1.0f / (float)(n * n);
+    auto u8 = [](float v) { return (unsigned char)__float2int_rn(fminf(fmaxf(v, 0.0f), 1.0f) * 255.0f); };
+    out[(size_t)py * out_w + px] = make_uchar4(u8(sqrtf(ar * inv)), u8(sqrtf(ag * inv)), u8(sqrtf(ab * inv)), 255);
+}
+
 // Mass of channel 0 and toroidal centroid (circular mean per axis), one CTA per world.
 __global__ void world_stats_kernel(const DevWorld* __restrict__ worlds, float* out) {
     const DevWorld& wd = worlds[blockIdx.x];
@@ -108,6 +175,16 @@ void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* 
 void launch_seed_tiles(float* state, int W, int H, uint32_t seed, const float* pattern, int pw, int ph, int spacing,
                        cudaStream_t s) {
     seed_tiles_kernel<<<grid_for((size_t)W * H), 256, 0, s>>>(state, W, H, seed, pattern, pw, ph, spacing);
+}
+
+void launch_seed_rule(float* state, int W, int H, uint32_t seed, int kind, cudaStream_t s) {
+    seed_rule_kernel<<<grid_for((size_t)W * H), 256, 0, s>>>(state, W, H, seed, kind);
+}
+
+void launch_render(const float* state, int W, int H, float ox, float oy, float scale, int n, int out_w, int out_h,
+                   int palette, uchar4* out, cudaStream_t s) {
+    const dim3 blk(16, 16), grd((out_w + 15) / 16, (out_h + 15) / 16);
+    render_kernel<<<grd, blk, 0, s>>>(state, W, H, ox, oy, scale, n, out_w, out_h, palette, out);
 }
 
 void launch_world_stats(const DevWorld* worlds, int nworlds, float* out, cudaStream_t s) {

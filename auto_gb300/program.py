@@ -51,7 +51,7 @@ class Kernel:
 @dataclass
 class Seed:
     """How a world's initial state is made on the device (the reference's seed pass)."""
-    kind: str = "none"                    # "none" | "patches" | "tiles"
+    kind: str = "none"                    # "none" | "patches" | "tiles" | "discs" | "blocks"
     patches: List[Tuple[int, int, int, int]] = field(default_factory=list)
     spacing: int = 64
     pattern: Optional[object] = None      # 2-D float array for "tiles"
@@ -105,7 +105,7 @@ def lenia(w: int, h: int, radius: float = 13.0, pattern=None) -> World:
 def smoothlife(w: int, h: int, ra: float = 21.0) -> World:
     """spectral.rs:355-415: inner disc ra/3 and outer ring, Rafler's transition."""
     return World(w, h, [Kernel(SHAPE_SL_INNER, ra), Kernel(SHAPE_SL_OUTER, ra)], rule=RULE_SMOOTHLIFE,
-                 id="smoothlife")
+                 id="smoothlife", seed=Seed("discs"))
 
 
 MNCA_RINGS = (12.0, 18.0, 3.0, 8.0)  # spectral.rs:423
@@ -114,7 +114,7 @@ MNCA_RINGS = (12.0, 18.0, 3.0, 8.0)  # spectral.rs:423
 def mnca_shaped(w: int, h: int, rings: Sequence[float] = MNCA_RINGS) -> World:
     """spectral.rs:426-480: two hard rings [inner0, outer0, inner1, outer1]."""
     return World(w, h, [Kernel(SHAPE_RING, lo=rings[0], hi=rings[1]), Kernel(SHAPE_RING, lo=rings[2], hi=rings[3])],
-                 rule=RULE_MNCA, id="mnca")
+                 rule=RULE_MNCA, id="mnca", seed=Seed("blocks"))
 
 
 def mnca(w: int, h: int) -> World:

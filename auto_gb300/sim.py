@@ -60,6 +60,10 @@ class Sim:
                 self.seed_patches(i, self.seed, s.patches)
             elif s.kind == "tiles" and s.pattern is not None:
                 self.seed_tiles(i, self.seed, s.pattern, s.spacing)
+            elif s.kind == "discs":
+                self.seed_rule(i, self.seed, _lib.SEED_SL_DISCS)
+            elif s.kind == "blocks":
+                self.seed_rule(i, self.seed, _lib.SEED_MNCA_BLOCKS)
 
     @property
     def tick(self) -> int:
@@ -112,6 +116,18 @@ class Sim:
     def seed_tiles(self, world: int, seed: int, pattern, spacing: int = 64):
         pat = np.ascontiguousarray(pattern, np.float32)
         self._check(self._L.lenia_seed_tiles(self._ctx, world, seed, fptr(pat), pat.shape[1], pat.shape[0], spacing))
+
+    def seed_rule(self, world: int, seed: int, kind: int):
+        """SmoothLife discs (_lib.SEED_SL_DISCS) or MNCA blocks (_lib.SEED_MNCA_BLOCKS)."""
+        self._check(self._L.lenia_seed_rule(self._ctx, world, seed, kind))
+
+    def render(self, world: int = 0, out_w: int = 256, out_h: int = 256, origin=(0.0, 0.0), scale: float = 1.0,
+               samples: int = 2, palette: int = 0, channel: int = 0) -> np.ndarray:
+        """Headless view (sim.rs:17-41): (out_h, out_w, 4) uint8 RGBA."""
+        out = np.zeros((out_h, out_w, 4), np.uint8)
+        self._check(self._L.lenia_render(self._ctx, world, channel, float(origin[0]), float(origin[1]), float(scale),
+                                         samples, out_w, out_h, palette, out.ctypes.data_as(ctypes.c_void_p)))
+        return out
 
     def u_field(self, world: int = 0, kernel: int = 0) -> np.ndarray:
         w = self.worlds[world]

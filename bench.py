@@ -16,6 +16,7 @@ Rust + WGSL on Vulkan and cannot run here) on all host cores, on the same worklo
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -36,7 +37,7 @@ PUBLISHED_REF = {"lenia_4096x4096_R13": 3.174e8, "hardware": "AMD RX 7900 XT (wg
                  "source": "results/gpu.jsonl:81"}
 
 
-def parse():
+def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=10)
@@ -48,23 +49,29 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--autotune", action="store_true")
-    return p.parse_args()
+    p.add_argument("--jsonl", default=None, help="also append a sample in the reference's results/*.jsonl format")
+    return p.parse_args(argv)
 
 
 # ----------------------------------------------------------------------------- distributed plumbing
 
 class Dist:
+    """torchrun plumbing: barrier and max over ranks (NCCL on GPUs, gloo without)."""
+
     def __init__(self):
         self.world = int(os.environ.get("WORLD_SIZE", "1"))
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.torch = None
+        self.device = "cpu"
         if self.world > 1:
             import torch
             import torch.distributed as dist
             self.torch = torch
-            torch.cuda.set_device(self.local)
-            dist.init_process_group("nccl")
+            if torch.cuda.is_available():
+                torch.cuda.set_device(self.local)
+                self.device = "cuda"
+            dist.init_process_group("nccl" if self.device == "cuda" else "gloo")
 
     def barrier(self):
         if self.world > 1:
@@ -73,8 +80,15 @@ class Dist:
     def max(self, v):
         if self.world == 1:
             return v
-        t = self.torch.tensor([v], dtype=self.torch.float64, device="cuda")
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.device)
         self.torch.distributed.all_reduce(t, op=self.torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v):
+        if self.world == 1:
+            return v
+        t = self.torch.tensor([float(v)], dtype=self.torch.float64, device=self.device)
+        self.torch.distributed.all_reduce(t, op=self.torch.distributed.ReduceOp.SUM)
         return float(t.item())
 
     def close(self):
@@ -159,6 +173,20 @@ def workload(name):
         return [configs.multichannel()], [configs.SEED_MULTI], {"workload": "3 channels x 1024^2, 9 kernels"}
     ws = configs.batched(384)
     return ws, list(range(len(ws))), {"workload": "384 uneven worlds, sides 128..1024, per-world R/mu/sigma/dt"}
+
+
+def shard(worlds, rank, nranks):
+    """Indices of the worlds rank `rank` runs: largest first, each to the least-loaded rank, so
+    every rank gets a near-equal share of the cells (deterministic on every rank)."""
+    load = [0] * nranks
+    mine = []
+    order = sorted(range(len(worlds)), key=lambda i: (-worlds[i].cells_per_step, i))
+    for i in order:
+        r = min(range(nranks), key=lambda k: (load[k], k))
+        load[r] += worlds[i].cells_per_step
+        if r == rank:
+            mine.append(i)
+    return sorted(mine)
 
 
 def seed_all(sim, worlds, seeds):
@@ -251,6 +279,12 @@ def run_ours(args, dist):
     from auto_gb300 import Sim
 
     worlds, seeds, cfg = workload(args.config)
+    scaling = "weak"
+    if dist.world > 1 and len(worlds) > 1:
+        # several worlds: split them across ranks (total work fixed); one world: every rank a replica
+        idx = shard(worlds, dist.rank, dist.world)
+        worlds, seeds = [worlds[i] for i in idx], [seeds[i] for i in idx]
+        scaling = "strong"
     sim = Sim(worlds, seed=0, path=args.path)
     seed_all(sim, worlds, seeds)
     if args.autotune:
@@ -271,7 +305,8 @@ def run_ours(args, dist):
     device_sync()
     clk = clocks.stop()
     ms = dist.max(ms)
-    value = dist.world * cells * G * args.steps / (ms * 1e-3)
+    total_cells = dist.sum(cells)
+    value = total_cells * G * args.steps / (ms * 1e-3)
     ms_per_gen = ms / (args.steps * G)
 
     # per-kernel breakdown (event-timed launches on the engine stream, right after the timed region)
@@ -327,7 +362,7 @@ def run_ours(args, dist):
         device_sync()
         t_e2e = dist.max(time.perf_counter() - t0)
         nbytes = sum(a.nbytes for _, a in host)
-        e2e = {"value": dist.world * cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes,
+        e2e = {"value": total_cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "gens_per_step": G}
 
     cpu = None
@@ -339,14 +374,53 @@ def run_ours(args, dist):
         cfg.update({"path": args.path, "gens_per_step": G, "cells_per_generation": cells, "worlds": len(worlds),
                     "l2": "no flush: per-generation working set (state + half-spectrum + kernel spectrum) "
                           "exceeds the 129 MB L2" if cells >= 4096 * 4096 else "no flush",
-                    "parallelism": "replicas" if dist.world > 1 else "single"})
+                    "parallelism": ("replicas" if scaling == "weak" else "worlds sharded") if dist.world > 1
+                    else "single"})
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
-               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches_per_gen * G * args.steps,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
         print(json.dumps(out))
+    if args.jsonl and dist.rank == 0:
+        append_reference_sample(args.jsonl, sim, worlds, cfg, args.path)
     sim.close()
+
+
+def append_reference_sample(path, sim, worlds, cfg, impl_path, seconds=2.0, warmup=32):
+    """One record in the reference's results/*.jsonl format (crates/auto-cli/src/bench.rs:39-55),
+    measured its way (bench.rs:112-166): warm up, grow the batch until one submit takes >= 20 ms,
+    then run batches for `seconds` and keep the median rate and the 10-90% spread."""
+    sim.step(warmup)
+    sim.wait()
+    batch = 1
+    while True:
+        t = time.perf_counter()
+        sim.step(batch)
+        sim.wait()
+        dt = time.perf_counter() - t
+        if dt >= 0.02 or batch >= 1 << 16:
+            break
+        want = int(math.ceil(batch * 0.025 / max(dt, 1e-5)))
+        batch = min(max(want, batch + 1), batch * 8, 1 << 16)
+    rates = []
+    start = time.perf_counter()
+    while time.perf_counter() - start < seconds or len(rates) < 3:
+        t = time.perf_counter()
+        sim.step(batch)
+        sim.wait()
+        rates.append(batch / (time.perf_counter() - t))
+    rates.sort()
+    median = rates[len(rates) // 2]
+    spread = (rates[len(rates) * 9 // 10] - rates[len(rates) // 10]) / median
+    cells = sim.cells_per_step
+    w0 = worlds[0]
+    rec = {"id": w0.id if len(worlds) == 1 else "batched", "tag": impl_path, "adapter": "NVIDIA GB300 (CUDA, sm_103a)",
+           "checks": "Safe", "width": w0.width, "height": w0.height, "cells": cells, "memory_bytes": sim.memory_bytes,
+           "steps_per_second": median, "generations_per_second": median, "cells_per_second": median * cells,
+           "batch_steps": batch, "batches": len(rates), "spread": spread}
+    with open(path, "a") as f:
+        f.write(json.dumps(rec) + "\n")
 
 
 def main():

@@ -126,6 +126,24 @@ LENIA_API int lenia_seed_tiles(LeniaCtx* ctx, int32_t world, uint32_t seed, cons
 LENIA_API int lenia_seed_patches(LeniaCtx* ctx, int32_t world, uint32_t seed, const int32_t* patches_xywh,
                        int32_t npatches);
 
+/* The reference's other seed passes, on the device: SmoothLife's scattered discs of radius 24 in
+ * 96-cell tiles (spectral.rs:385-395) and MNCA's random 3x3 blocks with density 0.32
+ * (spectral.rs:456-460).  Channel c uses seed + c. */
+#define LENIA_SEED_SL_DISCS 1
+#define LENIA_SEED_MNCA_BLOCKS 2
+LENIA_API int lenia_seed_rule(LeniaCtx* ctx, int32_t world, uint32_t seed, int32_t kind);
+
+/* Headless view (sim.rs:17-41): out_w x out_h RGBA8 pixels of one channel, each the average in
+ * light of samples x samples sub-pixel colours at world position origin + (pixel + sub) * scale,
+ * black outside the world, with the reference's palettes (spectral.rs:347-349, 410-412, 475-477).
+ * No window, swapchain or graphics API: the pixels are written to a host buffer (4*out_w*out_h
+ * bytes). */
+#define LENIA_PALETTE_LENIA 0
+#define LENIA_PALETTE_SMOOTHLIFE 1
+#define LENIA_PALETTE_MNCA 2
+LENIA_API int lenia_render(LeniaCtx* ctx, int32_t world, int32_t channel, float origin_x, float origin_y, float scale,
+                           uint32_t samples, uint32_t out_w, uint32_t out_h, int32_t palette, uint8_t* rgba);
+
 /* Program::cells_per_step (program.rs:116-119) summed over worlds and channels. */
 LENIA_API int lenia_cells_per_step(const LeniaCtx* ctx, uint64_t* cells);
 /* Program::total_bytes (program.rs:122-129): device bytes this context holds. */

@@ -19,6 +19,9 @@
  *   - SmoothLife shapes and update ....... spectral.rs:355-407
  *   - MNCA rings and update .............. spectral.rs:426-472
  *   - Orbium tile seeding ................ spectral.rs:313-335 (pattern supplied by caller)
+ *   - SmoothLife and MNCA seeds .......... spectral.rs:385-395, 456-460
+ *   - view pass (colour ramps) ........... sim.rs:17-41, program.rs:148-157,
+ *                                          spectral.rs:347-349, 410-412, 475-477
  *   - size guards ........................ spectral.rs:103-116
  *
  * The multi-shell kernel (beta shells) has no reference code: it follows Chan's
@@ -420,4 +423,75 @@ void orc_seed_patches(int w, int h, uint32_t seed, const int32_t* patches, int n
                 out[(size_t)y * w + x] = orc_unit_f(orc_rand3((uint32_t)x, (uint32_t)y, seed));
             }
     }
+}
+
+/* spectral.rs:385-395: SmoothLife's seed, discs of radius 24 in the 96-cell tiles whose
+ * rand3(tx, ty, seed) is odd. */
+void orc_seed_sl_discs(int w, int h, uint32_t seed, float* out) {
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const uint32_t tile = 96u;
+            uint32_t c = orc_rand3((uint32_t)x / tile, (uint32_t)y / tile, seed);
+            float v = 0.0f;
+            if ((c & 1u) != 0u) {
+                float dx = (float)((uint32_t)x % tile) - (float)tile / 2.0f;
+                float dy = (float)((uint32_t)y % tile) - (float)tile / 2.0f;
+                v = (dx * dx + dy * dy < 24.0f * 24.0f) ? 1.0f : 0.0f;
+            }
+            out[(size_t)y * w + x] = v;
+        }
+}
+
+/* spectral.rs:456-460: MNCA's seed, 3x3 blocks set where unit_f(rand3(x/3, y/3, seed)) < 0.32. */
+void orc_seed_mnca_blocks(int w, int h, uint32_t seed, float* out) {
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++)
+            out[(size_t)y * w + x] = orc_unit_f(orc_rand3((uint32_t)x / 3u, (uint32_t)y / 3u, seed)) < 0.32f ? 1.0f : 0.0f;
+}
+
+/* program.rs:148-157 (mix3, ramp) and the shade functions of spectral.rs:347-349, 410-412, 475-477 */
+static void mix3(const float* a, const float* b, float t, float* o) {
+    t = t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t);
+    for (int i = 0; i < 3; i++) o[i] = a[i] + (b[i] - a[i]) * t;
+}
+static void shade(float t, int palette, float* o) {
+    static const float L[5][3] = {{0.01f, 0.01f, 0.05f}, {0.08f, 0.12f, 0.45f}, {0.1f, 0.6f, 0.7f},
+                                  {0.95f, 0.85f, 0.4f}, {1.0f, 0.98f, 0.9f}};
+    static const float S[5][3] = {{0.02f, 0.02f, 0.03f}, {0.3f, 0.07f, 0.25f}, {0.85f, 0.25f, 0.25f},
+                                  {0.98f, 0.7f, 0.3f}, {1.0f, 0.98f, 0.85f}};
+    static const float M[2][3] = {{0.02f, 0.02f, 0.07f}, {0.75f, 0.95f, 0.85f}};
+    if (palette == 2) { mix3(M[0], M[1], t, o); return; }
+    const float (*c)[3] = palette == 1 ? S : L;
+    float s = (t < 0.0f ? 0.0f : (t > 1.0f ? 1.0f : t)) * 4.0f;
+    if (s < 1.0f) mix3(c[0], c[1], s, o);
+    else if (s < 2.0f) mix3(c[1], c[2], s - 1.0f, o);
+    else if (s < 3.0f) mix3(c[2], c[3], s - 2.0f, o);
+    else mix3(c[3], c[4], s - 3.0f, o);
+}
+
+/* crates/auto-core/src/sim.rs:17-41 (view_main): n x n supersampling, averaging c*c, then sqrt. */
+void orc_render(const float* state, int w, int h, float ox, float oy, float scale, int n, int out_w, int out_h,
+                int palette, uint8_t* out) {
+    for (int py = 0; py < out_h; py++)
+        for (int px = 0; px < out_w; px++) {
+            float acc[3] = {0.0f, 0.0f, 0.0f};
+            for (int sy = 0; sy < n; sy++)
+                for (int sx = 0; sx < n; sx++) {
+                    float subx = ((float)sx + 0.5f) / (float)n, suby = ((float)sy + 0.5f) / (float)n;
+                    float x = ox + ((float)px + subx) * scale, y = oy + ((float)py + suby) * scale;
+                    if (x >= 0.0f && y >= 0.0f && x < (float)w && y < (float)h) {
+                        int cx = (int)x < w - 1 ? (int)x : w - 1, cy = (int)y < h - 1 ? (int)y : h - 1;
+                        float c[3];
+                        shade(state[(size_t)cy * w + cx], palette, c);
+                        for (int i = 0; i < 3; i++) acc[i] += c[i] * c[i];
+                    }
+                }
+            uint8_t* o = out + 4 * ((size_t)py * out_w + px);
+            for (int i = 0; i < 3; i++) {
+                float v = sqrtf(acc[i] / (float)(n * n));
+                v = v < 0.0f ? 0.0f : (v > 1.0f ? 1.0f : v);
+                o[i] = (uint8_t)lrintf(v * 255.0f);
+            }
+            o[3] = 255;
+        }
 }

@@ -96,6 +96,11 @@ class RefF32:
                                      ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
         L.orc_seed_patches.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint32,
                                        ctypes.POINTER(ctypes.c_int32), ctypes.c_int, ctypes.POINTER(ctypes.c_float)]
+        L.orc_seed_sl_discs.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
+        L.orc_seed_mnca_blocks.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.POINTER(ctypes.c_float)]
+        L.orc_render.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                 ctypes.c_float, ctypes.c_float, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_void_p]
         self.threads = threads or (os.cpu_count() or 1)
 
     # RNG (program.rs:140-147)
@@ -158,6 +163,24 @@ class RefF32:
         pat = np.ascontiguousarray(pattern, np.float32)
         out = np.zeros((h, w), np.float32)
         self.lib.orc_seed_tiles(w, h, seed, _fptr(pat), pat.shape[1], pat.shape[0], spacing, _fptr(out))
+        return out
+
+    def seed_sl_discs(self, w, h, seed):
+        out = np.zeros((h, w), np.float32)
+        self.lib.orc_seed_sl_discs(w, h, seed, _fptr(out))
+        return out
+
+    def seed_mnca_blocks(self, w, h, seed):
+        out = np.zeros((h, w), np.float32)
+        self.lib.orc_seed_mnca_blocks(w, h, seed, _fptr(out))
+        return out
+
+    def render(self, state, out_w, out_h, origin=(0.0, 0.0), scale=1.0, samples=2, palette=0):
+        s = np.ascontiguousarray(state, np.float32)
+        h, w = s.shape
+        out = np.zeros((out_h, out_w, 4), np.uint8)
+        self.lib.orc_render(_fptr(s), w, h, float(origin[0]), float(origin[1]), float(scale), samples, out_w, out_h,
+                            palette, out.ctypes.data_as(ctypes.c_void_p))
         return out
 
     def seed_patches(self, w, h, seed, patches):

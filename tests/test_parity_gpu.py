@@ -262,3 +262,26 @@ def test_autotune_keeps_results():
         a.step(10)
         b.step(10)
         assert np.abs(a.read_state(0) - b.read_state(0)).max() < 1e-5
+
+
+@pytest.mark.parametrize("kind,path", [(_lib.SEED_SL_DISCS, "fp32"), (_lib.SEED_MNCA_BLOCKS, "fp32"),
+                                       (_lib.SEED_MNCA_BLOCKS, "radix2")])
+def test_rule_seeds_on_device(ref, kind, path):
+    world = ag.smoothlife(256, 256) if kind == _lib.SEED_SL_DISCS else ag.mnca(256, 256)
+    with Sim(world, seed=7, path=path) as sim:
+        got = sim.read_state(0)[0]
+    want = ref.seed_sl_discs(256, 256, 7) if kind == _lib.SEED_SL_DISCS else ref.seed_mnca_blocks(256, 256, 7)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("palette,samples,scale,origin", [(0, 2, 1.0, (0.0, 0.0)), (1, 3, 2.5, (-10.0, 5.0)),
+                                                          (2, 1, 0.5, (30.0, 40.0))])
+def test_headless_view_matches_oracle(ref, palette, samples, scale, origin):
+    rng = np.random.default_rng(palette)
+    s = rng.random((192, 256), dtype=np.float32)
+    with Sim(ag.World(256, 192, [ag.Kernel(radius=10.0)])) as sim:
+        sim.write_state(0, s)
+        img = sim.render(0, 200, 150, origin=origin, scale=scale, samples=samples, palette=palette)
+    want = ref.render(s, 200, 150, origin=origin, scale=scale, samples=samples, palette=palette)
+    diff = np.abs(img.astype(int) - want.astype(int))
+    assert diff.max() <= 1 and (diff > 0).mean() < 1e-3
