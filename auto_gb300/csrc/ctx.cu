@@ -375,7 +375,7 @@ int setup_fused(LeniaCtx* ctx) {
             if (d.channels == 1 && d.nkernels == 1) w.conv = w.spec;
             else if ((rc = dalloc(ctx, &w.conv, spec_elems(d.width, d.height) * d.nkernels))) return rc;
             float* kh;
-            if ((rc = dalloc(ctx, &kh, (size_t)(d.width / 2 + 1) * (d.height / 2 + 1) * d.nkernels))) return rc;
+            if ((rc = dalloc(ctx, &kh, (size_t)(d.width / 2 + 1) * khat_stride(d.height) * d.nkernels))) return rc;
             w.khat = kh;
         }
         return 0;
@@ -403,7 +403,7 @@ int setup_fused(LeniaCtx* ctx) {
     for (int i = 0; i < nw; i++) {
         const LeniaWorldDesc& d = ctx->desc[i];
         khat_off[i] = khat_total;
-        khat_total += (size_t)(d.width / 2 + 1) * (d.height / 2 + 1) * d.nkernels;
+        khat_total += (size_t)(d.width / 2 + 1) * khat_stride(d.height) * d.nkernels;
         for (uint32_t k = 0; k < d.nkernels; k++) jobs.push_back({i, (int)k});
     }
     std::vector<float> khat_host(khat_total, 0.0f);
@@ -413,8 +413,8 @@ int setup_fused(LeniaCtx* ctx) {
         auto worker = [&]() {
             for (size_t j = next++; j < jobs.size(); j = next++) {
                 const LeniaWorldDesc& d = ctx->desc[jobs[j].first];
-                const size_t khn = (size_t)(d.width / 2 + 1) * (d.height / 2 + 1);
-                compute_khat(d.kernels[jobs[j].second], d.width, d.height, d.height / 2 + 1,
+                const size_t khn = (size_t)(d.width / 2 + 1) * khat_stride(d.height);
+                compute_khat(d.kernels[jobs[j].second], d.width, d.height, khat_stride(d.height),
                              khat_host.data() + khat_off[jobs[j].first] + khn * jobs[j].second, jobs.size() < nth);
             }
         };
@@ -432,7 +432,7 @@ int setup_fused(LeniaCtx* ctx) {
         w.K = d.nkernels;
         w.rule = d.rule;
         w.dt = d.dt;
-        w.HQ = d.height / 2 + 1;
+        w.HQ = khat_stride(d.height);
         w.u_out = nullptr;
         for (uint32_t k = 0; k < d.nkernels; k++) {
             const LeniaKernel& kk = d.kernels[k];
@@ -446,7 +446,7 @@ int setup_fused(LeniaCtx* ctx) {
     CK(cudaMemsetAsync(ctx->arena, 0, ctx->arena_need, ctx->stream));
     for (int i = 0; i < nw; i++) {
         const LeniaWorldDesc& d = ctx->desc[i];
-        const size_t khn = (size_t)(d.width / 2 + 1) * (d.height / 2 + 1) * d.nkernels;
+        const size_t khn = (size_t)(d.width / 2 + 1) * khat_stride(d.height) * d.nkernels;
         CK(cudaMemcpyAsync((float*)ctx->hw[i].khat, khat_host.data() + khat_off[i], khn * sizeof(float),
                            cudaMemcpyHostToDevice, ctx->stream));
     }

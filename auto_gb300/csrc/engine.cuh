@@ -22,7 +22,8 @@ struct DevKernel {
 //                                 column 0 packs the DC column (real part) with the Nyquist
 //                                 column W/2 (imaginary part)
 //   conv  [K][W/(2*TC)][H][TC] float2   per-kernel convolved spectrum (aliases spec when C = K = 1)
-//   khat  [K][W/2+1][HQ] float    real, even kernel spectrum for ky in [0, H/2], times 1/(W*H)
+//   khat  [K][W/2+1][HQ] float    real, even kernel spectrum for ky in [0, H/2], times 1/(W*H);
+//                                 HQ = khat_stride(H) >= H/2+1
 struct DevWorld {
     int W, H, C, K, rule;
     float dt;
@@ -72,5 +73,8 @@ void set_thread_error(const std::string& msg);
 // Tile-layout helpers on the host.
 inline size_t spec_elems(int W, int H) { return (size_t)(W / 2) * H; }
 inline int spec_tiles(int W) { return W / (2 * TC); }
+// Row stride of the kernel spectrum (floats): H/2+1 rounded up to a multiple of 4, so that
+// every row starts 16-byte aligned and can be moved by a bulk copy.
+inline int khat_stride(int H) { return (H / 2 + 1 + 3) / 4 * 4; }
 
 }  // namespace lenia

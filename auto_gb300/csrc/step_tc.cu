@@ -483,8 +483,7 @@ bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, 
     const bool x3 = path == LENIA_PATH_BF16X3;
     int* e = (int*)plan.d_err;
     switch (H) {
-    case 4096: return x3 ? launch_shape<TcShape<64, 64, 2, true>>(fm, worlds, groups, ngroups, tw, e, s)
-                         : launch_shape<TcShape<64, 64, 2, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    case 4096: return launch_col_tc64(x3, fm, worlds, groups, ngroups, tw, e, s);
     case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s)
                          : launch_shape<TcShape<64, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s);
     case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s)
