@@ -129,6 +129,18 @@ __global__ void __launch_bounds__(256, 1)
         mbar_arrive_expect_tx(bar_f, S::FB * S::NOP);
         bulk_g2s(f, fmat, S::FB * S::NOP, bar_f);
     }
+    // Both hand-overs that need a twiddle (A -> B and C -> D) use exp(-2 pi i f j / 4096) with
+    // f = t >> 1 fixed per thread and j in [0, 64) the column index: with j = 8a + b it is
+    // P8[a] * P1[b], two exactly rounded table values and one product.
+    float2 P8[8], P1[8];
+    {
+        const int fidx = t >> 1;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            P1[i] = tw[((fidx * i) & 4095) * (lfft::TWN / 4096)];
+            P8[i] = tw[((fidx * 8 * i) & 4095) * (lfft::TWN / 4096)];
+        }
+    }
     bool ok = mbar_wait(bar_f, 0);
     uint32_t ph_mma = 0, ph_kh = 0;
     const uint32_t fa = smem_u32(f), oa = smem_u32(op);
@@ -161,6 +173,13 @@ __global__ void __launch_bounds__(256, 1)
             bulk_prefetch_l2(nw.spec + nx.chan * (size_t)(nw.W / 2) * S::H + (size_t)nx.tile * S::H * TC,
                              S::H * TC * 8);
         }
+        // kernel-spectrum rows of the first kernel that reads this channel, in flight during the transforms
+        int kfirst = 0;
+        while (kfirst < K && wd.kern[kfirst].src != it.chan) kfirst++;
+        if (t == 0 && kfirst < K) {
+            mbar_arrive_expect_tx(bar_kh, S::KH);
+            bulk_g2s(kh, wd.khat + ((size_t)kfirst * (W / 2 + 1) + (size_t)it.tile * TC) * S::HQ, S::KH, bar_kh);
+        }
         // ---- stage 0: X rows (c, y1) = t, K (re/im, y2), straight from global memory
         {
             const int c = t >> 6, y1 = t & 63;
@@ -186,7 +205,7 @@ __global__ void __launch_bounds__(256, 1)
         // ---- A -> B: lane (k2, ro); twiddle exp(-2 pi i y1 k2 / 4096); X_B row (c, k2), K (ro, y1)
         {
             const int k2 = t >> 1, ro = t & 1;
-#pragma unroll 1
+#pragma unroll
             for (int q = 0; q < 4; q++) {
                 float v[32], o[32];
                 tmem_ld32(t_x + lane_off + 32 * q, v);
@@ -195,7 +214,7 @@ __global__ void __launch_bounds__(256, 1)
                 for (int j = 0; j < 32; j++) {
                     const float p = __shfl_xor_sync(0xffffffffu, v[j], 1);
                     const float re = ro ? p : v[j], im = ro ? v[j] : p;
-                    const float2 w = tw[(((ybase + j) * k2) & 4095) * (lfft::TWN / 4096)];
+                    const float2 w = lfft::cmul(P8[(ybase + j) >> 3], P1[(ybase + j) & 7]);
                     o[j] = ro ? (re * w.y + im * w.x) : (re * w.x - im * w.y);
                 }
                 store32<X3>(op, c * 64 + k2, ro * 64 + ybase, o);
@@ -204,7 +223,7 @@ __global__ void __launch_bounds__(256, 1)
         gemm_wait(t_b, oa, fa);  // GEMM B: D[(c, k2)][(k1, ro)]
         for (int k = 0; k < K && ok; k++) {
             if (wd.kern[k].src != it.chan) continue;
-            if (t == 0) {
+            if (t == 0 && k != kfirst) {
                 mbar_arrive_expect_tx(bar_kh, S::KH);
                 bulk_g2s(kh, wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)it.tile * TC) * S::HQ, S::KH, bar_kh);
             }
@@ -237,7 +256,7 @@ __global__ void __launch_bounds__(256, 1)
             // ---- C -> D: lane (y1, ro); twiddle exp(-2 pi i k2 y1 / 4096); X_D row (c, y1), K (ro, k2)
             {
                 const int y1 = t >> 1, ro = t & 1;
-#pragma unroll 1
+#pragma unroll
                 for (int q = 0; q < 4; q++) {
                     float v[32], o[32];
                     tmem_ld32(t_x + lane_off + 32 * q, v);
@@ -246,24 +265,32 @@ __global__ void __launch_bounds__(256, 1)
                     for (int j = 0; j < 32; j++) {
                         const float p = __shfl_xor_sync(0xffffffffu, v[j], 1);
                         const float re = ro ? p : v[j], im = ro ? v[j] : p;
-                        const float2 w = tw[(((kbase + j) * y1) & 4095) * (lfft::TWN / 4096)];
+                        const float2 w = lfft::cmul(P8[(kbase + j) >> 3], P1[(kbase + j) & 7]);
                         o[j] = ro ? (re * w.y + im * w.x) : (re * w.x - im * w.y);
                     }
                     store32<X3>(op, c * 64 + y1, ro * 64 + kbase, o);
                 }
             }
             gemm_wait(t_x, oa, fa);  // GEMM D: D[(c, y1)][(y2, ro)]
-            // ---- output: lane (c, y1); conjugate; y = y1 + 64 y2, straight to global memory
+            // ---- output: lane (c, y1); conjugate; y = y1 + 64 y2 into the free operand buffer, then one
+            // bulk copy to the convolved-spectrum tile
             {
                 const int c = t >> 6, y1 = t & 63;
-                float2* dst = wd.conv + (size_t)k * cplane + (size_t)it.tile * S::H * TC + c;
+                float2* out = reinterpret_cast<float2*>(op) + c;
 #pragma unroll 1
                 for (int q = 0; q < 4; q++) {
                     float v[32];
                     tmem_ld32(t_x + lane_off + 32 * q, v);
 #pragma unroll
-                    for (int u = 0; u < 16; u++) dst[(size_t)(y1 + 64 * (16 * q + u)) * TC] = make_float2(v[2 * u], -v[2 * u + 1]);
+                    for (int u = 0; u < 16; u++) out[(y1 + 64 * (16 * q + u)) * TC] = make_float2(v[2 * u], -v[2 * u + 1]);
                 }
+            }
+            fence_async_smem();
+            wg_sync();
+            if (t == 0) {
+                bulk_s2g(wd.conv + (size_t)k * cplane + (size_t)it.tile * S::H * TC, op, S::H * TC * 8);
+                bulk_commit();
+                bulk_wait_read0();  // the operand buffer is rebuilt next
             }
             tc_fence_before();
             wg_sync();
@@ -272,6 +299,7 @@ __global__ void __launch_bounds__(256, 1)
         if (*abort_flag) ok = false;
     }
     if (*abort_flag && t == 0) atomicExch(err, 1);
+    if (t == 0) bulk_wait0();
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {

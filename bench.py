@@ -40,7 +40,7 @@ PUBLISHED_REF = {"lenia_4096x4096_R13": 3.174e8, "hardware": "AMD RX 7900 XT (wg
 def parse(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--config", default="single_4096", choices=["single_4096", "batched", "single_256", "multichannel"])
@@ -50,6 +50,7 @@ def parse(argv=None):
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--jsonl", default=None, help="also append a sample in the reference's results/*.jsonl format")
+    p.add_argument("--no-paths", action="store_true", help="skip timing the other step paths side by side")
     return p.parse_args(argv)
 
 
@@ -122,7 +123,7 @@ class Clocks:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -313,7 +314,11 @@ def run_ours(args, dist):
     prof = sim.profile(5)
     col_ms, row_ms, step_ms = [float(x) for x in prof]
     nclasses = len({(w.width, w.height) for w in worlds})
-    launches_per_gen = 2 * nclasses
+    # per size class and generation: one column and one row launch; the tensor-core paths add the
+    # FP32 column launch for each channel's first tile group (sizes 256..4096)
+    tc_sizes = (256, 512, 1024, 2048, 4096)
+    launches_per_gen = sum(3 if args.path in ("tf32", "bf16x3") and h in tc_sizes else 2
+                           for (_, h) in {(w.width, w.height) for w in worlds})
     if args.path == "radix2":
         n = worlds[0].width
         lg = int(np.log2(n))
@@ -365,6 +370,34 @@ def run_ours(args, dist):
         e2e = {"value": total_cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "gens_per_step": G}
 
+    # every step path on the same workload, side by side (event-timed, state resident)
+    paths = {}
+    if not args.no_paths:
+        for pth in ("fp32", "bf16x3", "tf32", "radix2"):
+            if pth == args.path:
+                paths[pth] = {"value": value, "ms_per_generation": ms_per_gen}
+                continue
+            if pth == "radix2" and any(w.channels != 1 or (w.width & (w.width - 1)) or (w.height & (w.height - 1))
+                                       for w in worlds):
+                paths[pth] = {"value": None, "why": "the radix-2 path runs one-channel power-of-two worlds only"}
+                continue
+            with Sim(worlds, seed=0, path=pth) as other:
+                seed_all(other, worlds, seeds)
+                g = G if pth != "radix2" else 4
+                other.step(g)
+                other.wait()
+                reps = max(2, min(args.steps, 20)) if pth != "radix2" else 5
+                t_ms = other.step_timed(reps * g)
+                t_ms = dist.max(t_ms)
+                paths[pth] = {"value": dist.sum(other.cells_per_step) * g * reps / (t_ms * 1e-3),
+                              "ms_per_generation": t_ms / (reps * g)}
+        if paths.get("fp32", {}).get("value") and paths.get("radix2", {}).get("value"):
+            paths["fp32_over_radix2"] = paths["fp32"]["value"] / paths["radix2"]["value"]
+        if paths.get("bf16x3", {}).get("value") and paths.get("radix2", {}).get("value"):
+            paths["bf16x3_over_radix2"] = paths["bf16x3"]["value"] / paths["radix2"]["value"]
+        if paths.get("bf16x3", {}).get("value") and paths.get("fp32", {}).get("value"):
+            paths["bf16x3_over_fp32"] = paths["bf16x3"]["value"] / paths["fp32"]["value"]
+
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
         v, cores, sample = cpu_leg(worlds, seeds)
@@ -380,6 +413,7 @@ def run_ours(args, dist):
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches_per_gen * G * args.steps,
+               "paths": paths,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
         print(json.dumps(out))
     if args.jsonl and dist.rank == 0:
