@@ -17,18 +17,19 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include "cache_hints.cuh"
 #include "engine.cuh"
 #include "fft_core.cuh"
 
 namespace lenia {
 using namespace lfft;
 
-// S sequences of length N in shared memory (stride seq_stride(N)), transformed in place by NT
-// threads; stw holds the per-stage twiddle tables (fill_stage_twiddles).  Starts after the
-// caller's barrier; ends with a barrier.
-template <int N, int S, int NT, bool INV, int I = 0>
-__device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
-    if constexpr (I < plan_len(N)) {
+// Stages [I, I1) of the transform of S sequences of length N in shared memory (stride
+// seq_stride(N)), in place, by NT threads; stw holds the per-stage twiddle tables
+// (fill_stage_twiddles).  Starts after the caller's barrier; ends with a barrier.
+template <int N, int S, int NT, bool INV, int I, int I1>
+__device__ __forceinline__ void fft_stages(float2* buf, const float2* stw) {
+    if constexpr (I < I1) {
         constexpr int R = plan_radix(N, I);
         constexpr int L = plan_L(N, I);
         constexpr int NB = N / R;
@@ -54,8 +55,58 @@ __device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
             }
         }
         __syncthreads();
-        fft_seqs<N, S, NT, INV, I + 1>(buf, stw);
+        fft_stages<N, S, NT, INV, I + 1, I1>(buf, stw);
     }
+}
+
+template <int N, int S, int NT, bool INV>
+__device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
+    fft_stages<N, S, NT, INV, 0, plan_len(N)>(buf, stw);
+}
+
+// Two transforms back to back (A, then B) with work on the values in between.  When the plan's
+// first and last radix are equal, the last stage of A leaves butterfly j holding the elements
+// j + m*N/R (m < R) in natural order -- exactly the inputs of butterfly j of B's first stage.  So
+// `mid(s, j, v, aux)` runs on those registers and B's first stage follows without a round trip
+// through shared memory.  `pre(s, j, aux)` runs before A starts, to issue the global loads mid
+// needs (aux: R values of type T per butterfly).
+template <int N>
+constexpr bool fusable() {
+    return plan_len(N) >= 2 && plan_radix(N, 0) == plan_radix(N, plan_len(N) - 1);
+}
+
+template <int N, int S, int NT, bool INV_A, bool INV_B, typename T, class Pre, class Mid>
+__device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Pre pre, Mid mid) {
+    constexpr int LAST = plan_len(N) - 1;
+    constexpr int R = plan_radix(N, LAST), L = plan_L(N, LAST), NB = N / R;
+    static_assert(L == NB && plan_radix(N, 0) == R, "fusable plans only");
+    constexpr int TOT = NB * S, PER = (TOT + NT - 1) / NT, SEQ = seq_stride(N);
+    T aux[PER][R];
+#pragma unroll
+    for (int p = 0; p < PER; p++) {
+        const int b = threadIdx.x + p * NT;
+        if ((TOT % NT) == 0 || b < TOT) pre(b / NB, b % NB, aux[p]);
+    }
+    fft_stages<N, S, NT, INV_A, 0, LAST>(buf, stw);
+    float2 v[PER][R];
+#pragma unroll
+    for (int p = 0; p < PER; p++) {
+        const int b = threadIdx.x + p * NT;
+        if ((TOT % NT) == 0 || b < TOT) {
+            const int s = b / NB, j = b - s * NB;
+            stage_load<N, R, L, INV_A>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, LAST));
+            mid(s, j, v[p], aux[p]);
+            Dft<R, INV_B>::run(v[p]);  // B's first stage: L = 1, no twiddle
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < PER; p++) {
+        const int b = threadIdx.x + p * NT;
+        if ((TOT % NT) == 0 || b < TOT) stage_store<N, R, 1>(buf + (b / NB) * SEQ, b % NB, v[p]);
+    }
+    __syncthreads();
+    fft_stages<N, S, NT, INV_B, 1, plan_len(N)>(buf, stw);
 }
 
 // Shared memory of a pass: the sequences, then (float2-aligned) the stage twiddle tables.
@@ -107,8 +158,9 @@ __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __re
         if (IT * NT == W || e < W) {
             const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC;
             const float2* src = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
-            A[i] = src[0];
-            B[i] = src[TC];
+            const uint64_t keep = hint::policy_keep();
+            A[i] = hint::ld2(src, keep);
+            B[i] = hint::ld2(src + TC, keep);
         }
     }
 #pragma unroll
@@ -146,8 +198,9 @@ __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __r
             B = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
         }
         float2* dst = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
-        dst[0] = A;
-        dst[TC] = B;
+        const uint64_t keep = hint::policy_keep();
+        hint::st2(dst, A, keep);
+        hint::st2(dst + TC, B, keep);
     }
 }
 
@@ -226,8 +279,9 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
             for (int i = 0; i < CH; i++) {
                 const int e = threadIdx.x + (i0 + i) * NT, p = e / W, x = e - p * W;
                 if (i0 + i < IT && (IT * NT == 2 * W || e < 2 * W)) {
-                    a[i] = st[(2 * p) * W + x];
-                    b[i] = st[(2 * p + 1) * W + x];
+                    const uint64_t stream = hint::policy_stream();
+                    a[i] = hint::ld1(st + (2 * p) * W + x, stream);
+                    b[i] = hint::ld1(st + (2 * p + 1) * W + x, stream);
                 }
             }
 #pragma unroll
@@ -237,8 +291,9 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
                     const float2 u = Z[p * SEQ + pad(x)];
                     const float n0 = clamp01(a[i] + dtw * growth(u.x, kp.mu, kp.sigma));
                     const float n1 = clamp01(b[i] + dtw * growth(u.y, kp.mu, kp.sigma));
-                    st[(2 * p) * W + x] = n0;
-                    st[(2 * p + 1) * W + x] = n1;
+                    const uint64_t stream = hint::policy_stream();
+                    hint::st1(st + (2 * p) * W + x, n0, stream);
+                    hint::st1(st + (2 * p + 1) * W + x, n1, stream);
                     Z[p * SEQ + pad(x)] = make_float2(n0, n1);
                 }
             }
@@ -335,7 +390,7 @@ __device__ __forceinline__ void load_tile(float2* X, const float2* __restrict__ 
 #pragma unroll
     for (int i = 0; i < IT; i++) {
         const int y = threadIdx.x + i * NT;
-        if (IT * NT == H || y < H) v[i] = s4[y];
+        if (IT * NT == H || y < H) v[i] = hint::ld4(s4 + y, hint::policy_keep());
     }
 #pragma unroll
     for (int i = 0; i < IT; i++) {
@@ -353,7 +408,7 @@ __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__
     float4* d4 = reinterpret_cast<float4*>(dst);
     for (int y = threadIdx.x; y < H; y += NT) {
         const float2 a = X[pad(y)], b = X[SEQ + pad(y)];
-        d4[y] = make_float4(a.x, a.y, b.x, b.y);
+        hint::st4(d4 + y, make_float4(a.x, a.y, b.x, b.y), hint::policy_keep());
     }
 }
 
