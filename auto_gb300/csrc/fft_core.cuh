@@ -122,19 +122,33 @@ template <bool INV> struct Dft<8, INV> { FFT_HD static void run(float2* v) { dft
 template <bool INV> struct Dft<16, INV> { FFT_HD static void run(float2* v) { dft_split<4, 4, INV>(v); } };
 
 // ------------------------------------------------------------------ radix plans
-// N = 2^a * 3^b (b <= 1): radix 3 first, then 16s, then the remaining 2, 4 or 8.
-FFT_CHD constexpr int plan_len(int n) {
+// N = 2^a * 3^b (b <= 1).  With two or more factors of 16 the plan is 16, then the 3 and the
+// remaining 2/4/8, then the other 16s: first and last radix are equal, so two transforms can be
+// chained in registers (see fft_fused).  Otherwise: 3, then 16s, then the remainder.
+FFT_CHD constexpr int plan_n16(int n) {
+    if (n % 3 == 0) n /= 3;
     int c = 0;
-    if (n % 3 == 0) { c++; n /= 3; }
     while (n % 16 == 0 && n >= 16) { c++; n /= 16; }
-    if (n > 1) c++;
     return c;
 }
-FFT_CHD constexpr int plan_radix(int n, int i) {
-    int c = 0;
-    if (n % 3 == 0) { if (c == i) return 3; c++; n /= 3; }
-    while (n % 16 == 0 && n >= 16) { if (c == i) return 16; c++; n /= 16; }
+FFT_CHD constexpr int plan_rest(int n) {
+    if (n % 3 == 0) n /= 3;
+    while (n % 16 == 0 && n >= 16) n /= 16;
     return n;
+}
+FFT_CHD constexpr int plan_len(int n) { return (n % 3 == 0 ? 1 : 0) + plan_n16(n) + (plan_rest(n) > 1 ? 1 : 0); }
+FFT_CHD constexpr int plan_radix(int n, int i) {
+    const int n16 = plan_n16(n), rest = plan_rest(n), three = n % 3 == 0 ? 1 : 0;
+    if (n16 >= 2) {
+        if (i == 0) return 16;
+        i -= 1;
+        if (three) { if (i == 0) return 3; i -= 1; }
+        if (rest > 1) { if (i == 0) return rest; i -= 1; }
+        return 16;
+    }
+    if (three) { if (i == 0) return 3; i -= 1; }
+    if (i < n16) return 16;
+    return rest;
 }
 FFT_CHD constexpr int plan_L(int n, int i) {  // product of the radices before stage i
     int l = 1;

@@ -3,8 +3,18 @@
 
 namespace lenia {
 
+static size_t col_khat_bytes_of(int H) {
+    switch (H) {
+#define KB_CASE(N) case N: return col_khat_bytes<N>();
+        LENIA_SIZES_SMALL(KB_CASE) LENIA_SIZES_LARGE(KB_CASE)
+#undef KB_CASE
+    }
+    return 0;
+}
+
 size_t col_smem_bytes(int H, int nbuf) {
-    return (size_t)nbuf * TC * lfft::seq_stride(H) * sizeof(float2) + (lfft::tw_table_size(H) + 1) * sizeof(float2);
+    return (size_t)nbuf * TC * lfft::seq_stride(H) * sizeof(float2) + (lfft::tw_table_size(H) + 1) * sizeof(float2) +
+           col_khat_bytes_of(H);
 }
 size_t row_smem_bytes(int W, int acc_planes) {
     return (size_t)2 * lfft::seq_stride(W) * sizeof(float2) + (lfft::tw_table_size(W) + 1) * sizeof(float2) +

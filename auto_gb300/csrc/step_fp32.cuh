@@ -20,9 +20,17 @@
 #include "cache_hints.cuh"
 #include "engine.cuh"
 #include "fft_core.cuh"
+#include "tc_ptx.cuh"
 
 namespace lenia {
 using namespace lfft;
+
+// 16-byte asynchronous global -> shared copy: nothing is held in registers while it is in flight.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // Stages [I, I1) of the transform of S sequences of length N in shared memory (stride
 // seq_stride(N)), in place, by NT threads; stw holds the per-stage twiddle tables
@@ -67,26 +75,20 @@ __device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
 // Two transforms back to back (A, then B) with work on the values in between.  When the plan's
 // first and last radix are equal, the last stage of A leaves butterfly j holding the elements
 // j + m*N/R (m < R) in natural order -- exactly the inputs of butterfly j of B's first stage.  So
-// `mid(s, j, v, aux)` runs on those registers and B's first stage follows without a round trip
-// through shared memory.  `pre(s, j, aux)` runs before A starts, to issue the global loads mid
-// needs (aux: R values of type T per butterfly).
+// `mid(s, j, v)` runs on those registers (sequence s, elements j + m*N/R) and B's first stage
+// follows without a round trip through shared memory: two barriers and one shared-memory
+// read/write sweep fewer than A, mid-pass, B.
 template <int N>
-constexpr bool fusable() {
+FFT_CHD constexpr bool fusable() {
     return plan_len(N) >= 2 && plan_radix(N, 0) == plan_radix(N, plan_len(N) - 1);
 }
 
-template <int N, int S, int NT, bool INV_A, bool INV_B, typename T, class Pre, class Mid>
-__device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Pre pre, Mid mid) {
+template <int N, int S, int NT, bool INV_A, bool INV_B, class Mid>
+__device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Mid mid) {
     constexpr int LAST = plan_len(N) - 1;
     constexpr int R = plan_radix(N, LAST), L = plan_L(N, LAST), NB = N / R;
     static_assert(L == NB && plan_radix(N, 0) == R, "fusable plans only");
     constexpr int TOT = NB * S, PER = (TOT + NT - 1) / NT, SEQ = seq_stride(N);
-    T aux[PER][R];
-#pragma unroll
-    for (int p = 0; p < PER; p++) {
-        const int b = threadIdx.x + p * NT;
-        if ((TOT % NT) == 0 || b < TOT) pre(b / NB, b % NB, aux[p]);
-    }
     fft_stages<N, S, NT, INV_A, 0, LAST>(buf, stw);
     float2 v[PER][R];
 #pragma unroll
@@ -95,7 +97,7 @@ __device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Pre pr
         if ((TOT % NT) == 0 || b < TOT) {
             const int s = b / NB, j = b - s * NB;
             stage_load<N, R, L, INV_A>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, LAST));
-            mid(s, j, v[p], aux[p]);
+            mid(s, j, v[p]);
             Dft<R, INV_B>::run(v[p]);  // B's first stage: L = 1, no twiddle
         }
     }
@@ -112,6 +114,16 @@ __device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Pre pr
 // Shared memory of a pass: the sequences, then (float2-aligned) the stage twiddle tables.
 template <int N>
 constexpr size_t stage_table_bytes() { return (size_t)(tw_table_size(N) + 1) * sizeof(float2); }
+
+// Column pass, fused form: after the stage tables (16-byte aligned), the tile's TC khat columns.
+template <int H>
+FFT_CHD constexpr int khat_cols_stride() { return (H / 2 + 1 + 3) / 4 * 4; }
+template <int H>
+constexpr size_t col_khat_bytes() { return fusable<H>() ? (size_t)TC * khat_cols_stride<H>() * sizeof(float) : 0; }
+template <int H>
+__device__ __forceinline__ float* col_khat_smem(float2* stw) {
+    return reinterpret_cast<float*>(((uintptr_t)(stw + tw_table_size(H)) + 15) & ~(uintptr_t)15);
+}
 
 __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
 
@@ -265,10 +277,42 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         // one channel, one kernel, Lenia growth: U -> state -> spectrum without a staging buffer
         const DevKernel kp = wd.kern[0];
         const float dtw = wd.dt * kp.weight;
+        float* st = wd.state + (size_t)r0 * W;
+        if constexpr (fusable<W>()) {
+            // The growth update runs in registers between the inverse and the forward row FFT.
+            // The item's four state rows (contiguous) are pulled into L2 while the inverse runs.
+            if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, 4 * W * (uint32_t)sizeof(float));
+            load_rows_spectrum<W, NT>(Z, wd.conv, H, r0);
+            __syncthreads();
+            fft_fused<W, 2, NT, true, false>(Z, stw, [&](int s, int j, float2* v) {
+                constexpr int R = plan_radix(W, 0), NB = W / R, CH = 8;
+                float* ra = st + (2 * s) * W + j;
+                float* rb = ra + W;
+#pragma unroll
+                for (int m0 = 0; m0 < R; m0 += CH) {
+                    float a[CH], b[CH];
+                    const uint64_t stream = hint::policy_stream();
+#pragma unroll
+                    for (int i = 0; i < CH; i++) {
+                        a[i] = hint::ld1(ra + (m0 + i) * NB, stream);
+                        b[i] = hint::ld1(rb + (m0 + i) * NB, stream);
+                    }
+#pragma unroll
+                    for (int i = 0; i < CH; i++) {
+                        const float n0 = clamp01(a[i] + dtw * growth(v[m0 + i].x, kp.mu, kp.sigma));
+                        const float n1 = clamp01(b[i] + dtw * growth(v[m0 + i].y, kp.mu, kp.sigma));
+                        hint::st1(ra + (m0 + i) * NB, n0, stream);
+                        hint::st1(rb + (m0 + i) * NB, n1, stream);
+                        v[m0 + i] = make_float2(n0, n1);
+                    }
+                }
+            });
+            store_rows_spectrum<W, NT>(Z, wd.spec, H, r0);
+            return;
+        }
         load_rows_spectrum<W, NT>(Z, wd.conv, H, r0);
         __syncthreads();
         fft_seqs<W, 2, NT, true>(Z, stw);
-        float* st = wd.state + (size_t)r0 * W;
         // state values for this thread's cells, in chunks of up to 8 loads per row pair
         constexpr int IT = (2 * W + NT - 1) / NT;
         constexpr int CH = IT < 8 ? IT : 8;
@@ -426,9 +470,35 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
     const int W = wd.W, c = it.chan, t = it.tile, K = wd.K, HQ = wd.HQ;
     const size_t cplane = (size_t)(W / 2) * H;
     const float2* src = wd.spec + c * cplane + (size_t)t * H * TC;
-    int nsrc = 0;
-    for (int k = 0; k < K; k++) nsrc += (wd.kern[k].src == c);
+    int nsrc = 0, k1 = 0;
+    for (int k = K - 1; k >= 0; k--)
+        if (wd.kern[k].src == c) nsrc++, k1 = k;
     if (nsrc == 0) return;
+    if constexpr (fusable<H>()) {
+        // One kernel on this channel, tile without the packed DC/Nyquist column: the khat multiply
+        // runs in registers between the forward and the inverse column FFT.  The tile's two khat
+        // columns (contiguous, HQ floats each) are copied to shared memory while the tile loads.
+        constexpr int HQC = khat_cols_stride<H>();
+        const float* kh = wd.khat + ((size_t)k1 * (W / 2 + 1) + (size_t)TC * t) * HQC;
+        if (nsrc == 1 && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
+            float* ksm = col_khat_smem<H>(stw);
+            for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
+            load_tile<H, NT>(X, src);
+            cp_async_wait_all();
+            __syncthreads();
+            fft_fused<H, TC, NT, false, true>(X, stw, [&](int s, int j, float2* v) {
+                constexpr int R = plan_radix(H, 0), NB = H / R;
+                const float* kc = ksm + s * HQC;
+#pragma unroll
+                for (int m = 0; m < R; m++) {
+                    const int ky = j + m * NB;
+                    v[m] = cscale(v[m], kc[ky <= H / 2 ? ky : H - ky]);
+                }
+            });
+            store_tile<H, NT>(X, wd.conv + k1 * cplane + (size_t)t * H * TC);
+            return;
+        }
+    }
     const bool reload = (nsrc > 1 && nbuf < 2);
     bool have = false;
     for (int k = 0; k < K; k++) {
@@ -461,7 +531,7 @@ template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) /
 // its first launch and before any stream capture that contains it; a zero-item call does just that.
 template <int H, int NT, int MINB>
 bool col_go(int nbuf, const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
-    const size_t smem = (size_t)nbuf * TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>();
+    const size_t smem = (size_t)nbuf * TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>() + col_khat_bytes<H>();
     static int attr_max = 0;
     if ((int)smem > attr_max) {
         if (cudaFuncSetAttribute(col_pass<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
