@@ -480,7 +480,7 @@ int setup_fused(LeniaCtx* ctx) {
                     for (int t = 0; t < ntiles; t++) col.push_back(ColItem{wi, (int)c, t, 0});
                 }
             }
-            for (uint32_t r = 0; r < d.height; r += 4) row.push_back(RowItem{wi, (int)r});
+            for (uint32_t r = 0; r < d.height; r += (uint32_t)row_item_rows((int)d.width)) row.push_back(RowItem{wi, (int)r});
             const bool simple = d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA;
             if (!simple) general = 1;
             planes = std::max(planes, (int)(simple ? 0 : (d.rule == LENIA_RULE_LENIA ? d.channels : d.nkernels)));
@@ -496,8 +496,11 @@ int setup_fused(LeniaCtx* ctx) {
         cl.nbuf = nbuf;
         cl.general = general;
         cl.planes = planes;
-        cl.var_col = 0;
-        cl.var_row = 0;
+        // Default launch variant: the 64-register form (more resident CTAs) unless it spills more
+        // than 128 bytes a thread and the 128-register form spills less than half as much.
+        auto pick = [](int v0, int v1) { return (v0 > 128 && v1 >= 0 && v1 < v0 / 2) ? 1 : 0; };
+        cl.var_col = pick(fp32_local_bytes(0, cl.H, 0), fp32_local_bytes(0, cl.H, 1));
+        cl.var_row = pick(fp32_local_bytes(1, cl.W, 0), fp32_local_bytes(1, cl.W, 1));
         cl.ncol = (int)col.size();
         cl.nrow = (int)row.size();
         cl.ntcg = (int)tcg.size();

@@ -54,6 +54,8 @@ bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* 
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s);
 size_t col_smem_bytes(int H, int nbuf);
 size_t row_smem_bytes(int W, int acc_planes);
+int row_item_rows(int W);  // rows per row-pass item (two per packed sequence)
+int fp32_local_bytes(int row, int n, int variant);  // spill/stack bytes per thread of a pass instantiation
 int max_smem_optin();
 int threads_for(int n);  // threads per CTA of the transforms of length n
 

@@ -62,6 +62,17 @@ template <int R, bool INV> FFT_HD float2 wR(int j) {
     return make_float2(c16(t), INV ? s16(t) : -s16(t));
 }
 
+// z * exp(sign*2*pi*i*j/R) for compile-time j: quarter turns are exact swaps and negations
+// (a general complex multiply by 0 and +-1 would cost four instructions under IEEE rules).
+template <int R, bool INV> FFT_HD float2 cmul_wR(float2 z, int j) {
+    const int t = (j * (16 / R)) & 15;
+    if (t == 0) return z;
+    if (t == 8) return make_float2(-z.x, -z.y);
+    if (t == 4) return rot90<INV>(z);
+    if (t == 12) return rot90<!INV>(z);
+    return cmul(z, wR<R, INV>(j));
+}
+
 // ------------------------------------------------------------------ register DFTs
 template <int R, bool INV> struct Dft;
 
@@ -105,7 +116,7 @@ template <int R1, int R2, bool INV> FFT_HD void dft_split(float2* v) {
         for (int m1 = 0; m1 < R1; m1++) a[m1] = v[R2 * m1 + m2];
         Dft<R1, INV>::run(a);
 #pragma unroll
-        for (int q1 = 0; q1 < R1; q1++) u[m2 * R1 + q1] = (m2 * q1 == 0) ? a[q1] : cmul(a[q1], wR<R, INV>(m2 * q1));
+        for (int q1 = 0; q1 < R1; q1++) u[m2 * R1 + q1] = cmul_wR<R, INV>(a[q1], m2 * q1);
     }
 #pragma unroll
     for (int q1 = 0; q1 < R1; q1++) {

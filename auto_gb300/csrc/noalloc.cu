@@ -37,7 +37,7 @@ constexpr size_t SPEC_BYTES = NOALLOC_MAX_CELLS / 2 * sizeof(float2);
 constexpr size_t TW_BYTES = (size_t)lfft::TWN * sizeof(float2);
 constexpr size_t WORLD_BYTES = (sizeof(DevWorld) + 255) / 256 * 256;
 constexpr size_t COL_BYTES = (size_t)(NOALLOC_MAX_SIDE / (2 * TC)) * sizeof(ColItem);
-constexpr size_t ROW_BYTES = (size_t)(NOALLOC_MAX_SIDE / 4) * sizeof(RowItem);
+constexpr size_t ROW_BYTES = (size_t)(NOALLOC_MAX_SIDE / 2) * sizeof(RowItem);  // items of >= 2 rows
 constexpr size_t OFF_TW = SPEC_BYTES, OFF_WORLD = OFF_TW + TW_BYTES, OFF_COL = OFF_WORLD + WORLD_BYTES,
                  OFF_ROW = OFF_COL + COL_BYTES, SCRATCH_BYTES = OFF_ROW + ROW_BYTES;
 
@@ -80,11 +80,11 @@ int setup_device(int dev, unsigned char** base) {
 }
 
 // Writes the world descriptor and the work lists into the array on the caller's stream.
-__global__ void noalloc_prepare(DevWorld* w, DevWorld value, ColItem* col, int ncol, RowItem* row, int nrow) {
+__global__ void noalloc_prepare(DevWorld* w, DevWorld value, ColItem* col, int ncol, RowItem* row, int nrow, int rows) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) *w = value;
     if (i < ncol) col[i] = ColItem{0, 0, i, 0};
-    if (i < nrow) row[i] = RowItem{0, 4 * i};
+    if (i < nrow) row[i] = RowItem{0, rows * i};
 }
 
 }  // namespace
@@ -133,9 +133,10 @@ LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, 
     ColItem* col = reinterpret_cast<ColItem*>(base + OFF_COL);
     RowItem* row = reinterpret_cast<RowItem*>(base + OFF_ROW);
     const float2* tw = reinterpret_cast<const float2*>(base + OFF_TW);
-    const int ncol = spec_tiles((int)width), nrow = (int)height / 4;
+    const int rows = row_item_rows((int)width);
+    const int ncol = spec_tiles((int)width), nrow = (int)height / rows;
     const int n = ncol > nrow ? ncol : nrow;
-    noalloc_prepare<<<(n + 255) / 256, 256, 0, s>>>(dw, w, col, ncol, row, nrow);
+    noalloc_prepare<<<(n + 255) / 256, 256, 0, s>>>(dw, w, col, ncol, row, nrow, rows);
     bool ok = launch_row_fp32((int)width, 0, MODE_FORWARD, 0, dw, row, nrow, 0, tw, s);
     for (uint32_t i = 0; ok && i < steps; i++) {
         ok = launch_col_fp32((int)height, 0, 1, dw, col, ncol, tw, s) &&

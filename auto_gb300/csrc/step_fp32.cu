@@ -17,9 +17,15 @@ size_t col_smem_bytes(int H, int nbuf) {
            col_khat_bytes_of(H);
 }
 size_t row_smem_bytes(int W, int acc_planes) {
-    return (size_t)2 * lfft::seq_stride(W) * sizeof(float2) + (lfft::tw_table_size(W) + 1) * sizeof(float2) +
-           (size_t)acc_planes * 4 * W * sizeof(float);
+    switch (W) {
+#define RS_CASE(N) case N: return row_smem<N>(acc_planes > 0, acc_planes);
+        LENIA_SIZES_SMALL(RS_CASE) LENIA_SIZES_LARGE(RS_CASE)
+#undef RS_CASE
+    }
+    return 0;
 }
+
+int row_item_rows(int W) { return 2 * row_seqs(W); }
 
 int max_smem_optin() {
     int dev = 0, v = 0;
@@ -47,6 +53,11 @@ bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* 
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s) {
     return launch_row_group_small(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s) ||
            launch_row_group_large(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s);
+}
+
+int fp32_local_bytes(int row, int n, int variant) {
+    const int a = row ? row_local_bytes_small(n, variant) : col_local_bytes_small(n, variant);
+    return a >= 0 ? a : (row ? row_local_bytes_large(n, variant) : col_local_bytes_large(n, variant));
 }
 
 }  // namespace lenia

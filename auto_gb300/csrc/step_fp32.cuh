@@ -77,14 +77,18 @@ __device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
 // j + m*N/R (m < R) in natural order -- exactly the inputs of butterfly j of B's first stage.  So
 // `mid(s, j, v)` runs on those registers (sequence s, elements j + m*N/R) and B's first stage
 // follows without a round trip through shared memory: two barriers and one shared-memory
-// read/write sweep fewer than A, mid-pass, B.
+// read/write sweep fewer than A, mid-pass, B.  `pre(s, j)` runs just before the last stage of A.
 template <int N>
 FFT_CHD constexpr bool fusable() {
     return plan_len(N) >= 2 && plan_radix(N, 0) == plan_radix(N, plan_len(N) - 1);
 }
 
-template <int N, int S, int NT, bool INV_A, bool INV_B, class Mid>
-__device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Mid mid) {
+struct NoPre {
+    __device__ void operator()(int, int) const {}
+};
+
+template <int N, int S, int NT, bool INV_A, bool INV_B, class Mid, class Pre = NoPre>
+__device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Mid mid, Pre pre = Pre()) {
     constexpr int LAST = plan_len(N) - 1;
     constexpr int R = plan_radix(N, LAST), L = plan_L(N, LAST), NB = N / R;
     static_assert(L == NB && plan_radix(N, 0) == R, "fusable plans only");
@@ -96,6 +100,7 @@ __device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Mid mi
         const int b = threadIdx.x + p * NT;
         if ((TOT % NT) == 0 || b < TOT) {
             const int s = b / NB, j = b - s * NB;
+            pre(s, j);  // global loads that mid needs, issued before the last stage of A
             stage_load<N, R, L, INV_A>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, LAST));
             mid(s, j, v[p]);
             Dft<R, INV_B>::run(v[p]);  // B's first stage: L = 1, no twiddle
@@ -127,10 +132,13 @@ __device__ __forceinline__ float* col_khat_smem(float2* stw) {
 
 __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
 
-// Gaussian growth mapped to [-1, 1] (spectral.rs:341-344).
-__device__ __forceinline__ float growth(float u, float mu, float sigma) {
-    float d = (u - mu) / sigma;
-    return 2.0f * expf(-0.5f * d * d) - 1.0f;
+// Gaussian growth mapped to [-1, 1] (spectral.rs:341-344): 2 exp(-d^2/2) - 1, d = (u - mu)/sigma.
+// Evaluated as 2 * 2^(c d^2) - 1 with c = -log2(e)/2 and d formed with the reciprocal of sigma
+// (taken once per thread): about ten instructions per cell instead of a divide and an expf.
+// Differs from the direct form by a few float ulps of the exponential.
+__device__ __forceinline__ float growth(float u, float mu, float inv_sigma) {
+    const float d = (u - mu) * inv_sigma;
+    return 2.0f * exp2f(-0.72134752044448170f * (d * d)) - 1.0f;
 }
 
 // SmoothLife update (spectral.rs:396-407).
@@ -155,31 +163,57 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 }
 
 // ---------------------------------------------------------------------------- row pass
+//
+// One CTA per item of 2S rows (S packed sequences, row pairs), S = 2.  The code is written for
+// any S; measured at 4096 x 4096, S = 1 (256 threads, three or four CTAs per SM) was 5-30%
+// slower than S = 2 (512 threads, two CTAs per SM), whether the state rows were staged in shared
+// memory or loaded into registers.
+FFT_CHD constexpr int row_seqs(int) { return 2; }
+template <int W>
+constexpr int row_nt() {
+    constexpr int n = row_seqs(W) * W / 16;
+    return n < 64 ? 64 : (n > 512 ? 512 : n);
+}
+// variant 0: at most 1024 threads' worth of registers per SM (64 a thread at 512 threads);
+// variant 1: at most 128 a thread
+template <int W, int V>
+constexpr int row_minb() {
+    constexpr int t = V == 0 ? 1024 : 512;
+    return t / row_nt<W>() < 1 ? 1 : t / row_nt<W>();
+}
+// Shared memory after the sequences and stage tables: the state rows of the fast path at widths
+// that cannot chain their FFTs, or the accumulation planes ([planes][2S][W]) of the general path.
+template <int W>
+__device__ __forceinline__ float* row_extra_smem(float2* stw) {
+    return reinterpret_cast<float*>(((uintptr_t)(stw + tw_table_size(W)) + 15) & ~(uintptr_t)15);
+}
 
-// Half-spectra of rows r0..r0+3 (tile layout) -> two packed complex sequences
+// Half-spectra of rows r0..r0+2S-1 (tile layout) -> S packed complex sequences
 // Z_p = A + iB with A = row r0+2p, B = row r0+2p+1, using Hermitian symmetry for k > W/2.
-// Consecutive threads cover whole tiles: 4 rows x TC columns = one contiguous chunk.
-template <int W, int NT>
+// One unit = one tile's TC columns of one row pair: two 16-byte loads (rows 2p and 2p+1, which
+// are adjacent in the tile, so one 32-byte sector).
+template <int W, int S, int NT>
 __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __restrict__ sp, int H, int r0) {
+    static_assert(TC == 2, "one float4 holds the two columns of a tile row");
     constexpr int SEQ = seq_stride(W);
-    constexpr int IT = (W + NT - 1) / NT;  // W/(2 TC) tiles x 2 pairs x TC columns, over NT threads
-    float2 A[IT], B[IT];
+    constexpr int U = W / (2 * TC) * S, IT = (U + NT - 1) / NT;
+    float4 A[IT], B[IT];
 #pragma unroll
     for (int i = 0; i < IT; i++) {  // every load in flight before the first use
-        const int e = threadIdx.x + i * NT;
-        if (IT * NT == W || e < W) {
-            const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC;
-            const float2* src = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
+        const int u = threadIdx.x + i * NT;
+        if (IT * NT == U || u < U) {
+            const int t = u / S, p = u - t * S;
+            const float4* src = reinterpret_cast<const float4*>(sp + ((size_t)t * H + r0 + 2 * p) * TC);
             const uint64_t keep = hint::policy_keep();
-            A[i] = hint::ld2(src, keep);
-            B[i] = hint::ld2(src + TC, keep);
+            A[i] = hint::ld4(src, keep);
+            B[i] = hint::ld4(src + 1, keep);
         }
     }
 #pragma unroll
     for (int i = 0; i < IT; i++) {
-        const int e = threadIdx.x + i * NT;
-        if (IT * NT == W || e < W) {
-            const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC, kx = TC * t + c;
+        const int u = threadIdx.x + i * NT;
+        if (IT * NT == U || u < U) {
+            const int t = u / S, p = u - t * S, kx = TC * t;
             float2* z = Z + p * SEQ;
             if (kx == 0) {
                 z[pad(0)] = make_float2(A[i].x, B[i].x);
@@ -188,42 +222,48 @@ __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __re
                 z[pad(kx)] = make_float2(A[i].x - B[i].y, A[i].y + B[i].x);
                 z[pad(W - kx)] = make_float2(A[i].x + B[i].y, B[i].x - A[i].y);
             }
+            z[pad(kx + 1)] = make_float2(A[i].z - B[i].w, A[i].w + B[i].z);
+            z[pad(W - kx - 1)] = make_float2(A[i].z + B[i].w, B[i].z - A[i].w);
         }
     }
 }
 
-// Two packed complex spectra Z_p = FFT(a + ib) -> half-spectra of rows r0+2p (A) and r0+2p+1 (B).
-template <int W, int NT>
+// S packed complex spectra Z_p = FFT(a + ib) -> half-spectra of rows r0+2p (A) and r0+2p+1 (B).
+template <int W, int S, int NT>
 __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __restrict__ sp, int H, int r0) {
     constexpr int SEQ = seq_stride(W);
-    for (int e = threadIdx.x; e < W; e += NT) {
-        const int t = e / (2 * TC), p = (e / TC) & 1, c = e % TC, kx = TC * t + c;
+    constexpr int U = W / (2 * TC) * S;
+    for (int u = threadIdx.x; u < U; u += NT) {
+        const int t = u / S, p = u - t * S, kx = TC * t;
         const float2* z = Z + p * SEQ;
-        float2 A, B;
+        float4 A, B;
         if (kx == 0) {
             const float2 z0 = z[pad(0)], zn = z[pad(W / 2)];
-            A = make_float2(z0.x, zn.x);
-            B = make_float2(z0.y, zn.y);
+            A.x = z0.x, A.y = zn.x, B.x = z0.y, B.y = zn.y;
         } else {
             const float2 a = z[pad(kx)], b = z[pad(W - kx)];
-            A = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
-            B = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
+            A.x = 0.5f * (a.x + b.x), A.y = 0.5f * (a.y - b.y);
+            B.x = 0.5f * (a.y + b.y), B.y = -0.5f * (a.x - b.x);
         }
-        float2* dst = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
+        const float2 a = z[pad(kx + 1)], b = z[pad(W - kx - 1)];
+        A.z = 0.5f * (a.x + b.x), A.w = 0.5f * (a.y - b.y);
+        B.z = 0.5f * (a.y + b.y), B.w = -0.5f * (a.x - b.x);
+        float4* dst = reinterpret_cast<float4*>(sp + ((size_t)t * H + r0 + 2 * p) * TC);
         const uint64_t keep = hint::policy_keep();
-        hint::st2(dst, A, keep);
-        hint::st2(dst + TC, B, keep);
+        hint::st4(dst, A, keep);
+        hint::st4(dst + 1, B, keep);
     }
 }
 
 template <int W, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items,
                                                 int mode, int general, const float2* __restrict__ tw) {
+    constexpr int S = row_seqs(W), ROWS = 2 * S;
     extern __shared__ float4 smem_raw[];
     constexpr int SEQ = seq_stride(W);
     float2* Z = reinterpret_cast<float2*>(smem_raw);
-    float2* stw = Z + 2 * SEQ;
-    float* acc = reinterpret_cast<float*>(stw + tw_table_size(W) + 1);  // [planes][4][W]
+    float2* stw = Z + S * SEQ;
+    float* extra = row_extra_smem<W>(stw);
     fill_stage_twiddles<W>(stw, tw, threadIdx.x, NT);
     const RowItem it = items[blockIdx.x];
     const DevWorld& wd = worlds[it.world];
@@ -233,12 +273,12 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     if (mode == MODE_FORWARD) {
         for (int d = 0; d < C; d++) {
             const float* st = wd.state + d * plane + (size_t)r0 * W;
-            constexpr int IT = (2 * W + NT - 1) / NT;
+            constexpr int IT = (S * W + NT - 1) / NT;
             float a[IT], b[IT];
 #pragma unroll
             for (int i = 0; i < IT; i++) {
                 const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
-                if (IT * NT == 2 * W || e < 2 * W) {
+                if (IT * NT == S * W || e < S * W) {
                     a[i] = st[(2 * p) * W + x];
                     b[i] = st[(2 * p + 1) * W + x];
                 }
@@ -246,11 +286,11 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
 #pragma unroll
             for (int i = 0; i < IT; i++) {
                 const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
-                if (IT * NT == 2 * W || e < 2 * W) Z[p * SEQ + pad(x)] = make_float2(a[i], b[i]);
+                if (IT * NT == S * W || e < S * W) Z[p * SEQ + pad(x)] = make_float2(a[i], b[i]);
             }
             __syncthreads();
-            fft_seqs<W, 2, NT, false>(Z, stw);
-            store_rows_spectrum<W, NT>(Z, wd.spec + d * cplane, H, r0);
+            fft_seqs<W, S, NT, false>(Z, stw);
+            store_rows_spectrum<W, S, NT>(Z, wd.spec + d * cplane, H, r0);
             __syncthreads();
         }
         return;
@@ -258,11 +298,11 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
 
     if (mode == MODE_U) {
         for (int k = 0; k < K; k++) {
-            load_rows_spectrum<W, NT>(Z, wd.conv + k * cplane, H, r0);
+            load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
             __syncthreads();
-            fft_seqs<W, 2, NT, true>(Z, stw);
+            fft_seqs<W, S, NT, true>(Z, stw);
             float* u = wd.u_out + k * plane + (size_t)r0 * W;
-            for (int e = threadIdx.x; e < 2 * W; e += NT) {
+            for (int e = threadIdx.x; e < S * W; e += NT) {
                 const int p = e / W, x = e - p * W;
                 const float2 z = Z[p * SEQ + pad(x)];
                 u[(2 * p) * W + x] = z.x;
@@ -274,98 +314,92 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     }
 
     if (!general) {
-        // one channel, one kernel, Lenia growth: U -> state -> spectrum without a staging buffer
+        // One channel, one kernel, Lenia growth.
         const DevKernel kp = wd.kern[0];
-        const float dtw = wd.dt * kp.weight;
+        const float dtw = wd.dt * kp.weight, isig = 1.0f / kp.sigma;
         float* st = wd.state + (size_t)r0 * W;
+        const uint64_t stream = hint::policy_stream();
         if constexpr (fusable<W>()) {
-            // The growth update runs in registers between the inverse and the forward row FFT.
-            // The item's four state rows (contiguous) are pulled into L2 while the inverse runs.
-            if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, 4 * W * (uint32_t)sizeof(float));
-            load_rows_spectrum<W, NT>(Z, wd.conv, H, r0);
+            // The growth update runs in registers between the inverse and the forward row FFT.  The
+            // item's state rows are pulled into L2 when the CTA starts, and each thread's 2 x R state
+            // values are loaded into registers just before the last inverse stage.
+            constexpr int R = plan_radix(W, 0), NB = W / R;
+            static_assert(S * NB <= NT, "one butterfly per thread in the fused stage");
+            if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, ROWS * W * (uint32_t)sizeof(float));
+            load_rows_spectrum<W, S, NT>(Z, wd.conv, H, r0);
             __syncthreads();
-            fft_fused<W, 2, NT, true, false>(Z, stw, [&](int s, int j, float2* v) {
-                constexpr int R = plan_radix(W, 0), NB = W / R, CH = 8;
-                float* ra = st + (2 * s) * W + j;
-                float* rb = ra + W;
+            float sa[R], sb[R];
+            fft_fused<W, S, NT, true, false>(
+                Z, stw,
+                [&](int s, int j, float2* v) {
+                    float* ga = st + (2 * s) * W + j;
 #pragma unroll
-                for (int m0 = 0; m0 < R; m0 += CH) {
-                    float a[CH], b[CH];
-                    const uint64_t stream = hint::policy_stream();
-#pragma unroll
-                    for (int i = 0; i < CH; i++) {
-                        a[i] = hint::ld1(ra + (m0 + i) * NB, stream);
-                        b[i] = hint::ld1(rb + (m0 + i) * NB, stream);
+                    for (int m = 0; m < R; m++) {
+                        const float n0 = clamp01(sa[m] + dtw * growth(v[m].x, kp.mu, isig));
+                        const float n1 = clamp01(sb[m] + dtw * growth(v[m].y, kp.mu, isig));
+                        hint::st1(ga + m * NB, n0, stream);
+                        hint::st1(ga + W + m * NB, n1, stream);
+                        v[m] = make_float2(n0, n1);
                     }
+                },
+                [&](int s, int j) {
+                    const float* ga = st + (2 * s) * W + j;
 #pragma unroll
-                    for (int i = 0; i < CH; i++) {
-                        const float n0 = clamp01(a[i] + dtw * growth(v[m0 + i].x, kp.mu, kp.sigma));
-                        const float n1 = clamp01(b[i] + dtw * growth(v[m0 + i].y, kp.mu, kp.sigma));
-                        hint::st1(ra + (m0 + i) * NB, n0, stream);
-                        hint::st1(rb + (m0 + i) * NB, n1, stream);
-                        v[m0 + i] = make_float2(n0, n1);
+                    for (int m = 0; m < R; m++) {
+                        sa[m] = hint::ld1(ga + m * NB, stream);
+                        sb[m] = hint::ld1(ga + W + m * NB, stream);
                     }
-                }
-            });
-            store_rows_spectrum<W, NT>(Z, wd.spec, H, r0);
+                });
+            store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
             return;
         }
-        load_rows_spectrum<W, NT>(Z, wd.conv, H, r0);
+        // Other widths: the item's state rows (contiguous) are staged in shared memory while the
+        // spectrum loads and the inverse FFT run.
+        float* ss = extra;  // [ROWS][W]
+        if (((uintptr_t)st & 15) == 0) {
+            for (int e = threadIdx.x; e < ROWS * W / 4; e += NT) cp_async16(ss + 4 * e, st + 4 * e);
+        } else {
+            for (int e = threadIdx.x; e < ROWS * W; e += NT) ss[e] = st[e];
+        }
+        load_rows_spectrum<W, S, NT>(Z, wd.conv, H, r0);
+        cp_async_wait_all();
         __syncthreads();
-        fft_seqs<W, 2, NT, true>(Z, stw);
-        // state values for this thread's cells, in chunks of up to 8 loads per row pair
-        constexpr int IT = (2 * W + NT - 1) / NT;
-        constexpr int CH = IT < 8 ? IT : 8;
-#pragma unroll
-        for (int i0 = 0; i0 < IT; i0 += CH) {
-            float a[CH], b[CH];
-#pragma unroll
-            for (int i = 0; i < CH; i++) {
-                const int e = threadIdx.x + (i0 + i) * NT, p = e / W, x = e - p * W;
-                if (i0 + i < IT && (IT * NT == 2 * W || e < 2 * W)) {
-                    const uint64_t stream = hint::policy_stream();
-                    a[i] = hint::ld1(st + (2 * p) * W + x, stream);
-                    b[i] = hint::ld1(st + (2 * p + 1) * W + x, stream);
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < CH; i++) {
-                const int e = threadIdx.x + (i0 + i) * NT, p = e / W, x = e - p * W;
-                if (i0 + i < IT && (IT * NT == 2 * W || e < 2 * W)) {
-                    const float2 u = Z[p * SEQ + pad(x)];
-                    const float n0 = clamp01(a[i] + dtw * growth(u.x, kp.mu, kp.sigma));
-                    const float n1 = clamp01(b[i] + dtw * growth(u.y, kp.mu, kp.sigma));
-                    const uint64_t stream = hint::policy_stream();
-                    hint::st1(st + (2 * p) * W + x, n0, stream);
-                    hint::st1(st + (2 * p + 1) * W + x, n1, stream);
-                    Z[p * SEQ + pad(x)] = make_float2(n0, n1);
-                }
-            }
+        fft_seqs<W, S, NT, true>(Z, stw);
+        for (int e = threadIdx.x; e < S * W; e += NT) {
+            const int p = e / W, x = e - p * W;
+            const float2 u = Z[p * SEQ + pad(x)];
+            const float n0 = clamp01(ss[(2 * p) * W + x] + dtw * growth(u.x, kp.mu, isig));
+            const float n1 = clamp01(ss[(2 * p + 1) * W + x] + dtw * growth(u.y, kp.mu, isig));
+            hint::st1(st + (2 * p) * W + x, n0, stream);
+            hint::st1(st + (2 * p + 1) * W + x, n1, stream);
+            Z[p * SEQ + pad(x)] = make_float2(n0, n1);
         }
         __syncthreads();
-        fft_seqs<W, 2, NT, false>(Z, stw);
-        store_rows_spectrum<W, NT>(Z, wd.spec, H, r0);
+        fft_seqs<W, S, NT, false>(Z, stw);
+        store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
         return;
     }
 
     // General: several channels and/or kernels, or a rule that needs every U at once.
     const int rule = wd.rule;
     const int planes = (rule == LENIA_RULE_LENIA) ? C : K;
-    for (int e = threadIdx.x; e < planes * 4 * W; e += NT) acc[e] = 0.0f;
+    float* acc = extra;  // [planes][ROWS][W]
+    for (int e = threadIdx.x; e < planes * ROWS * W; e += NT) acc[e] = 0.0f;
     for (int k = 0; k < K; k++) {
         const DevKernel kp = wd.kern[k];
-        load_rows_spectrum<W, NT>(Z, wd.conv + k * cplane, H, r0);
+        const float isig = 1.0f / kp.sigma;
+        load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
         __syncthreads();
-        fft_seqs<W, 2, NT, true>(Z, stw);
-        for (int e = threadIdx.x; e < 2 * W; e += NT) {
+        fft_seqs<W, S, NT, true>(Z, stw);
+        for (int e = threadIdx.x; e < S * W; e += NT) {
             const int p = e / W, x = e - p * W;
             const float2 u = Z[p * SEQ + pad(x)];
             if (rule == LENIA_RULE_LENIA) {
-                float* a = acc + (size_t)kp.dst * 4 * W;
-                a[(2 * p) * W + x] += kp.weight * growth(u.x, kp.mu, kp.sigma);
-                a[(2 * p + 1) * W + x] += kp.weight * growth(u.y, kp.mu, kp.sigma);
+                float* a = acc + (size_t)kp.dst * ROWS * W;
+                a[(2 * p) * W + x] += kp.weight * growth(u.x, kp.mu, isig);
+                a[(2 * p + 1) * W + x] += kp.weight * growth(u.y, kp.mu, isig);
             } else {
-                float* a = acc + (size_t)k * 4 * W;
+                float* a = acc + (size_t)k * ROWS * W;
                 a[(2 * p) * W + x] = u.x;
                 a[(2 * p + 1) * W + x] = u.y;
             }
@@ -374,23 +408,23 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     }
     for (int d = 0; d < C; d++) {
         float* st = wd.state + d * plane + (size_t)r0 * W;
-        for (int e = threadIdx.x; e < 2 * W; e += NT) {
+        for (int e = threadIdx.x; e < S * W; e += NT) {
             const int p = e / W, x = e - p * W;
             float n[2];
 #pragma unroll
             for (int q = 0; q < 2; q++) {
                 const int r = 2 * p + q;
                 const float s = st[r * W + x];
-                if (rule == LENIA_RULE_LENIA) n[q] = clamp01(s + wd.dt * acc[(size_t)d * 4 * W + r * W + x]);
-                else if (rule == LENIA_RULE_SMOOTHLIFE) n[q] = smoothlife_update(s, acc[r * W + x], acc[4 * W + r * W + x]);
-                else n[q] = mnca_update(s, acc[r * W + x], acc[4 * W + r * W + x]);
+                if (rule == LENIA_RULE_LENIA) n[q] = clamp01(s + wd.dt * acc[(size_t)d * ROWS * W + r * W + x]);
+                else if (rule == LENIA_RULE_SMOOTHLIFE) n[q] = smoothlife_update(s, acc[r * W + x], acc[ROWS * W + r * W + x]);
+                else n[q] = mnca_update(s, acc[r * W + x], acc[ROWS * W + r * W + x]);
                 st[r * W + x] = n[q];
             }
             Z[p * SEQ + pad(x)] = make_float2(n[0], n[1]);
         }
         __syncthreads();
-        fft_seqs<W, 2, NT, false>(Z, stw);
-        store_rows_spectrum<W, NT>(Z, wd.spec + d * cplane, H, r0);
+        fft_seqs<W, S, NT, false>(Z, stw);
+        store_rows_spectrum<W, S, NT>(Z, wd.spec + d * cplane, H, r0);
         __syncthreads();
     }
 }
@@ -543,11 +577,19 @@ bool col_go(int nbuf, const DevWorld* worlds, const ColItem* items, int nitems, 
     return true;
 }
 
+// Shared memory of a row-pass launch: sequences, stage tables, then the general path's
+// accumulation planes or the fast path's staged state rows.
+template <int W>
+constexpr size_t row_smem(int general, int planes) {
+    const int rows = 2 * row_seqs(W);
+    return (size_t)row_seqs(W) * seq_stride(W) * sizeof(float2) + stage_table_bytes<W>() +
+           (size_t)(general ? planes : (fusable<W>() ? 0 : 1)) * rows * W * sizeof(float);
+}
+
 template <int W, int NT, int MINB>
 bool row_go(int mode, int general, int planes, const DevWorld* worlds, const RowItem* items, int nitems,
             const float2* tw, cudaStream_t s) {
-    const size_t smem = (size_t)2 * seq_stride(W) * sizeof(float2) + stage_table_bytes<W>() +
-                        (size_t)planes * 4 * W * sizeof(float);
+    const size_t smem = row_smem<W>(general, planes);
     static int attr_max = 0;
     if ((int)smem > attr_max) {
         if (cudaFuncSetAttribute(row_pass<W, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -566,8 +608,27 @@ bool row_go(int mode, int general, int planes, const DevWorld* worlds, const Row
 #define LENIA_ROW_CASE(N)                                                                                   \
     case N:                                                                                                 \
         return variant == 0                                                                                 \
-                   ? row_go<N, nt_of<N>(), minb_of<N, 0>()>(mode, general, planes, worlds, items, nitems, tw, s) \
-                   : row_go<N, nt_of<N>(), minb_of<N, 1>()>(mode, general, planes, worlds, items, nitems, tw, s);
+                   ? row_go<N, row_nt<N>(), row_minb<N, 0>()>(mode, general, planes, worlds, items, nitems, tw, s) \
+                   : row_go<N, row_nt<N>(), row_minb<N, 1>()>(mode, general, planes, worlds, items, nitems, tw, s);
+
+// Local memory (spills and stack) of one instantiation, bytes per thread; -1 if unknown.
+template <class F>
+int local_bytes_of(F* f) {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, f) == cudaSuccess ? (int)a.localSizeBytes : -1;
+}
+#define LENIA_COL_LOCAL_CASE(N)                                                    \
+    case N:                                                                        \
+        return variant == 0 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>) \
+                            : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
+#define LENIA_ROW_LOCAL_CASE(N)                                                          \
+    case N:                                                                              \
+        return variant == 0 ? local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>()>) \
+                            : local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>()>);
+int col_local_bytes_small(int H, int variant);
+int col_local_bytes_large(int H, int variant);
+int row_local_bytes_small(int W, int variant);
+int row_local_bytes_large(int W, int variant);
 
 bool launch_col_group_small(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
                             const float2* tw, cudaStream_t s);

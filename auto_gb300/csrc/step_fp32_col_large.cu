@@ -9,4 +9,9 @@ bool launch_col_group_large(int H, int variant, int nbuf, const DevWorld* worlds
     return false;
 }
 
+int col_local_bytes_large(int H, int variant) {
+    switch (H) { LENIA_SIZES_LARGE(LENIA_COL_LOCAL_CASE) }
+    return -1;
+}
+
 }  // namespace lenia

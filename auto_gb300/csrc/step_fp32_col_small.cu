@@ -9,4 +9,9 @@ bool launch_col_group_small(int H, int variant, int nbuf, const DevWorld* worlds
     return false;
 }
 
+int col_local_bytes_small(int H, int variant) {
+    switch (H) { LENIA_SIZES_SMALL(LENIA_COL_LOCAL_CASE) }
+    return -1;
+}
+
 }  // namespace lenia

@@ -9,4 +9,9 @@ bool launch_row_group_large(int W, int variant, int mode, int general, int plane
     return false;
 }
 
+int row_local_bytes_large(int W, int variant) {
+    switch (W) { LENIA_SIZES_LARGE(LENIA_ROW_LOCAL_CASE) }
+    return -1;
+}
+
 }  // namespace lenia
