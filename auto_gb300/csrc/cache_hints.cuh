@@ -52,5 +52,18 @@ __device__ __forceinline__ void st1(float* p, float v, uint64_t pol) {
     asm volatile("st.global.L2::cache_hint.f32 [%0], %1, %2;" ::"l"(p), "f"(v), "l"(pol) : "memory");
 }
 
+// The same with a compile-time byte offset folded into the address ([p + OFF]), so that a run of
+// accesses off one base pointer does not need a 64-bit register pair per address.
+template <int OFF>
+__device__ __forceinline__ float ld1_at(const float* p, uint64_t pol) {
+    float v;
+    asm volatile("ld.global.L2::cache_hint.f32 %0, [%1+%3], %2;" : "=f"(v) : "l"(p), "l"(pol), "n"(OFF));
+    return v;
+}
+template <int OFF>
+__device__ __forceinline__ void st1_at(float* p, float v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.f32 [%0+%3], %1, %2;" ::"l"(p), "f"(v), "l"(pol), "n"(OFF) : "memory");
+}
+
 }  // namespace hint
 }  // namespace lenia

@@ -32,6 +32,20 @@ __device__ __forceinline__ void cp_async16(void* dst, const void* src) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
+// f(Int<I>()) for I = 0..N-1, so that I (decltype(i)::value) can be a template argument.
+template <int I>
+struct Int {
+    static constexpr int value = I;
+    __host__ __device__ constexpr operator int() const { return I; }
+};
+template <int I, int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+    if constexpr (I < N) {
+        f(Int<I>());
+        static_for<I + 1, N>(f);
+    }
+}
+
 // Stages [I, I1) of the transform of S sequences of length N in shared memory (stride
 // seq_stride(N)), in place, by NT threads; stw holds the per-stage twiddle tables
 // (fill_stage_twiddles).  Starts after the caller's barrier; ends with a barrier.
@@ -333,22 +347,20 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
                 Z, stw,
                 [&](int s, int j, float2* v) {
                     float* ga = st + (2 * s) * W + j;
-#pragma unroll
-                    for (int m = 0; m < R; m++) {
+                    static_for<0, R>([&](auto m) {
                         const float n0 = clamp01(sa[m] + dtw * growth(v[m].x, kp.mu, isig));
                         const float n1 = clamp01(sb[m] + dtw * growth(v[m].y, kp.mu, isig));
-                        hint::st1(ga + m * NB, n0, stream);
-                        hint::st1(ga + W + m * NB, n1, stream);
+                        hint::st1_at<decltype(m)::value * NB * 4>(ga, n0, stream);
+                        hint::st1_at<(W + decltype(m)::value * NB) * 4>(ga, n1, stream);
                         v[m] = make_float2(n0, n1);
-                    }
+                    });
                 },
                 [&](int s, int j) {
                     const float* ga = st + (2 * s) * W + j;
-#pragma unroll
-                    for (int m = 0; m < R; m++) {
-                        sa[m] = hint::ld1(ga + m * NB, stream);
-                        sb[m] = hint::ld1(ga + W + m * NB, stream);
-                    }
+                    static_for<0, R>([&](auto m) {
+                        sa[m] = hint::ld1_at<decltype(m)::value * NB * 4>(ga, stream);
+                        sb[m] = hint::ld1_at<(W + decltype(m)::value * NB) * 4>(ga, stream);
+                    });
                 });
             store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
             return;
