@@ -4,7 +4,7 @@
 // (crates/auto-core/src/sim.rs:59-80, program.rs:102-129): it owns the device buffers of every
 // world, the kernel spectra, the work lists of each size class and the CUDA graphs that replay
 // steps.  Worlds of one grid size form a size class; each class is one column launch and one
-// row launch per step over all of its worlds, and classes run as parallel branches of the graph.
+// row launch per step over all of its worlds, and the graph runs the classes one after another.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -39,8 +39,6 @@ struct SizeClass {
     int nrow = 0;
     int var_col = 0, var_row = 0;  // launch variants (see launch_col_fp32)
     int nbuf = 1, general = 0, planes = 0;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
 };
 
 struct WorldBuffers {
@@ -60,7 +58,6 @@ struct LeniaCtx {
     int device = 0;
     int path = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t fork = nullptr;
     std::vector<LeniaWorldDesc> desc;
     std::vector<DevWorld> hw;
     DevWorld* d_worlds = nullptr;
@@ -296,21 +293,17 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
         CK(cudaGetLastError());
         return 0;
     }
-    const bool fork = ctx->classes.size() > 1;
-    if (fork) CK(cudaEventRecord(ctx->fork, ctx->stream));
+    // Size classes one after another, each for all its steps: a class's half-spectrum then stays in
+    // L2 between its column and row passes.  Measured on the 384-world batched workload, this order
+    // is 6% faster than running the classes as concurrent graph branches.
+    cudaStream_t s = ctx->stream;
     for (auto& cl : ctx->classes) {
-        cudaStream_t s = fork ? cl.stream : ctx->stream;
-        if (fork) CK(cudaStreamWaitEvent(s, ctx->fork, 0));
         for (int st = 0; st < steps; st++) {
             bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, cl.var_col, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
             ok = launch_row_fp32(cl.W, cl.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
                                  ctx->d_tw, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
-        }
-        if (fork) {
-            CK(cudaEventRecord(cl.done, s));
-            CK(cudaStreamWaitEvent(ctx->stream, cl.done, 0));
         }
     }
     CK(cudaGetLastError());
@@ -525,8 +518,6 @@ int setup_fused(LeniaCtx* ctx) {
             ro += b.nrow;
             go += b.ntcg;
         }
-        CK(cudaStreamCreateWithFlags(&cl.stream, cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&cl.done, cudaEventDisableTiming));
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
             if (!launch_col_fp32(cl.H, v, cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
@@ -631,8 +622,7 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         g_create_error = msg;
         return code;
     };
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
         fail(ctx, LENIA_ECUDA, "stream creation failed");
         return bail(LENIA_ECUDA);
     }
@@ -670,13 +660,8 @@ int lenia_destroy(LeniaCtx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     if (ctx->graph_big) cudaGraphExecDestroy(ctx->graph_big);
     if (ctx->graph_one) cudaGraphExecDestroy(ctx->graph_one);
-    for (auto& cl : ctx->classes) {
-        if (cl.stream) cudaStreamDestroy(cl.stream);
-        if (cl.done) cudaEventDestroy(cl.done);
-    }
     tc_release(ctx->tc);
     for (void* p : ctx->allocs) cudaFree(p);
-    if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return 0;

@@ -133,34 +133,39 @@ template <bool INV> struct Dft<8, INV> { FFT_HD static void run(float2* v) { dft
 template <bool INV> struct Dft<16, INV> { FFT_HD static void run(float2* v) { dft_split<4, 4, INV>(v); } };
 
 // ------------------------------------------------------------------ radix plans
-// N = 2^a * 3^b (b <= 1).  With two or more factors of 16 the plan is 16, then the 3 and the
-// remaining 2/4/8, then the other 16s: first and last radix are equal, so two transforms can be
-// chained in registers (see fft_fused).  Otherwise: 3, then 16s, then the remainder.
-FFT_CHD constexpr int plan_n16(int n) {
-    if (n % 3 == 0) n /= 3;
-    int c = 0;
-    while (n % 16 == 0 && n >= 16) { c++; n /= 16; }
-    return c;
-}
-FFT_CHD constexpr int plan_rest(int n) {
-    if (n % 3 == 0) n /= 3;
-    while (n % 16 == 0 && n >= 16) n /= 16;
-    return n;
-}
-FFT_CHD constexpr int plan_len(int n) { return (n % 3 == 0 ? 1 : 0) + plan_n16(n) + (plan_rest(n) > 1 ? 1 : 0); }
-FFT_CHD constexpr int plan_radix(int n, int i) {
-    const int n16 = plan_n16(n), rest = plan_rest(n), three = n % 3 == 0 ? 1 : 0;
-    if (n16 >= 2) {
-        if (i == 0) return 16;
-        i -= 1;
-        if (three) { if (i == 0) return 3; i -= 1; }
-        if (rest > 1) { if (i == 0) return rest; i -= 1; }
-        return 16;
+// N = 2^a * 3^b (b <= 1).  Every plan starts and ends with the same "outer" radix -- 16 when the
+// power-of-two part p is at least 256, else 8 (p >= 64), 4 (p >= 16) or 2 -- with the 3, the
+// remaining factor of two and any further 16s in between: 4096 = 16.16.16, 3072 = 16.3.4.16,
+// 384 = 8.3.2.8, 96 = 4.3.2.4.  Equal first and last radix let two transforms be chained in
+// registers (fft_fused), which every size then does.
+struct Plan {
+    int len;
+    int r[12];
+};
+FFT_CHD constexpr Plan make_plan(int n) {
+    Plan P = {0, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
+    const bool three = n % 3 == 0;
+    const int p = three ? n / 3 : n;
+    const int outer = p >= 256 ? 16 : p >= 64 ? 8 : p >= 16 ? 4 : p >= 4 ? 2 : 0;
+    if (outer == 0) {  // p = 1 or 2: no pair of equal radices
+        if (three) P.r[P.len++] = 3;
+        if (p == 2) P.r[P.len++] = 2;
+        return P;
     }
-    if (three) { if (i == 0) return 3; i -= 1; }
-    if (i < n16) return 16;
-    return rest;
+    int q = p / (outer * outer), inner16 = 0;
+    while (outer == 16 && q >= 16 && q % 16 == 0) {
+        inner16++;
+        q /= 16;
+    }
+    P.r[P.len++] = outer;
+    if (three) P.r[P.len++] = 3;
+    if (q > 1) P.r[P.len++] = q;  // 2, 4 or 8
+    for (int i = 0; i < inner16; i++) P.r[P.len++] = 16;
+    P.r[P.len++] = outer;
+    return P;
 }
+FFT_CHD constexpr int plan_len(int n) { return make_plan(n).len; }
+FFT_CHD constexpr int plan_radix(int n, int i) { return make_plan(n).r[i]; }
 FFT_CHD constexpr int plan_L(int n, int i) {  // product of the radices before stage i
     int l = 1;
     for (int s = 0; s < i; s++) l *= plan_radix(n, s);
