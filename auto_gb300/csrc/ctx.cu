@@ -39,6 +39,7 @@ struct SizeClass {
     int nrow = 0;
     int var_col = 0, var_row = 0;  // launch variants (see launch_col_fp32)
     int nbuf = 1, general = 0, planes = 0;
+    int multi = 0;  // some channel is read by several kernels (column-pass variant bit 1)
 };
 
 struct WorldBuffers {
@@ -282,7 +283,7 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
                     int variant, cudaStream_t s) {
     bool ok = true;
     if (ntcg > 0) ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
-    return ok && launch_col_fp32(cl.H, variant, cl.nbuf, ctx->d_worlds, col, ncol, ctx->d_tw, s);
+    return ok && launch_col_fp32(cl.H, variant | (cl.multi ? 2 : 0), cl.nbuf, ctx->d_worlds, col, ncol, ctx->d_tw, s);
 }
 
 // Enqueue `steps` steps of every world on the context's streams (captured into graphs).
@@ -452,7 +453,7 @@ int setup_fused(LeniaCtx* ctx) {
     for (auto& cl : ctx->classes) {
         std::vector<ColItem> col, tcg;
         std::vector<RowItem> row;
-        int nbuf = 1, general = 0, planes = 0;
+        int nbuf = 1, general = 0, planes = 0, multi = 0;
         // tensor-core groups of CT columns, except the first group of every channel: column 0
         // packs the DC and Nyquist columns, which the FP32 pass pairs up (ky with H - ky)
         const bool use_tc = tc_path && tc_supports(cl.H);
@@ -464,7 +465,7 @@ int setup_fused(LeniaCtx* ctx) {
                 int nsrc = 0;
                 for (uint32_t k = 0; k < d.nkernels; k++) nsrc += d.kernels[k].src == (int)c;
                 if (nsrc == 0) continue;
-                if (nsrc > 1) nbuf = 2;
+                if (nsrc > 1) nbuf = 2, multi = 1;
                 const int ntiles = spec_tiles(d.width);
                 if (use_tc && ntiles % tpg == 0) {
                     for (int t = 0; t < tpg; t++) col.push_back(ColItem{wi, (int)c, t, 0});
@@ -487,13 +488,16 @@ int setup_fused(LeniaCtx* ctx) {
             return fail(ctx, LENIA_ESIZE, "%dx%d with %d planes needs more shared memory than a CTA has", cl.W, cl.H,
                         planes);
         cl.nbuf = nbuf;
+        cl.multi = multi;
         cl.general = general;
         cl.planes = planes;
         // Default launch variant: the 64-register form (more resident CTAs) unless it spills more
         // than 128 bytes a thread and the 128-register form spills less than half as much.
         auto pick = [](int v0, int v1) { return (v0 > 128 && v1 >= 0 && v1 < v0 / 2) ? 1 : 0; };
-        cl.var_col = pick(fp32_local_bytes(0, cl.H, 0), fp32_local_bytes(0, cl.H, 1));
-        cl.var_row = pick(fp32_local_bytes(1, cl.W, 0), fp32_local_bytes(1, cl.W, 1));
+        const int m2 = multi ? 2 : 0;
+        cl.var_col = pick(fp32_local_bytes(0, cl.H, m2), fp32_local_bytes(0, cl.H, 1 | m2));
+        const int g2 = general ? 2 : 0;
+        cl.var_row = pick(fp32_local_bytes(1, cl.W, g2), fp32_local_bytes(1, cl.W, 1 | g2));
         cl.ncol = (int)col.size();
         cl.nrow = (int)row.size();
         cl.ntcg = (int)tcg.size();
@@ -520,7 +524,8 @@ int setup_fused(LeniaCtx* ctx) {
         }
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
-            if (!launch_col_fp32(cl.H, v, cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
+            if (!launch_col_fp32(cl.H, v | (cl.multi ? 2 : 0), cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw,
+                                 ctx->stream) ||
                 !launch_row_fp32(cl.W, v, MODE_STEP, 0, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw, ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
         }

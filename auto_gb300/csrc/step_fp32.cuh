@@ -265,7 +265,11 @@ __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __r
     }
 }
 
-template <int W, int NT, int MINB>
+// GEN: the instantiation for size classes with worlds that need the general step (several
+// channels or kernels, SmoothLife, MNCA).  Without it the kernel carries only the one-channel,
+// one-kernel Lenia step (and the forward and U modes), so the general path's register pressure
+// does not set the budget of the common path.
+template <int W, int NT, int MINB, bool GEN>
 __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items,
                                                 int mode, int general, const float2* __restrict__ tw) {
     constexpr int S = row_seqs(W), ROWS = 2 * S;
@@ -323,7 +327,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         return;
     }
 
-    if (!general) {
+    if (!GEN || !general) {
         // One channel, one kernel, Lenia growth.
         const DevKernel kp = wd.kern[0];
         const float dtw = wd.dt * kp.weight, isig = 1.0f / kp.sigma;
@@ -389,6 +393,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     }
 
     // General: several channels and/or kernels, or a rule that needs every U at once.
+    if constexpr (!GEN) return;
     const int rule = wd.rule;
     const int planes = (rule == LENIA_RULE_LENIA) ? C : K;
     float* acc = extra;  // [planes][ROWS][W]
@@ -498,7 +503,11 @@ __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__
     }
 }
 
-template <int H, int NT, int MINB>
+// MULTI: the instantiation for size classes with a channel that several kernels read.  Without
+// it, every channel has exactly one kernel (the host guarantees this), and the kernel carries no
+// code for sharing one forward transform between kernels -- that code's register pressure would
+// otherwise set the register budget, and the spills, of the common single-kernel path.
+template <int H, int NT, int MINB, bool MULTI>
 __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
                                                 int nbuf, const float2* __restrict__ tw) {
     extern __shared__ float4 smem_raw[];
@@ -516,13 +525,14 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
     for (int k = K - 1; k >= 0; k--)
         if (wd.kern[k].src == c) nsrc++, k1 = k;
     if (nsrc == 0) return;
-    if constexpr (fusable<H>()) {
-        // One kernel on this channel, tile without the packed DC/Nyquist column: the khat multiply
-        // runs in registers between the forward and the inverse column FFT.  The tile's two khat
-        // columns (contiguous, HQ floats each) are copied to shared memory while the tile loads.
+    if (!MULTI || nsrc == 1) {
+        // One kernel on this channel.  Tiles without the packed DC/Nyquist column: the khat
+        // multiply runs in registers between the forward and the inverse column FFT, and the
+        // tile's two khat columns (contiguous, HQ floats each) are copied to shared memory while
+        // the tile loads.
         constexpr int HQC = khat_cols_stride<H>();
         const float* kh = wd.khat + ((size_t)k1 * (W / 2 + 1) + (size_t)TC * t) * HQC;
-        if (nsrc == 1 && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
+        if (fusable<H>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
             float* ksm = col_khat_smem<H>(stw);
             for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
             load_tile<H, NT>(X, src);
@@ -540,7 +550,17 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
             store_tile<H, NT>(X, wd.conv + k1 * cplane + (size_t)t * H * TC);
             return;
         }
+        // tile 0 (DC and Nyquist columns paired, ky with H - ky) or khat not 16-byte aligned
+        load_tile<H, NT>(X, src);
+        __syncthreads();
+        fft_seqs<H, TC, NT, false>(X, stw);
+        multiply_khat<H, NT>(X, X, wd.khat + (size_t)k1 * (W / 2 + 1) * HQ, HQ, W, t);
+        __syncthreads();
+        fft_seqs<H, TC, NT, true>(X, stw);
+        store_tile<H, NT>(X, wd.conv + k1 * cplane + (size_t)t * H * TC);
+        return;
     }
+    if constexpr (!MULTI) return;
     const bool reload = (nsrc > 1 && nbuf < 2);
     bool have = false;
     for (int k = 0; k < K; k++) {
@@ -574,17 +594,17 @@ template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) /
 
 // Launch one instantiation.  Dynamic shared memory above 48 KB must be enabled per kernel before
 // its first launch and before any stream capture that contains it; a zero-item call does just that.
-template <int H, int NT, int MINB>
+template <int H, int NT, int MINB, bool MULTI>
 bool col_go(int nbuf, const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
     const size_t smem = (size_t)nbuf * TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>() + col_khat_bytes<H>();
     static int attr_max = 0;
     if ((int)smem > attr_max) {
-        if (cudaFuncSetAttribute(col_pass<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(col_pass<H, NT, MINB, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return false;
         attr_max = (int)smem;
     }
-    if (nitems > 0) col_pass<H, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, nbuf, tw);
+    if (nitems > 0) col_pass<H, NT, MINB, MULTI><<<nitems, NT, smem, s>>>(worlds, items, nbuf, tw);
     return true;
 }
 
@@ -597,30 +617,39 @@ constexpr size_t row_smem(int general, int planes) {
            (size_t)(general ? planes : (fusable<W>() ? 0 : 1)) * rows * W * sizeof(float);
 }
 
-template <int W, int NT, int MINB>
+template <int W, int NT, int MINB, bool GEN>
 bool row_go(int mode, int general, int planes, const DevWorld* worlds, const RowItem* items, int nitems,
             const float2* tw, cudaStream_t s) {
     const size_t smem = row_smem<W>(general, planes);
     static int attr_max = 0;
     if ((int)smem > attr_max) {
-        if (cudaFuncSetAttribute(row_pass<W, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(row_pass<W, NT, MINB, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return false;
         attr_max = (int)smem;
     }
-    if (nitems > 0) row_pass<W, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, mode, general, tw);
+    if (nitems > 0) row_pass<W, NT, MINB, GEN><<<nitems, NT, smem, s>>>(worlds, items, mode, general, tw);
     return true;
 }
 
-#define LENIA_COL_CASE(N)                                                                                   \
-    case N:                                                                                                 \
-        return variant == 0 ? col_go<N, nt_of<N>(), minb_of<N, 0>()>(nbuf, worlds, items, nitems, tw, s)    \
-                            : col_go<N, nt_of<N>(), minb_of<N, 1>()>(nbuf, worlds, items, nitems, tw, s);
-#define LENIA_ROW_CASE(N)                                                                                   \
-    case N:                                                                                                 \
-        return variant == 0                                                                                 \
-                   ? row_go<N, row_nt<N>(), row_minb<N, 0>()>(mode, general, planes, worlds, items, nitems, tw, s) \
-                   : row_go<N, row_nt<N>(), row_minb<N, 1>()>(mode, general, planes, worlds, items, nitems, tw, s);
+// Column-pass variant: bit 0 selects the register cap (minb_of), bit 1 the MULTI instantiation.
+#define LENIA_COL_CASE(N)                                                                               \
+    case N:                                                                                             \
+        switch (variant & 3) {                                                                          \
+        case 0: return col_go<N, nt_of<N>(), minb_of<N, 0>(), false>(nbuf, worlds, items, nitems, tw, s); \
+        case 1: return col_go<N, nt_of<N>(), minb_of<N, 1>(), false>(nbuf, worlds, items, nitems, tw, s); \
+        case 2: return col_go<N, nt_of<N>(), minb_of<N, 0>(), true>(nbuf, worlds, items, nitems, tw, s);  \
+        default: return col_go<N, nt_of<N>(), minb_of<N, 1>(), true>(nbuf, worlds, items, nitems, tw, s); \
+        }
+// Row-pass variant: bit 0 selects the register cap (row_minb); the GEN build runs when `general`.
+#define LENIA_ROW_CASE(N)                                                                                        \
+    case N:                                                                                                      \
+        switch ((variant & 1) | (general ? 2 : 0)) {                                                             \
+        case 0: return row_go<N, row_nt<N>(), row_minb<N, 0>(), false>(mode, general, planes, worlds, items, nitems, tw, s); \
+        case 1: return row_go<N, row_nt<N>(), row_minb<N, 1>(), false>(mode, general, planes, worlds, items, nitems, tw, s); \
+        case 2: return row_go<N, row_nt<N>(), row_minb<N, 0>(), true>(mode, general, planes, worlds, items, nitems, tw, s);  \
+        default: return row_go<N, row_nt<N>(), row_minb<N, 1>(), true>(mode, general, planes, worlds, items, nitems, tw, s); \
+        }
 
 // Local memory (spills and stack) of one instantiation, bytes per thread; -1 if unknown.
 template <class F>
@@ -628,14 +657,22 @@ int local_bytes_of(F* f) {
     cudaFuncAttributes a;
     return cudaFuncGetAttributes(&a, f) == cudaSuccess ? (int)a.localSizeBytes : -1;
 }
-#define LENIA_COL_LOCAL_CASE(N)                                                    \
-    case N:                                                                        \
-        return variant == 0 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>) \
-                            : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
-#define LENIA_ROW_LOCAL_CASE(N)                                                          \
-    case N:                                                                              \
-        return variant == 0 ? local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>()>) \
-                            : local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>()>);
+#define LENIA_COL_LOCAL_CASE(N)                                                            \
+    case N:                                                                                \
+        switch (variant & 3) {                                                             \
+        case 0: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>(), false>);    \
+        case 1: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>(), false>);    \
+        case 2: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>(), true>);     \
+        default: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>(), true>);    \
+        }
+#define LENIA_ROW_LOCAL_CASE(N)                                                             \
+    case N:                                                                                 \
+        switch (variant & 3) {                                                              \
+        case 0: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>(), false>);   \
+        case 1: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>(), false>);   \
+        case 2: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>(), true>);    \
+        default: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>(), true>);   \
+        }
 int col_local_bytes_small(int H, int variant);
 int col_local_bytes_large(int H, int variant);
 int row_local_bytes_small(int W, int variant);
