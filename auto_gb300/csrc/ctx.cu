@@ -78,6 +78,14 @@ struct LeniaCtx {
     int graph_steps = 64;
     cudaGraphExec_t graph_big = nullptr, graph_one = nullptr;
     TcPlan tc;
+    // Worlds whose state changed since their half-spectrum was last formed.  The forward row
+    // transforms run at the next call that reads spectra (flush_spectra), one launch per size class
+    // when a whole class changed.
+    std::vector<char> dirty;
+    int ndirty = 0;
+    // all states back to back in world order (fused paths): one copy for every world
+    float* states = nullptr;
+    size_t states_count = 0;
 };
 
 namespace {
@@ -266,15 +274,41 @@ int world_from_ctx(const LeniaCtx* ctx, int32_t w) { return (w >= 0 && w < (int)
 
 size_t state_count(const LeniaWorldDesc& d) { return (size_t)d.channels * d.width * d.height; }
 
-// Forward row transform of one world (state -> spectrum), after its state changed.
+// A world's state changed: its half-spectrum is re-formed by the next flush_spectra.
 int refresh_spectrum(LeniaCtx* ctx, int w) {
     if (ctx->path == LENIA_PATH_RADIX2) return 0;
-    const WorldBuffers& b = ctx->wb[w];
-    const SizeClass& cl = ctx->classes[b.cls];
-    if (!launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw,
-                         ctx->stream))
-        return fail(ctx, LENIA_ECUDA, "row transform launch failed for %dx%d", cl.W, cl.H);
+    if (!ctx->dirty[w]) {
+        ctx->dirty[w] = 1;
+        ctx->ndirty++;
+    }
+    return 0;
+}
+
+// Forward row transforms (state -> half-spectrum) of every changed world: one launch for a size
+// class whose worlds all changed, else one launch per changed world.
+int flush_spectra(LeniaCtx* ctx) {
+    if (ctx->ndirty == 0) return 0;
+    for (const SizeClass& cl : ctx->classes) {
+        size_t n = 0;
+        for (int w : cl.worlds) n += ctx->dirty[w] ? 1 : 0;
+        if (n == 0) continue;
+        bool ok = true;
+        if (n == cl.worlds.size()) {
+            ok = launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, 0, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+                                 ctx->d_tw, ctx->stream);
+        } else {
+            for (int w : cl.worlds) {
+                if (!ctx->dirty[w]) continue;
+                const WorldBuffers& b = ctx->wb[w];
+                ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, 0, ctx->d_worlds, b.d_row, b.nrow,
+                                           cl.planes, ctx->d_tw, ctx->stream);
+            }
+        }
+        if (!ok) return fail(ctx, LENIA_ECUDA, "row transform launch failed for %dx%d", cl.W, cl.H);
+    }
     CK(cudaGetLastError());
+    std::fill(ctx->dirty.begin(), ctx->dirty.end(), 0);
+    ctx->ndirty = 0;
     return 0;
 }
 
@@ -358,13 +392,18 @@ int setup_fused(LeniaCtx* ctx) {
     }
     const int smem_max = max_smem_optin();
     // per-world buffers: a sizing pass, one arena, then the same calls carve it
+    // every world's state first, back to back in world order (each a multiple of 256 bytes), so
+    // that lenia_write_states / lenia_read_states are one copy each
     auto world_buffers = [&](void) -> int {
         for (int i = 0; i < nw; i++) {
             const LeniaWorldDesc& d = ctx->desc[i];
+            int rc = dalloc(ctx, &ctx->hw[i].state, (size_t)d.width * d.height * d.channels);
+            if (rc) return rc;
+        }
+        for (int i = 0; i < nw; i++) {
+            const LeniaWorldDesc& d = ctx->desc[i];
             DevWorld& w = ctx->hw[i];
-            const size_t cells = (size_t)d.width * d.height;
             int rc;
-            if ((rc = dalloc(ctx, &w.state, cells * d.channels))) return rc;
             if ((rc = dalloc(ctx, &w.spec, spec_elems(d.width, d.height) * d.channels))) return rc;
             if (d.channels == 1 && d.nkernels == 1) w.conv = w.spec;
             else if ((rc = dalloc(ctx, &w.conv, spec_elems(d.width, d.height) * d.nkernels))) return rc;
@@ -648,8 +687,19 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         rc = tc_setup(ctx->tc, path, &ctx->err);
         if (rc) return bail(rc);
     }
+    ctx->dirty.assign(nworlds, 0);
     rc = (path == LENIA_PATH_RADIX2) ? setup_radix2(ctx) : setup_fused(ctx);
     if (rc) return bail(rc);
+    if (path != LENIA_PATH_RADIX2) {
+        // the states were carved back to back from the arena (checked, not assumed)
+        bool packed = true;
+        size_t off = 0;
+        for (int w = 0; w < nworlds; w++) {
+            packed = packed && ctx->hw[w].state == ctx->hw[0].state + off;
+            off += state_count(ctx->desc[w]);
+        }
+        if (packed) ctx->states = ctx->hw[0].state, ctx->states_count = off;
+    }
     if ((rc = dalloc(ctx, &ctx->d_stats, 3 * (size_t)nworlds))) return bail(rc);
     if ((rc = rebuild_graphs(ctx))) return bail(rc);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
@@ -707,8 +757,48 @@ int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, size_t cou
     return 0;
 }
 
+int lenia_write_states(LeniaCtx* ctx, const float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    size_t total = 0;
+    for (const auto& d : ctx->desc) total += state_count(d);
+    if (!host || count != total) return fail(ctx, LENIA_EINVAL, "the worlds hold %zu state values, got %zu", total, count);
+    if (ctx->states) {
+        CK(cudaMemcpyAsync(ctx->states, host, count * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        size_t off = 0;
+        for (size_t w = 0; w < ctx->desc.size(); w++) {
+            const size_t n = state_count(ctx->desc[w]);
+            CK(cudaMemcpyAsync(state_ptr(ctx, (int)w), host + off, n * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+            off += n;
+        }
+    }
+    for (size_t w = 0; w < ctx->desc.size(); w++) refresh_spectrum(ctx, (int)w);
+    return 0;
+}
+
+int lenia_read_states(LeniaCtx* ctx, float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    size_t total = 0;
+    for (const auto& d : ctx->desc) total += state_count(d);
+    if (!host || count != total) return fail(ctx, LENIA_EINVAL, "the worlds hold %zu state values, got %zu", total, count);
+    if (ctx->states) {
+        CK(cudaMemcpyAsync(host, ctx->states, count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+    } else {
+        size_t off = 0;
+        for (size_t w = 0; w < ctx->desc.size(); w++) {
+            const size_t n = state_count(ctx->desc[w]);
+            CK(cudaMemcpyAsync(host + off, state_ptr(ctx, (int)w), n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+            off += n;
+        }
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    return tc_check_error(ctx->tc, &ctx->err);
+}
+
 int lenia_step(LeniaCtx* ctx, uint32_t steps) {
     if (!ctx) return LENIA_EINVAL;
+    int frc = flush_spectra(ctx);
+    if (frc) return frc;
     uint32_t full = steps / ctx->graph_steps, rem = steps % ctx->graph_steps;
     for (uint32_t i = 0; i < full; i++) CK(cudaGraphLaunch(ctx->graph_big, ctx->stream));
     for (uint32_t i = 0; i < rem; i++) CK(cudaGraphLaunch(ctx->graph_one, ctx->stream));
@@ -718,6 +808,8 @@ int lenia_step(LeniaCtx* ctx, uint32_t steps) {
 
 int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms) {
     if (!ctx || !ms) return LENIA_EINVAL;
+    int frc = flush_spectra(ctx);  // outside the timed region
+    if (frc) return frc;
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
     CK(cudaEventCreate(&b));
@@ -843,6 +935,8 @@ int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host
         CK(cudaStreamSynchronize(ctx->stream));
         return 0;
     }
+    int frc = flush_spectra(ctx);
+    if (frc) return frc;
     DevWorld& w = ctx->hw[world];
     if (!w.u_out) {
         int rc = dalloc(ctx, &w.u_out, cells * d.nkernels);
@@ -870,6 +964,8 @@ int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel, float* ho
     if (channel < 0 || channel >= (int)d.channels) return fail(ctx, LENIA_EINVAL, "no channel %d", channel);
     const int W = d.width, H = d.height, KX = W / 2 + 1;
     if (!host || count != (size_t)H * KX * 2) return fail(ctx, LENIA_EINVAL, "spectrum has %d values", H * KX * 2);
+    int frc = flush_spectra(ctx);
+    if (frc) return frc;
     std::vector<float2> tiles(spec_elems(W, H));
     CK(cudaMemcpyAsync(tiles.data(), ctx->hw[world].spec + (size_t)channel * spec_elems(W, H), tiles.size() * sizeof(float2),
                        cudaMemcpyDeviceToHost, ctx->stream));
@@ -904,6 +1000,10 @@ int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count) {
 
 int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
     if (!ctx || !out3 || steps == 0) return LENIA_EINVAL;
+    {
+        int frc = flush_spectra(ctx);
+        if (frc) return frc;
+    }
     if (ctx->path == LENIA_PATH_RADIX2) {
         cudaEvent_t a, b;
         CK(cudaEventCreate(&a));
@@ -982,6 +1082,10 @@ int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const 
 int lenia_autotune(LeniaCtx* ctx) {
     if (!ctx) return LENIA_EINVAL;
     if (ctx->path == LENIA_PATH_RADIX2) return 0;
+    {
+        int frc = flush_spectra(ctx);
+        if (frc) return frc;
+    }
     // Try both built thread counts for each class's column and row launches; keep the fastest.
     // The trial steps advance the worlds, so save and restore every state.
     std::vector<std::vector<float>> saved(ctx->desc.size());

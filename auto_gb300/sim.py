@@ -103,6 +103,20 @@ class Sim:
         self._check(self._L.lenia_read_state(self._ctx, world, fptr(out), out.size))
         return out
 
+    def read_states(self, out: np.ndarray = None) -> np.ndarray:
+        """Every world's state, back to back in world order, as one flat float32 array."""
+        n = sum(w.channels * w.height * w.width for w in self.worlds)
+        if out is None:
+            out = np.empty(n, np.float32)
+        self._check(self._L.lenia_read_states(self._ctx, fptr(out), out.size))
+        return out
+
+    def write_states(self, states: np.ndarray):
+        """Write every world's state from one flat array (world order, as read_states returns)."""
+        a = np.ascontiguousarray(states, np.float32).ravel()
+        self._check(self._L.lenia_write_states(self._ctx, fptr(a), a.size))
+        self.wait()
+
     def write_state(self, world: int, state: np.ndarray):
         a = np.ascontiguousarray(state, np.float32).ravel()
         self._check(self._L.lenia_write_state(self._ctx, world, fptr(a), a.size))

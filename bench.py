@@ -8,8 +8,14 @@ Printed JSON (one line, rank 0):
   value   cell-updates/s with the state resident in HBM, from CUDA events on the engine stream
           around the K timed bench steps, max over ranks
   e2e     the same metric through the public C ABI with host buffers: every bench step writes
-          each world's state from pinned host memory, runs G generations and reads the state back
-  roofline, cpu_baseline, clocks, gpu_launches: see the design doc
+          every world's state from one pinned host buffer (lenia_write_states), runs G generations
+          and reads every state back (lenia_read_states)
+  roofline  12 algorithmic bytes per cell-update (state read and written, one complex f32
+          half-spectrum value) over the event-timed generation time, against the measured HBM
+          copy bandwidth; traffic = DRAM bytes per generation from an ncu capture
+  cpu_baseline  the CPU restatement of the reference step on the host cores, bounded sample
+  clocks  SM clock and throttle reasons sampled with nvidia-smi during the timed region
+  gpu_launches  kernel launches in the timed region (two per size class per generation)
 
 ``--impl reference`` times the reference's step as restated on the CPU (the reference itself is
 Rust + WGSL on Vulkan and cannot run here) on all host cores, on the same workload.
@@ -347,26 +353,23 @@ def run_ours(args, dist):
     e2e = None
     if not args.no_e2e:
         import torch
-        host = []
-        for w in worlds:
-            t = torch.empty(w.channels * w.height * w.width, dtype=torch.float32, pin_memory=True)
-            a = t.numpy()
-            a[:] = sim.read_state(worlds.index(w)).ravel()
-            host.append((t, a))
+        # every world's state in one pinned host buffer, world after world
+        pinned = torch.empty(sum(w.channels * w.height * w.width for w in worlds), dtype=torch.float32,
+                             pin_memory=True)
+        a = pinned.numpy()
+        sim.read_states(a)
         L = sim._L
         from auto_gb300._lib import check, fptr
         device_sync()
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            for i, (_, a) in enumerate(host):
-                check(L.lenia_write_state(sim._ctx, i, fptr(a), a.size), sim._ctx)
+            check(L.lenia_write_states(sim._ctx, fptr(a), a.size), sim._ctx)
             check(L.lenia_step(sim._ctx, G), sim._ctx)
-            for i, (_, a) in enumerate(host):
-                check(L.lenia_read_state(sim._ctx, i, fptr(a), a.size), sim._ctx)
+            check(L.lenia_read_states(sim._ctx, fptr(a), a.size), sim._ctx)
         device_sync()
         t_e2e = dist.max(time.perf_counter() - t0)
-        nbytes = sum(a.nbytes for _, a in host)
+        nbytes = a.nbytes
         e2e = {"value": total_cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes,
                "d2h_bytes_per_step": nbytes, "gens_per_step": G}
 

@@ -104,6 +104,12 @@ LENIA_API int lenia_read_state(LeniaCtx* ctx, int32_t world, float* host, size_t
 /* Same with a device pointer on the caller's side (no host staging). */
 LENIA_API int lenia_write_state_device(LeniaCtx* ctx, int32_t world, const float* dev, size_t count);
 LENIA_API int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, size_t count);
+/* write_field / read_field of every world at once: the states back to back in world order
+ * (count = the sum of channels*height*width).  One host<->device copy and, for the read, one
+ * synchronisation, where a per-world loop would pay one of each per world.  The reference has
+ * one world per Sim, so its nearest equivalent is a loop of write_field / read_field calls. */
+LENIA_API int lenia_write_states(LeniaCtx* ctx, const float* host, size_t count);
+LENIA_API int lenia_read_states(LeniaCtx* ctx, float* host, size_t count);
 
 /* Sim::step (sim.rs:297-309): advance every world by `steps`, asynchronously.  Steps are
  * replayed from CUDA graphs of up to 64 steps each. */

@@ -159,6 +159,44 @@ def test_batched_worlds_equal_one_at_a_time():
             assert np.array_equal(one.read_state(0), batched[i]), i
 
 
+def test_all_world_state_calls_match_per_world_calls():
+    # lenia_write_states / lenia_read_states (one copy for every world) against the per-world calls,
+    # and the deferred spectrum refresh: partial rewrites, whole-context rewrites, then steps
+    worlds = configs.batched(40)
+    rng = np.random.default_rng(5)
+    states = [rng.random((w.channels, w.height, w.width), dtype=np.float32) for w in worlds]
+    flat = np.concatenate([s.ravel() for s in states])
+    with Sim(worlds, seed=0) as a, Sim(worlds, seed=0) as b:
+        a.write_states(flat)
+        for i, s in enumerate(states):
+            b.write_state(i, s)
+        assert np.array_equal(a.read_states(), flat)
+        a.step(3)
+        b.step(3)
+        got = a.read_states()
+        off = 0
+        for i, w in enumerate(worlds):
+            n = w.channels * w.height * w.width
+            assert np.array_equal(got[off:off + n], b.read_state(i).ravel()), i
+            off += n
+        # rewrite a few worlds only (one launch per changed world), then step both again
+        for i in (0, 7, 39):
+            a.write_state(i, states[i])
+            b.write_state(i, states[i])
+        a.step(2)
+        b.step(2)
+        got = a.read_states()
+        off = 0
+        for i, w in enumerate(worlds):
+            n = w.channels * w.height * w.width
+            assert np.array_equal(got[off:off + n], b.read_state(i).ravel()), i
+            off += n
+        with pytest.raises(LeniaError):
+            a.write_states(flat[:-1])
+        with pytest.raises(LeniaError):
+            a.read_states(np.empty(flat.size + 1, np.float32))
+
+
 def test_batched_worlds_teacher_forced_vs_fp64():
     worlds = configs.batched(32)
     with Sim(worlds, seed=0) as sim:
