@@ -39,6 +39,13 @@ if ROOT not in sys.path:
 METRIC = "Lenia cell-updates/s on 1 GB300, batched TC vs plain FP32, at ≤1e-4 vs FP64"
 UNIT = "cell-updates/s"
 ALG_BYTES_PER_UPDATE = 12.0  # state read + write (8 B) + one f32 complex half-spectrum of the kernel (4 B)
+
+
+def alg_bytes_per_gen(worlds):
+    """Algorithmic bytes of one generation: (8 C + 4 K) H W per world -- every channel's state read and
+    written once, plus one f32 complex half-spectrum (4 B per cell) per kernel.  12 B per cell-update
+    for one channel and one kernel; 20 B per channel-cell for 3 channels and 9 kernels."""
+    return sum((8.0 * w.channels + 4.0 * len(w.kernels)) * w.width * w.height for w in worlds)
 PUBLISHED_REF = {"lenia_4096x4096_R13": 3.174e8, "hardware": "AMD RX 7900 XT (wgpu/Vulkan)",
                  "source": "results/gpu.jsonl:81"}
 
@@ -338,11 +345,12 @@ def run_ours(args, dist):
     hbm = peaks.get("hbm_gbs")
     peak_src = "measured" if hbm else "fallback"
     hbm = hbm or 6800.0
-    achieved = cells * ALG_BYTES_PER_UPDATE / (ms_per_gen * 1e-3) / 1e9
+    achieved = alg_bytes_per_gen(worlds) / (ms_per_gen * 1e-3) / 1e9
     traffic = read_traffic().get("%s/%s" % (args.config, args.path))
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                 "traffic": traffic, "peak_source": peak_src,
-                "what": "whole step (column + row launch) as the unit: 12 B per cell-update over the event-timed "
+                "what": "whole step (column + row launch) as the unit: (8 C + 4 K) H W bytes per world-generation "
+                        "(12 B per cell-update at C = K = 1) over the event-timed "
                         "generation time",
                 "kernels": {"column_ms": col_ms, "row_ms": row_ms, "step_ms_serial": step_ms,
                             "column_share": col_ms / step_ms if step_ms else None,
@@ -400,6 +408,22 @@ def run_ours(args, dist):
             paths["bf16x3_over_radix2"] = paths["bf16x3"]["value"] / paths["radix2"]["value"]
         if paths.get("bf16x3", {}).get("value") and paths.get("fp32", {}).get("value"):
             paths["bf16x3_over_fp32"] = paths["bf16x3"]["value"] / paths["fp32"]["value"]
+        if len(worlds) > 1 and args.path != "radix2":
+            # the same worlds one at a time, each alone in its own context (every k-th world, up to 48)
+            pick = list(range(0, len(worlds), max(1, len(worlds) // 48)))[:48]
+            one_ms, one_cells = 0.0, 0
+            for i in pick:
+                with Sim(worlds[i], seed=0, path=args.path) as one:
+                    seed_all(one, [worlds[i]], [seeds[i]])
+                    one.step(G)
+                    one.wait()
+                    one_ms += one.step_timed(2 * G)
+                    one_cells += one.cells_per_step * 2 * G
+            one_value = one_cells / (one_ms * 1e-3)
+            paths["one_at_a_time"] = {"value": one_value, "worlds": len(pick),
+                                      "what": "each sampled world alone in a context, %d generations each, "
+                                              "summed cell-updates over summed event time" % (2 * G)}
+            paths["batched_over_one_at_a_time"] = value / one_value
 
     cpu = None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu:
