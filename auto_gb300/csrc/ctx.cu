@@ -513,10 +513,14 @@ int setup_fused(LeniaCtx* ctx) {
                     for (int t = 0; t < ntiles; t++) col.push_back(ColItem{wi, (int)c, t, 0});
                 }
             }
-            for (uint32_t r = 0; r < d.height; r += (uint32_t)row_item_rows((int)d.width)) row.push_back(RowItem{wi, (int)r});
+            // Lenia: one row item per target channel (its kernels, update and forward transform), so a
+            // multichannel world has C times the row items; other rules: one item for every channel
+            const uint32_t split = d.rule == LENIA_RULE_LENIA ? d.channels : 1;
+            for (uint32_t r = 0; r < d.height; r += (uint32_t)row_item_rows((int)d.width))
+                for (uint32_t c = 0; c < split; c++) row.push_back(RowItem{wi, (int)r, (int)c, 0});
             const bool simple = d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA;
             if (!simple) general = 1;
-            planes = std::max(planes, (int)(simple ? 0 : (d.rule == LENIA_RULE_LENIA ? d.channels : d.nkernels)));
+            planes = std::max(planes, (int)(simple ? 0 : (d.rule == LENIA_RULE_LENIA ? 1 : d.nkernels)));
             WorldBuffers& b = ctx->wb[wi];
             b.ncol = (int)col.size() - first_col;
             b.nrow = (int)row.size() - first_row;

@@ -41,7 +41,10 @@ constexpr int TC = 2;
 
 // Work items.  Column pass: (world, channel, tile of TC columns).  Row pass: (world, first of 4 rows).
 struct ColItem { int world, chan, tile, pad; };
-struct RowItem { int world, row0; };
+// A row item: rows row0.. of one world.  For Lenia worlds one item per target channel `chan`
+// (its kernels, its state update and its forward transform); other rules use chan = 0 and every
+// channel.
+struct RowItem { int world, row0, chan, pad; };
 
 enum RowMode { MODE_STEP = 0, MODE_FORWARD = 1, MODE_U = 2 };
 
@@ -59,7 +62,6 @@ size_t row_smem_bytes(int W, int acc_planes);
 int row_item_rows(int W);  // rows per row-pass item (two per packed sequence)
 int fp32_local_bytes(int row, int n, int variant);  // spill/stack bytes per thread of a pass instantiation
 int max_smem_optin();
-int threads_for(int n);  // threads per CTA of the transforms of length n
 
 // Seeding and statistics (seed.cu).
 void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* patches, int npatch,

@@ -34,15 +34,6 @@ int max_smem_optin() {
     return v;
 }
 
-int threads_for(int n) {
-    switch (n) {
-#define NT_CASE(N) case N: return nt_of<N>();
-        LENIA_SIZES_SMALL(NT_CASE) LENIA_SIZES_LARGE(NT_CASE)
-#undef NT_CASE
-    }
-    return 0;
-}
-
 bool launch_col_fp32(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
                      const float2* tw, cudaStream_t s) {
     return launch_col_group_small(H, variant, nbuf, worlds, items, nitems, tw, s) ||

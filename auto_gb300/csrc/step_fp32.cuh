@@ -205,8 +205,8 @@ constexpr int row_minb() {
     constexpr int t = V == 0 ? 1024 : 512;
     return t / row_nt<W>() < 1 ? 1 : t / row_nt<W>();
 }
-// Shared memory after the sequences and stage tables: the state rows of the fast path at widths
-// that cannot chain their FFTs, or the accumulation planes ([planes][2S][W]) of the general path.
+// Shared memory after the sequences and stage tables: the accumulation planes ([planes][2S][W]) of
+// the general path.
 template <int W>
 __device__ __forceinline__ float* row_extra_smem(float2* stw) {
     return reinterpret_cast<float*>(((uintptr_t)(stw + tw_table_size(W)) + 15) & ~(uintptr_t)15);
@@ -293,9 +293,12 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     const DevWorld& wd = worlds[it.world];
     const int H = wd.H, C = wd.C, K = wd.K, r0 = it.row0;
     const size_t plane = (size_t)W * H, cplane = (size_t)(W / 2) * H;
+    // Lenia items cover one target channel; SmoothLife and MNCA items every channel
+    const bool per_chan = wd.rule == LENIA_RULE_LENIA;
+    const int d0 = per_chan ? it.chan : 0, d1 = per_chan ? it.chan + 1 : C;
 
     if (mode == MODE_FORWARD) {
-        for (int d = 0; d < C; d++) {
+        for (int d = d0; d < d1; d++) {
             const float* st = wd.state + d * plane + (size_t)r0 * W;
             constexpr int IT = (S * W + NT - 1) / NT;
             float a[IT], b[IT];
@@ -322,6 +325,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
 
     if (mode == MODE_U) {
         for (int k = 0; k < K; k++) {
+            if (per_chan && wd.kern[k].dst != d0) continue;
             load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
             __syncthreads();
             fft_seqs<W, S, NT, true>(Z, stw);
@@ -344,10 +348,12 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         const Growth growth(kp.mu, kp.sigma);
         float* st = wd.state + (size_t)r0 * W;
         const uint64_t stream = hint::policy_stream();
-        if constexpr (fusable<W>()) {
-            // The growth update runs in registers between the inverse and the forward row FFT.  The
-            // item's state rows are pulled into L2 when the CTA starts, and each thread's 2 x R state
-            // values are loaded into registers just before the last inverse stage.
+        {
+            // The growth update runs in registers between the inverse and the forward row FFT (every
+            // built width has a plan with equal first and last radix).  The item's state rows are
+            // pulled into L2 when the CTA starts, and each thread's 2 x R state values are loaded into
+            // registers just before the last inverse stage.
+            static_assert(fusable<W>(), "row widths need a plan with equal first and last radix");
             constexpr int R = plan_radix(W, 0), NB = W / R;
             static_assert(S * NB <= NT, "one butterfly per thread in the fused stage");
             if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, ROWS * W * (uint32_t)sizeof(float));
@@ -376,41 +382,19 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
             store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
             return;
         }
-        // Other widths: the item's state rows (contiguous) are staged in shared memory while the
-        // spectrum loads and the inverse FFT run.
-        float* ss = extra;  // [ROWS][W]
-        if (((uintptr_t)st & 15) == 0) {
-            for (int e = threadIdx.x; e < ROWS * W / 4; e += NT) cp_async16(ss + 4 * e, st + 4 * e);
-        } else {
-            for (int e = threadIdx.x; e < ROWS * W; e += NT) ss[e] = st[e];
-        }
-        load_rows_spectrum<W, S, NT>(Z, wd.conv, H, r0);
-        cp_async_wait_all();
-        __syncthreads();
-        fft_seqs<W, S, NT, true>(Z, stw);
-        for (int e = threadIdx.x; e < S * W; e += NT) {
-            const int p = e / W, x = e - p * W;
-            const float2 u = Z[p * SEQ + pad(x)];
-            const float n0 = __saturatef(fmaf(dtw, growth(u.x), ss[(2 * p) * W + x]));
-            const float n1 = __saturatef(fmaf(dtw, growth(u.y), ss[(2 * p + 1) * W + x]));
-            hint::st1(st + (2 * p) * W + x, n0, stream);
-            hint::st1(st + (2 * p + 1) * W + x, n1, stream);
-            Z[p * SEQ + pad(x)] = make_float2(n0, n1);
-        }
-        __syncthreads();
-        fft_seqs<W, S, NT, false>(Z, stw);
-        store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
-        return;
     }
 
-    // General: several channels and/or kernels, or a rule that needs every U at once.
+    // General: several channels and/or kernels, or a rule that needs every U at once.  Lenia: the
+    // kernels that target this item's channel add their weighted growth into one plane; SmoothLife
+    // and MNCA keep each kernel's U.
     if constexpr (!GEN) return;
     const int rule = wd.rule;
-    const int planes = (rule == LENIA_RULE_LENIA) ? C : K;
+    const int planes = (rule == LENIA_RULE_LENIA) ? 1 : K;
     float* acc = extra;  // [planes][ROWS][W]
     for (int e = threadIdx.x; e < planes * ROWS * W; e += NT) acc[e] = 0.0f;
     for (int k = 0; k < K; k++) {
         const DevKernel kp = wd.kern[k];
+        if (per_chan && kp.dst != d0) continue;
         const Growth growth(kp.mu, kp.sigma);
         load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
         __syncthreads();
@@ -419,7 +403,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
             const int p = e / W, x = e - p * W;
             const float2 u = Z[p * SEQ + pad(x)];
             if (rule == LENIA_RULE_LENIA) {
-                float* a = acc + (size_t)kp.dst * ROWS * W;
+                float* a = acc;
                 a[(2 * p) * W + x] += kp.weight * growth(u.x);
                 a[(2 * p + 1) * W + x] += kp.weight * growth(u.y);
             } else {
@@ -430,7 +414,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         }
         __syncthreads();
     }
-    for (int d = 0; d < C; d++) {
+    for (int d = d0; d < d1; d++) {
         float* st = wd.state + d * plane + (size_t)r0 * W;
         for (int e = threadIdx.x; e < S * W; e += NT) {
             const int p = e / W, x = e - p * W;
@@ -439,7 +423,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
             for (int q = 0; q < 2; q++) {
                 const int r = 2 * p + q;
                 const float s = st[r * W + x];
-                if (rule == LENIA_RULE_LENIA) n[q] = clamp01(s + wd.dt * acc[(size_t)d * ROWS * W + r * W + x]);
+                if (rule == LENIA_RULE_LENIA) n[q] = clamp01(s + wd.dt * acc[r * W + x]);
                 else if (rule == LENIA_RULE_SMOOTHLIFE) n[q] = smoothlife_update(s, acc[r * W + x], acc[ROWS * W + r * W + x]);
                 else n[q] = mnca_update(s, acc[r * W + x], acc[ROWS * W + r * W + x]);
                 st[r * W + x] = n[q];
@@ -620,12 +604,12 @@ bool col_go(int nbuf, const DevWorld* worlds, const ColItem* items, int nitems, 
 }
 
 // Shared memory of a row-pass launch: sequences, stage tables, then the general path's
-// accumulation planes or the fast path's staged state rows.
+// accumulation planes.
 template <int W>
 constexpr size_t row_smem(int general, int planes) {
     const int rows = 2 * row_seqs(W);
     return (size_t)row_seqs(W) * seq_stride(W) * sizeof(float2) + stage_table_bytes<W>() +
-           (size_t)(general ? planes : (fusable<W>() ? 0 : 1)) * rows * W * sizeof(float);
+           (size_t)(general ? planes : 0) * rows * W * sizeof(float);
 }
 
 template <int W, int NT, int MINB, bool GEN>
