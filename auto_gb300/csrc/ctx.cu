@@ -38,8 +38,7 @@ struct SizeClass {
     RowItem* d_row = nullptr;
     int nrow = 0;
     int var_col = 0, var_row = 0;  // launch variants (see launch_col_fp32)
-    int nbuf = 1, general = 0, planes = 0;
-    int multi = 0;  // some channel is read by several kernels (column-pass variant bit 1)
+    int general = 0, planes = 0;
 };
 
 struct WorldBuffers {
@@ -317,7 +316,7 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
                     int variant, cudaStream_t s) {
     bool ok = true;
     if (ntcg > 0) ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
-    return ok && launch_col_fp32(cl.H, variant | (cl.multi ? 2 : 0), cl.nbuf, ctx->d_worlds, col, ncol, ctx->d_tw, s);
+    return ok && launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
 }
 
 // Enqueue `steps` steps of every world on the context's streams (captured into graphs).
@@ -492,7 +491,7 @@ int setup_fused(LeniaCtx* ctx) {
     for (auto& cl : ctx->classes) {
         std::vector<ColItem> col, tcg;
         std::vector<RowItem> row;
-        int nbuf = 1, general = 0, planes = 0, multi = 0;
+        int general = 0, planes = 0;
         // tensor-core groups of CT columns, except the first group of every channel: column 0
         // packs the DC and Nyquist columns, which the FP32 pass pairs up (ky with H - ky)
         const bool use_tc = tc_path && tc_supports(cl.H);
@@ -500,18 +499,19 @@ int setup_fused(LeniaCtx* ctx) {
         for (int wi : cl.worlds) {
             const LeniaWorldDesc& d = ctx->desc[wi];
             const int first_col = (int)col.size(), first_row = (int)row.size(), first_tcg = (int)tcg.size();
+            // FP32 column items: one per (channel tile, kernel reading that channel); the tensor-core
+            // groups cover every kernel of a channel in one item
             for (uint32_t c = 0; c < d.channels; c++) {
-                int nsrc = 0;
-                for (uint32_t k = 0; k < d.nkernels; k++) nsrc += d.kernels[k].src == (int)c;
-                if (nsrc == 0) continue;
-                if (nsrc > 1) nbuf = 2, multi = 1;
                 const int ntiles = spec_tiles(d.width);
-                if (use_tc && ntiles % tpg == 0) {
-                    for (int t = 0; t < tpg; t++) col.push_back(ColItem{wi, (int)c, t, 0});
-                    for (int t = tpg; t < ntiles; t += tpg) tcg.push_back(ColItem{wi, (int)c, t, 0});
-                } else {
-                    for (int t = 0; t < ntiles; t++) col.push_back(ColItem{wi, (int)c, t, 0});
+                const bool tc_here = use_tc && ntiles % tpg == 0;
+                bool read = false;
+                for (uint32_t k = 0; k < d.nkernels; k++) {
+                    if (d.kernels[k].src != (int)c) continue;
+                    read = true;
+                    for (int t = 0; t < (tc_here ? tpg : ntiles); t++) col.push_back(ColItem{wi, (int)c, t, (int)k});
                 }
+                if (read && tc_here)
+                    for (int t = tpg; t < ntiles; t += tpg) tcg.push_back(ColItem{wi, (int)c, t, 0});
             }
             // Lenia: one row item per target channel (its kernels, update and forward transform), so a
             // multichannel world has C times the row items; other rules: one item for every channel
@@ -526,19 +526,15 @@ int setup_fused(LeniaCtx* ctx) {
             b.nrow = (int)row.size() - first_row;
             b.ntcg = (int)tcg.size() - first_tcg;
         }
-        if ((int)col_smem_bytes(cl.H, nbuf) > smem_max) nbuf = 1;
-        if ((int)col_smem_bytes(cl.H, 1) > smem_max || (int)row_smem_bytes(cl.W, planes) > smem_max)
+        if ((int)col_smem_bytes(cl.H) > smem_max || (int)row_smem_bytes(cl.W, planes) > smem_max)
             return fail(ctx, LENIA_ESIZE, "%dx%d with %d planes needs more shared memory than a CTA has", cl.W, cl.H,
                         planes);
-        cl.nbuf = nbuf;
-        cl.multi = multi;
         cl.general = general;
         cl.planes = planes;
         // Default launch variant: the 64-register form (more resident CTAs) unless it spills more
         // than 128 bytes a thread and the 128-register form spills less than half as much.
         auto pick = [](int v0, int v1) { return (v0 > 128 && v1 >= 0 && v1 < v0 / 2) ? 1 : 0; };
-        const int m2 = multi ? 2 : 0;
-        cl.var_col = pick(fp32_local_bytes(0, cl.H, m2), fp32_local_bytes(0, cl.H, 1 | m2));
+        cl.var_col = pick(fp32_local_bytes(0, cl.H, 0), fp32_local_bytes(0, cl.H, 1));
         const int g2 = general ? 2 : 0;
         cl.var_row = pick(fp32_local_bytes(1, cl.W, g2), fp32_local_bytes(1, cl.W, 1 | g2));
         cl.ncol = (int)col.size();
@@ -567,8 +563,7 @@ int setup_fused(LeniaCtx* ctx) {
         }
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
-            if (!launch_col_fp32(cl.H, v | (cl.multi ? 2 : 0), cl.nbuf, ctx->d_worlds, cl.d_col, 0, ctx->d_tw,
-                                 ctx->stream) ||
+            if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
                 !launch_row_fp32(cl.W, v, MODE_STEP, 0, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw, ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
         }

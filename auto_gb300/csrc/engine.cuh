@@ -39,8 +39,10 @@ struct DevWorld {
 // Spectrum columns per tile: a column pass CTA transforms TC columns of length H.
 constexpr int TC = 2;
 
-// Work items.  Column pass: (world, channel, tile of TC columns).  Row pass: (world, first of 4 rows).
-struct ColItem { int world, chan, tile, pad; };
+// Work items.
+// A column item: spectrum tile `tile` of channel `chan` with kernel `kernel` (FP32 pass); the
+// tensor-core groups use world, chan and the first tile of the group.
+struct ColItem { int world, chan, tile, kernel; };
 // A row item: rows row0.. of one world.  For Lenia worlds one item per target channel `chan`
 // (its kernels, its state update and its forward transform); other rules use chan = 0 and every
 // channel.
@@ -50,14 +52,13 @@ enum RowMode { MODE_STEP = 0, MODE_FORWARD = 1, MODE_U = 2 };
 
 // Fused FP32 path (step_fp32_*.cu).  Every size is built in two launch variants with the same
 // threads per CTA: variant 0 caps registers at 64 per thread (more resident CTAs), variant 1 at
-// 128.  The autotuner picks per size class.  For the column pass, variant bit 1 (2, 3) selects
-// the build that also handles channels read by several kernels; the row launcher picks its general
-// build from its `general` argument.  Launchers return false if the size is not built.
-bool launch_col_fp32(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+// 128.  The autotuner picks per size class.  The row launcher picks its general build from its
+// `general` argument.  Launchers return false if the size is not built.
+bool launch_col_fp32(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                      const float2* tw, cudaStream_t s);
 bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* worlds, const RowItem* items,
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s);
-size_t col_smem_bytes(int H, int nbuf);
+size_t col_smem_bytes(int H);
 size_t row_smem_bytes(int W, int acc_planes);
 int row_item_rows(int W);  // rows per row-pass item (two per packed sequence)
 int fp32_local_bytes(int row, int n, int variant);  // spill/stack bytes per thread of a pass instantiation

@@ -139,7 +139,7 @@ LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, 
     noalloc_prepare<<<(n + 255) / 256, 256, 0, s>>>(dw, w, col, ncol, row, nrow, rows);
     bool ok = launch_row_fp32((int)width, 0, MODE_FORWARD, 0, dw, row, nrow, 0, tw, s);
     for (uint32_t i = 0; ok && i < steps; i++) {
-        ok = launch_col_fp32((int)height, 0, 1, dw, col, ncol, tw, s) &&
+        ok = launch_col_fp32((int)height, 0, dw, col, ncol, tw, s) &&
              launch_row_fp32((int)width, 0, MODE_STEP, 0, dw, row, nrow, 0, tw, s);
     }
     if (!ok) return set_error(LENIA_ECUDA, "launch configuration failed");

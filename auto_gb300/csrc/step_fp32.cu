@@ -12,8 +12,8 @@ static size_t col_khat_bytes_of(int H) {
     return 0;
 }
 
-size_t col_smem_bytes(int H, int nbuf) {
-    return (size_t)nbuf * TC * lfft::seq_stride(H) * sizeof(float2) + (lfft::tw_table_size(H) + 1) * sizeof(float2) +
+size_t col_smem_bytes(int H) {
+    return (size_t)TC * lfft::seq_stride(H) * sizeof(float2) + (lfft::tw_table_size(H) + 1) * sizeof(float2) +
            col_khat_bytes_of(H);
 }
 size_t row_smem_bytes(int W, int acc_planes) {
@@ -34,10 +34,10 @@ int max_smem_optin() {
     return v;
 }
 
-bool launch_col_fp32(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+bool launch_col_fp32(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                      const float2* tw, cudaStream_t s) {
-    return launch_col_group_small(H, variant, nbuf, worlds, items, nitems, tw, s) ||
-           launch_col_group_large(H, variant, nbuf, worlds, items, nitems, tw, s);
+    return launch_col_group_small(H, variant, worlds, items, nitems, tw, s) ||
+           launch_col_group_large(H, variant, worlds, items, nitems, tw, s);
 }
 
 bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* worlds, const RowItem* items,

@@ -498,82 +498,63 @@ __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__
     }
 }
 
-// MULTI: the instantiation for size classes with a channel that several kernels read.  Without
-// it, every channel has exactly one kernel (the host guarantees this), and the kernel carries no
-// code for sharing one forward transform between kernels -- that code's register pressure would
-// otherwise set the register budget, and the spills, of the common single-kernel path.
-template <int H, int NT, int MINB, bool MULTI>
+// Unchained column item: tile 0 (its column 0 packs the DC and Nyquist columns, paired ky with
+// H - ky in the khat multiply) or a khat array that is not 16-byte aligned.  Not inlined: one item
+// in W/4 takes this path, and as a separate function its registers do not add to the chained path's.
+template <int H, int NT>
+__device__ __noinline__ void col_item_unchained(float2* X, const float2* stw, const float2* src, float2* dst,
+                                                const float* kh, int HQ, int W, int t) {
+    load_tile<H, NT>(X, src);
+    __syncthreads();
+    fft_seqs<H, TC, NT, false>(X, stw);
+    multiply_khat<H, NT>(X, X, kh, HQ, W, t);
+    __syncthreads();
+    fft_seqs<H, TC, NT, true>(X, stw);
+    store_tile<H, NT>(X, dst);
+}
+
+// One column item: tile `tile` (TC spectrum columns) of channel `chan`, convolved with kernel
+// `kernel` (which reads that channel).  A channel read by several kernels has one item per kernel, each
+// repeating the channel's forward column transform: that keeps every item on the chained path and
+// multiplies the items, which the multichannel world needs more than it needs the saved transforms.
+template <int H, int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
-                                                int nbuf, const float2* __restrict__ tw) {
+                                                const float2* __restrict__ tw) {
     extern __shared__ float4 smem_raw[];
     constexpr int SEQ = seq_stride(H);
     float2* X = reinterpret_cast<float2*>(smem_raw);
-    float2* Y = X + TC * SEQ;
-    float2* stw = X + nbuf * TC * SEQ;
+    float2* stw = X + TC * SEQ;
     fill_stage_twiddles<H>(stw, tw, threadIdx.x, NT);
     const ColItem it = items[blockIdx.x];
     const DevWorld& wd = worlds[it.world];
-    const int W = wd.W, c = it.chan, t = it.tile, K = wd.K, HQ = wd.HQ;
+    const int W = wd.W, c = it.chan, t = it.tile, k = it.kernel, HQ = wd.HQ;
     const size_t cplane = (size_t)(W / 2) * H;
     const float2* src = wd.spec + c * cplane + (size_t)t * H * TC;
-    int nsrc = 0, k1 = 0;
-    for (int k = K - 1; k >= 0; k--)
-        if (wd.kern[k].src == c) nsrc++, k1 = k;
-    if (nsrc == 0) return;
-    if (!MULTI || nsrc == 1) {
-        // One kernel on this channel.  Tiles without the packed DC/Nyquist column: the khat
-        // multiply runs in registers between the forward and the inverse column FFT, and the
-        // tile's two khat columns (contiguous, HQ floats each) are copied to shared memory while
-        // the tile loads.
-        constexpr int HQC = khat_cols_stride<H>();
-        const float* kh = wd.khat + ((size_t)k1 * (W / 2 + 1) + (size_t)TC * t) * HQC;
-        if (fusable<H>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
-            float* ksm = col_khat_smem<H>(stw);
-            for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
-            load_tile<H, NT>(X, src);
-            cp_async_wait_all();
-            __syncthreads();
-            fft_fused<H, TC, NT, false, true>(X, stw, [&](int s, int j, float2* v) {
-                constexpr int R = plan_radix(H, 0), NB = H / R;
-                const float* kc = ksm + s * HQC;
-#pragma unroll
-                for (int m = 0; m < R; m++) {
-                    const int ky = j + m * NB;
-                    v[m] = cscale(v[m], kc[ky <= H / 2 ? ky : H - ky]);
-                }
-            });
-            store_tile<H, NT>(X, wd.conv + k1 * cplane + (size_t)t * H * TC);
-            return;
-        }
-        // tile 0 (DC and Nyquist columns paired, ky with H - ky) or khat not 16-byte aligned
+    // Tiles without the packed DC/Nyquist column: the khat multiply runs in registers between the
+    // forward and the inverse column FFT, and the tile's two khat columns (contiguous, HQ floats
+    // each) are copied to shared memory while the tile loads.
+    constexpr int HQC = khat_cols_stride<H>();
+    const float* kh = wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)TC * t) * HQC;
+    if (fusable<H>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
+        float* ksm = col_khat_smem<H>(stw);
+        for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
         load_tile<H, NT>(X, src);
+        cp_async_wait_all();
         __syncthreads();
-        fft_seqs<H, TC, NT, false>(X, stw);
-        multiply_khat<H, NT>(X, X, wd.khat + (size_t)k1 * (W / 2 + 1) * HQ, HQ, W, t);
-        __syncthreads();
-        fft_seqs<H, TC, NT, true>(X, stw);
-        store_tile<H, NT>(X, wd.conv + k1 * cplane + (size_t)t * H * TC);
+        fft_fused<H, TC, NT, false, true>(X, stw, [&](int s, int j, float2* v) {
+            constexpr int R = plan_radix(H, 0), NB = H / R;
+            const float* kc = ksm + s * HQC;
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                const int ky = j + m * NB;
+                v[m] = cscale(v[m], kc[ky <= H / 2 ? ky : H - ky]);
+            }
+        });
+        store_tile<H, NT>(X, wd.conv + k * cplane + (size_t)t * H * TC);
         return;
     }
-    if constexpr (!MULTI) return;
-    const bool reload = (nsrc > 1 && nbuf < 2);
-    bool have = false;
-    for (int k = 0; k < K; k++) {
-        if (wd.kern[k].src != c) continue;
-        if (!have || reload) {
-            load_tile<H, NT>(X, src);
-            __syncthreads();
-            fft_seqs<H, TC, NT, false>(X, stw);
-            have = true;
-        }
-        float2* T = (nsrc > 1 && !reload) ? Y : X;
-        const float* kh = wd.khat + (size_t)k * (W / 2 + 1) * HQ;
-        multiply_khat<H, NT>(X, T, kh, HQ, W, t);
-        __syncthreads();
-        fft_seqs<H, TC, NT, true>(T, stw);
-        store_tile<H, NT>(T, wd.conv + k * cplane + (size_t)t * H * TC);
-        __syncthreads();
-    }
+    col_item_unchained<H, NT>(X, stw, src, wd.conv + k * cplane + (size_t)t * H * TC,
+                              wd.khat + (size_t)k * (W / 2 + 1) * HQ, HQ, W, t);
 }
 
 // Sizes built: each TU instantiates one group.  Threads per CTA: one first-stage butterfly per
@@ -589,17 +570,17 @@ template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) /
 
 // Launch one instantiation.  Dynamic shared memory above 48 KB must be enabled per kernel before
 // its first launch and before any stream capture that contains it; a zero-item call does just that.
-template <int H, int NT, int MINB, bool MULTI>
-bool col_go(int nbuf, const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
-    const size_t smem = (size_t)nbuf * TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>() + col_khat_bytes<H>();
+template <int H, int NT, int MINB>
+bool col_go(const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
+    const size_t smem = (size_t)TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>() + col_khat_bytes<H>();
     static int attr_max = 0;
     if ((int)smem > attr_max) {
-        if (cudaFuncSetAttribute(col_pass<H, NT, MINB, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(col_pass<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return false;
         attr_max = (int)smem;
     }
-    if (nitems > 0) col_pass<H, NT, MINB, MULTI><<<nitems, NT, smem, s>>>(worlds, items, nbuf, tw);
+    if (nitems > 0) col_pass<H, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, tw);
     return true;
 }
 
@@ -627,15 +608,11 @@ bool row_go(int mode, int general, int planes, const DevWorld* worlds, const Row
     return true;
 }
 
-// Column-pass variant: bit 0 selects the register cap (minb_of), bit 1 the MULTI instantiation.
-#define LENIA_COL_CASE(N)                                                                               \
-    case N:                                                                                             \
-        switch (variant & 3) {                                                                          \
-        case 0: return col_go<N, nt_of<N>(), minb_of<N, 0>(), false>(nbuf, worlds, items, nitems, tw, s); \
-        case 1: return col_go<N, nt_of<N>(), minb_of<N, 1>(), false>(nbuf, worlds, items, nitems, tw, s); \
-        case 2: return col_go<N, nt_of<N>(), minb_of<N, 0>(), true>(nbuf, worlds, items, nitems, tw, s);  \
-        default: return col_go<N, nt_of<N>(), minb_of<N, 1>(), true>(nbuf, worlds, items, nitems, tw, s); \
-        }
+#define LENIA_COL_CASE(N)                                                                      \
+    case N:                                                                                    \
+        return variant == 0 ? col_go<N, nt_of<N>(), minb_of<N, 0>()>(worlds, items, nitems, tw, s) \
+                            : col_go<N, nt_of<N>(), minb_of<N, 1>()>(worlds, items, nitems, tw, s);
+
 // Row-pass variant: bit 0 selects the register cap (row_minb); the GEN build runs when `general`.
 #define LENIA_ROW_CASE(N)                                                                                        \
     case N:                                                                                                      \
@@ -652,14 +629,10 @@ int local_bytes_of(F* f) {
     cudaFuncAttributes a;
     return cudaFuncGetAttributes(&a, f) == cudaSuccess ? (int)a.localSizeBytes : -1;
 }
-#define LENIA_COL_LOCAL_CASE(N)                                                            \
-    case N:                                                                                \
-        switch (variant & 3) {                                                             \
-        case 0: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>(), false>);    \
-        case 1: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>(), false>);    \
-        case 2: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>(), true>);     \
-        default: return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>(), true>);    \
-        }
+#define LENIA_COL_LOCAL_CASE(N)                                                    \
+    case N:                                                                        \
+        return variant == 0 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>) \
+                            : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
 #define LENIA_ROW_LOCAL_CASE(N)                                                             \
     case N:                                                                                 \
         switch (variant & 3) {                                                              \
@@ -673,9 +646,9 @@ int col_local_bytes_large(int H, int variant);
 int row_local_bytes_small(int W, int variant);
 int row_local_bytes_large(int W, int variant);
 
-bool launch_col_group_small(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+bool launch_col_group_small(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                             const float2* tw, cudaStream_t s);
-bool launch_col_group_large(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+bool launch_col_group_large(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                             const float2* tw, cudaStream_t s);
 bool launch_row_group_small(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
                             const RowItem* items, int nitems, const float2* tw, cudaStream_t s);

@@ -3,7 +3,7 @@
 
 namespace lenia {
 
-bool launch_col_group_large(int H, int variant, int nbuf, const DevWorld* worlds, const ColItem* items, int nitems,
+bool launch_col_group_large(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                             const float2* tw, cudaStream_t s) {
     switch (H) { LENIA_SIZES_LARGE(LENIA_COL_CASE) }
     return false;
