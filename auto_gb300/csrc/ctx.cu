@@ -1086,12 +1086,20 @@ int lenia_autotune(LeniaCtx* ctx) {
         if (frc) return frc;
     }
     // Try both built thread counts for each class's column and row launches; keep the fastest.
-    // The trial steps advance the worlds, so save and restore every state.
-    std::vector<std::vector<float>> saved(ctx->desc.size());
-    for (size_t w = 0; w < ctx->desc.size(); w++) {
-        saved[w].resize(state_count(ctx->desc[w]));
-        int rc = lenia_read_state(ctx, (int)w, saved[w].data(), saved[w].size());
-        if (rc) return rc;
+    // The trial steps advance the worlds, so every state is saved to a device buffer and restored.
+    size_t total = 0;
+    for (const auto& d : ctx->desc) total += state_count(d);
+    float* saved = nullptr;
+    CK(cudaMalloc(&saved, total * sizeof(float)));
+    {
+        size_t off = 0;
+        for (size_t w = 0; w < ctx->desc.size(); w++) {
+            const size_t n = state_count(ctx->desc[w]);
+            if (!ctx->states || w == 0)
+                CK(cudaMemcpyAsync(saved + off, state_ptr(ctx, (int)w), (ctx->states ? total : n) * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+            off += n;
+        }
     }
     cudaEvent_t a, b;
     CK(cudaEventCreate(&a));
@@ -1132,10 +1140,19 @@ int lenia_autotune(LeniaCtx* ctx) {
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
-    for (size_t w = 0; w < ctx->desc.size(); w++) {
-        int rc = lenia_write_state(ctx, (int)w, saved[w].data(), saved[w].size());
-        if (rc) return rc;
+    {
+        size_t off = 0;
+        for (size_t w = 0; w < ctx->desc.size(); w++) {
+            const size_t n = state_count(ctx->desc[w]);
+            if (!ctx->states || w == 0)
+                CK(cudaMemcpyAsync(state_ptr(ctx, (int)w), saved + off, (ctx->states ? total : n) * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, ctx->stream));
+            refresh_spectrum(ctx, (int)w);
+            off += n;
+        }
     }
+    CK(cudaStreamSynchronize(ctx->stream));
+    cudaFree(saved);
     int rc = rebuild_graphs(ctx);
     if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->stream));

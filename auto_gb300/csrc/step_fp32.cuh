@@ -275,6 +275,58 @@ __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __r
     }
 }
 
+// Row-pass modes that run outside the step (after state writes, and for U-field reads).  Not
+// inlined, so that their registers do not add to the step path's.
+template <int W, int NT>
+__device__ __noinline__ void row_item_forward(float2* Z, const float2* stw, const DevWorld& wd, int r0, int d0, int d1) {
+    constexpr int S = row_seqs(W), SEQ = seq_stride(W);
+    const int H = wd.H;
+    const size_t plane = (size_t)W * H, cplane = (size_t)(W / 2) * H;
+    for (int d = d0; d < d1; d++) {
+        const float* st = wd.state + d * plane + (size_t)r0 * W;
+        constexpr int IT = (S * W + NT - 1) / NT;
+        float a[IT], b[IT];
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
+            if (IT * NT == S * W || e < S * W) {
+                a[i] = st[(2 * p) * W + x];
+                b[i] = st[(2 * p + 1) * W + x];
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < IT; i++) {
+            const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
+            if (IT * NT == S * W || e < S * W) Z[p * SEQ + pad(x)] = make_float2(a[i], b[i]);
+        }
+        __syncthreads();
+        fft_seqs<W, S, NT, false>(Z, stw);
+        store_rows_spectrum<W, S, NT>(Z, wd.spec + d * cplane, H, r0);
+        __syncthreads();
+    }
+}
+
+template <int W, int NT>
+__device__ __noinline__ void row_item_u(float2* Z, const float2* stw, const DevWorld& wd, int r0, int d0, bool per_chan) {
+    constexpr int S = row_seqs(W), SEQ = seq_stride(W);
+    const int H = wd.H, K = wd.K;
+    const size_t plane = (size_t)W * H, cplane = (size_t)(W / 2) * H;
+    for (int k = 0; k < K; k++) {
+        if (per_chan && wd.kern[k].dst != d0) continue;
+        load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
+        __syncthreads();
+        fft_seqs<W, S, NT, true>(Z, stw);
+        float* u = wd.u_out + k * plane + (size_t)r0 * W;
+        for (int e = threadIdx.x; e < S * W; e += NT) {
+            const int p = e / W, x = e - p * W;
+            const float2 z = Z[p * SEQ + pad(x)];
+            u[(2 * p) * W + x] = z.x;
+            u[(2 * p + 1) * W + x] = z.y;
+        }
+        __syncthreads();
+    }
+}
+
 // GEN: the instantiation for size classes with worlds that need the general step (several
 // channels or kernels, SmoothLife, MNCA).  Without it the kernel carries only the one-channel,
 // one-kernel Lenia step (and the forward and U modes), so the general path's register pressure
@@ -298,46 +350,11 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     const int d0 = per_chan ? it.chan : 0, d1 = per_chan ? it.chan + 1 : C;
 
     if (mode == MODE_FORWARD) {
-        for (int d = d0; d < d1; d++) {
-            const float* st = wd.state + d * plane + (size_t)r0 * W;
-            constexpr int IT = (S * W + NT - 1) / NT;
-            float a[IT], b[IT];
-#pragma unroll
-            for (int i = 0; i < IT; i++) {
-                const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
-                if (IT * NT == S * W || e < S * W) {
-                    a[i] = st[(2 * p) * W + x];
-                    b[i] = st[(2 * p + 1) * W + x];
-                }
-            }
-#pragma unroll
-            for (int i = 0; i < IT; i++) {
-                const int e = threadIdx.x + i * NT, p = e / W, x = e - p * W;
-                if (IT * NT == S * W || e < S * W) Z[p * SEQ + pad(x)] = make_float2(a[i], b[i]);
-            }
-            __syncthreads();
-            fft_seqs<W, S, NT, false>(Z, stw);
-            store_rows_spectrum<W, S, NT>(Z, wd.spec + d * cplane, H, r0);
-            __syncthreads();
-        }
+        row_item_forward<W, NT>(Z, stw, wd, r0, d0, d1);
         return;
     }
-
     if (mode == MODE_U) {
-        for (int k = 0; k < K; k++) {
-            if (per_chan && wd.kern[k].dst != d0) continue;
-            load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
-            __syncthreads();
-            fft_seqs<W, S, NT, true>(Z, stw);
-            float* u = wd.u_out + k * plane + (size_t)r0 * W;
-            for (int e = threadIdx.x; e < S * W; e += NT) {
-                const int p = e / W, x = e - p * W;
-                const float2 z = Z[p * SEQ + pad(x)];
-                u[(2 * p) * W + x] = z.x;
-                u[(2 * p + 1) * W + x] = z.y;
-            }
-            __syncthreads();
-        }
+        row_item_u<W, NT>(Z, stw, wd, r0, d0, per_chan);
         return;
     }
 

@@ -61,7 +61,8 @@ def parse(argv=None):
     p.add_argument("--gens", type=int, default=64, help="generations per bench step")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--autotune", action="store_true")
+    p.add_argument("--no-autotune", action="store_true",
+                   help="keep the default launch variants instead of timing both per size class")
     p.add_argument("--jsonl", default=None, help="also append a sample in the reference's results/*.jsonl format")
     p.add_argument("--no-paths", action="store_true", help="skip timing the other step paths side by side")
     return p.parse_args(argv)
@@ -301,8 +302,8 @@ def run_ours(args, dist):
         scaling = "strong"
     sim = Sim(worlds, seed=0, path=args.path)
     seed_all(sim, worlds, seeds)
-    if args.autotune:
-        sim.autotune()
+    if not args.no_autotune:
+        sim.autotune()  # the engine's autotuner: times both launch variants per size class
     G = args.gens
     cells = sim.cells_per_step
     for _ in range(args.warmup):
@@ -394,6 +395,8 @@ def run_ours(args, dist):
                 continue
             with Sim(worlds, seed=0, path=pth) as other:
                 seed_all(other, worlds, seeds)
+                if not args.no_autotune:
+                    other.autotune()
                 g = G if pth != "radix2" else 4
                 other.step(g)
                 other.wait()
@@ -415,6 +418,8 @@ def run_ours(args, dist):
             for i in pick:
                 with Sim(worlds[i], seed=0, path=args.path) as one:
                     seed_all(one, [worlds[i]], [seeds[i]])
+                    if not args.no_autotune:
+                        one.autotune()
                     one.step(G)
                     one.wait()
                     one_ms += one.step_timed(2 * G)
