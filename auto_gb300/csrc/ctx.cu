@@ -1106,8 +1106,7 @@ int lenia_autotune(LeniaCtx* ctx) {
     CK(cudaEventCreate(&b));
     const int reps = 5;
     for (auto& cl : ctx->classes) {
-        float best_col = 1e30f, best_row = 1e30f;
-        int pick_col = cl.var_col, pick_row = cl.var_row;
+        float tcol[2] = {1e30f, 1e30f}, trow[2] = {1e30f, 1e30f};
         for (int which = 0; which < 2; which++) {
             const int ntc = which, ntr = which;
             float t_col = 0, t_row = 0;
@@ -1132,11 +1131,13 @@ int lenia_autotune(LeniaCtx* ctx) {
                     break;
                 }
             }
-            if (t_col < best_col) { best_col = t_col; pick_col = ntc; }
-            if (t_row < best_row) { best_row = t_row; pick_row = ntr; }
+            tcol[which] = t_col;
+            trow[which] = t_row;
         }
-        cl.var_col = pick_col;
-        cl.var_row = pick_row;
+        // the default variant stays unless the other is at least 3% faster, so that timing noise does
+        // not flip the choice
+        if (tcol[1 - cl.var_col] < 0.97f * tcol[cl.var_col]) cl.var_col = 1 - cl.var_col;
+        if (trow[1 - cl.var_row] < 0.97f * trow[cl.var_row]) cl.var_row = 1 - cl.var_row;
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
