@@ -5,9 +5,9 @@
 // convolved, then update.  Here the same mathematics is regrouped so that each grid sweep
 // does as much as it can in shared memory:
 //
-//   column pass (per world, channel, tile of 4 spectrum columns):
+//   column pass (per world, channel, tile of TC = 2 spectrum columns, kernel k reading it):
 //       forward FFT along y  ->  x khat_k (real, even; includes 1/(W*H))  ->  inverse FFT along y
-//   row pass (per world, block of 4 rows):
+//   row pass (per world, block of 4 rows; Lenia: and target channel):
 //       inverse real FFT along x of U_k  ->  growth, dt, clamp (spectral.rs:337-345)  ->
 //       write state  ->  forward real FFT along x of the new rows  ->  write spectrum
 //
