@@ -70,6 +70,22 @@ def parse(argv=None):
 
 # ----------------------------------------------------------------------------- distributed plumbing
 
+def pin_gpu():
+    """Under torchrun, show each rank only its own GPU (CUDA_VISIBLE_DEVICES), before any CUDA use.
+
+    The engine library carries its own CUDA runtime, so a torch.cuda.set_device call would not
+    choose its device; with one visible GPU per process, every runtime in the process uses the
+    rank's GPU as device 0.  Returns the GPU's index among all GPUs (for nvidia-smi)."""
+    if int(os.environ.get("WORLD_SIZE", "1")) <= 1 or "LOCAL_RANK" not in os.environ:
+        return 0
+    local = int(os.environ["LOCAL_RANK"])
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+    ids = [x.strip() for x in vis.split(",") if x.strip()] if vis else []
+    phys = ids[local] if local < len(ids) else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = phys
+    return int(phys) if phys.isdigit() else local
+
+
 class Dist:
     """torchrun plumbing: barrier and max over ranks (NCCL on GPUs, gloo without)."""
 
@@ -84,7 +100,8 @@ class Dist:
             import torch.distributed as dist
             self.torch = torch
             if torch.cuda.is_available():
-                torch.cuda.set_device(self.local)
+                # one visible GPU per rank after pin_gpu(); the rank's own index otherwise
+                torch.cuda.set_device(0 if torch.cuda.device_count() == 1 else self.local)
                 self.device = "cuda"
             dist.init_process_group("nccl" if self.device == "cuda" else "gloo")
 
@@ -312,7 +329,7 @@ def run_ours(args, dist):
     device_sync()
     dist.barrier()
     device_sync()
-    clocks = Clocks(dist.local)
+    clocks = Clocks(getattr(dist, "gpu_index", dist.local))
     clocks.start()
     ms = sim.step_timed(args.steps * G)
     device_sync()
@@ -491,7 +508,9 @@ def append_reference_sample(path, sim, worlds, cfg, impl_path, seconds=2.0, warm
 
 def main():
     args = parse()
+    gpu = pin_gpu()
     dist = Dist()
+    dist.gpu_index = gpu
     try:
         if args.impl == "reference":
             run_reference(args, dist)
