@@ -136,7 +136,7 @@ int dalloc(LeniaCtx* ctx, T** p, size_t count) {
 bool supported_side(uint32_t n) {
     uint32_t m = (n % 3 == 0) ? n / 3 : n;
     if (m == 0 || (m & (m - 1)) != 0) return false;
-    return n >= 32 && n <= 4096;
+    return n >= 32 && n <= 8192;
 }
 bool is_pow2(uint32_t n) { return n && !(n & (n - 1)); }
 
@@ -237,7 +237,7 @@ float kernel_sum_f32(const LeniaKernel& k) {
 
 int validate(const LeniaWorldDesc& d, int i, int path) {
     if (!supported_side(d.width) || !supported_side(d.height))
-        return fail(nullptr, LENIA_ESIZE, "world %d: %ux%u is not supported (sides 2^a or 3*2^a, 32..4096)", i, d.width,
+        return fail(nullptr, LENIA_ESIZE, "world %d: %ux%u is not supported (sides 2^a or 3*2^a, 32..8192)", i, d.width,
                     d.height);
     if (path == LENIA_PATH_RADIX2 && (!is_pow2(d.width) || !is_pow2(d.height)))
         return fail(nullptr, LENIA_ESIZE, "world %d: FFT grids must be powers of two on the radix-2 path", i);

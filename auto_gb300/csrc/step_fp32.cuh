@@ -196,7 +196,7 @@ FFT_CHD constexpr int row_seqs(int) { return 2; }
 template <int W>
 constexpr int row_nt() {
     constexpr int n = row_seqs(W) * W / plan_radix(W, 0);
-    return n < 64 ? 64 : (n > 512 ? 512 : n);
+    return n < 64 ? 64 : (n > 1024 ? 1024 : n);
 }
 // variant 0: at most 1024 threads' worth of registers per SM (64 a thread at 512 threads);
 // variant 1: at most 128 a thread
@@ -575,12 +575,12 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
 }
 
 // Sizes built: each TU instantiates one group.  Threads per CTA: one first-stage butterfly per
-// thread for the two sequences a CTA holds (2N / first radix), between 64 and 512.
+// thread for the two sequences a CTA holds (2N / first radix), between 64 and 1024.
 #define LENIA_SIZES_SMALL(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768)
-#define LENIA_SIZES_LARGE(X) X(1024) X(1536) X(2048) X(3072) X(4096)
+#define LENIA_SIZES_LARGE(X) X(1024) X(1536) X(2048) X(3072) X(4096) X(6144) X(8192)
 template <int N> constexpr int nt_of() {
     constexpr int n = 2 * N / plan_radix(N, 0);  // one first-stage butterfly per thread, two sequences
-    return n < 64 ? 64 : (n > 512 ? 512 : n);
+    return n < 64 ? 64 : (n > 1024 ? 1024 : n);
 }
 // variant 0: at most 64 registers per thread; variant 1: at most 128
 template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) / nt_of<N>() < 1 ? 1 : (V == 0 ? 1024 : 512) / nt_of<N>(); }

@@ -76,7 +76,7 @@ typedef struct LeniaKernel {
 } LeniaKernel;
 
 typedef struct LeniaWorldDesc {
-    uint32_t width, height;   /* 2^a * 3^b (b <= 1), 32..4096 */
+    uint32_t width, height;   /* 2^a * 3^b (b <= 1), 32..8192 */
     uint32_t channels;        /* 1..LENIA_MAX_CHANNELS */
     uint32_t nkernels;        /* 1..LENIA_MAX_KERNELS */
     int32_t rule;             /* LENIA_RULE_* */

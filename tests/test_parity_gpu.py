@@ -56,7 +56,7 @@ def test_orbium_tiles_seeded_on_device(golden, path):
         assert np.array_equal(sim.read_state(0)[0], g["state0"])
 
 
-@pytest.mark.parametrize("w,h", [(256, 128), (192, 192), (768, 384), (4096, 64), (96, 3072)])
+@pytest.mark.parametrize("w,h", [(256, 128), (192, 192), (768, 384), (4096, 64), (96, 3072), (8192, 32), (6144, 64)])
 def test_row_spectrum_matches_numpy(w, h):
     """The engine keeps, between steps, the half-spectrum along x of every row (the column
     transform happens inside the column pass)."""
@@ -197,6 +197,19 @@ def test_all_world_state_calls_match_per_world_calls():
             a.read_states(np.empty(flat.size + 1, np.float32))
 
 
+@pytest.mark.parametrize("w,h", [(8192, 64), (64, 8192), (6144, 96), (96, 6144)])
+def test_largest_sides_teacher_forced_vs_fp64(w, h):
+    # the largest sides (up to 8192, 1024-thread CTAs) along either axis, one step from a random state
+    world = ag.World(w, h, [ag.Kernel(radius=13.0, beta=[1.0, 0.5])], dt=0.1)
+    rng = np.random.default_rng(w * 7 + h)
+    s = rng.random((1, h, w), dtype=np.float32)
+    with Sim(world) as sim:
+        sim.write_state(0, s)
+        sim.step(1)
+        got = sim.read_state(0)
+    assert np.abs(got - fp64_step(world, s)).max() < 1e-4
+
+
 def test_batched_worlds_teacher_forced_vs_fp64():
     worlds = configs.batched(32)
     with Sim(worlds, seed=0) as sim:
@@ -269,6 +282,9 @@ def test_stats():
 def test_errors_are_reported_not_raised_as_crashes():
     with pytest.raises(LeniaError) as e:
         Sim(ag.World(100, 100, [ag.Kernel()]))
+    assert e.value.code == _lib.ESIZE
+    with pytest.raises(LeniaError) as e:  # sides above 8192 are not built
+        Sim(ag.World(16384, 64, [ag.Kernel()]))
     assert e.value.code == _lib.ESIZE
     with pytest.raises(LeniaError) as e:
         Sim(ag.World(64, 64, [ag.Kernel(radius=40.0)]))
