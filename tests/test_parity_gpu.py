@@ -286,6 +286,9 @@ def test_errors_are_reported_not_raised_as_crashes():
     with pytest.raises(LeniaError) as e:  # sides above 8192 are not built
         Sim(ag.World(16384, 64, [ag.Kernel()]))
     assert e.value.code == _lib.ESIZE
+    with pytest.raises(LeniaError) as e:  # general step 8192 wide: more shared memory than a CTA has
+        Sim(ag.World(8192, 64, [ag.Kernel(), ag.Kernel(radius=9.0)]))
+    assert e.value.code == _lib.ESIZE
     with pytest.raises(LeniaError) as e:
         Sim(ag.World(64, 64, [ag.Kernel(radius=40.0)]))
     assert "smaller than its kernel" in str(e.value)
