@@ -106,6 +106,21 @@ int fail(LeniaCtx* c, int code, const char* fmt, ...) {
         if (e_ != cudaSuccess) return fail(ctx, LENIA_ECUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
     } while (0)
 
+// Owners that release on every return path (the CK macro returns early on a CUDA error).
+struct Events {
+    cudaEvent_t e[3] = {nullptr, nullptr, nullptr};
+    ~Events() {
+        for (cudaEvent_t x : e)
+            if (x) cudaEventDestroy(x);
+    }
+};
+struct DeviceBuffer {
+    void* p = nullptr;
+    ~DeviceBuffer() {
+        if (p) cudaFree(p);
+    }
+};
+
 template <typename T>
 int dalloc(LeniaCtx* ctx, T** p, size_t count) {
     const size_t bytes = (count * sizeof(T) + 255) / 256 * 256;
@@ -809,16 +824,14 @@ int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms) {
     if (!ctx || !ms) return LENIA_EINVAL;
     int frc = flush_spectra(ctx);  // outside the timed region
     if (frc) return frc;
-    cudaEvent_t a, b;
-    CK(cudaEventCreate(&a));
-    CK(cudaEventCreate(&b));
-    CK(cudaEventRecord(a, ctx->stream));
+    Events ev;
+    CK(cudaEventCreate(&ev.e[0]));
+    CK(cudaEventCreate(&ev.e[1]));
+    CK(cudaEventRecord(ev.e[0], ctx->stream));
     int rc = lenia_step(ctx, steps);
-    CK(cudaEventRecord(b, ctx->stream));
-    CK(cudaEventSynchronize(b));
-    CK(cudaEventElapsedTime(ms, a, b));
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
+    CK(cudaEventRecord(ev.e[1], ctx->stream));
+    CK(cudaEventSynchronize(ev.e[1]));
+    CK(cudaEventElapsedTime(ms, ev.e[0], ev.e[1]));
     if (!rc) rc = tc_check_error(ctx->tc, &ctx->err);
     return rc;
 }
@@ -1004,25 +1017,24 @@ int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
         if (frc) return frc;
     }
     if (ctx->path == LENIA_PATH_RADIX2) {
-        cudaEvent_t a, b;
-        CK(cudaEventCreate(&a));
-        CK(cudaEventCreate(&b));
-        CK(cudaEventRecord(a, ctx->stream));
+        Events ev;
+        CK(cudaEventCreate(&ev.e[0]));
+        CK(cudaEventCreate(&ev.e[1]));
+        CK(cudaEventRecord(ev.e[0], ctx->stream));
         for (uint32_t s = 0; s < steps; s++) CK(cudaGraphLaunch(ctx->graph_one, ctx->stream));
-        CK(cudaEventRecord(b, ctx->stream));
-        CK(cudaEventSynchronize(b));
+        CK(cudaEventRecord(ev.e[1], ctx->stream));
+        CK(cudaEventSynchronize(ev.e[1]));
         float ms = 0;
-        cudaEventElapsedTime(&ms, a, b);
-        cudaEventDestroy(a);
-        cudaEventDestroy(b);
+        cudaEventElapsedTime(&ms, ev.e[0], ev.e[1]);
         out3[0] = out3[1] = 0.0f;
         out3[2] = ms / steps;
         ctx->tick += steps;
         return 0;
     }
     // time every class's column and row launches on the context stream, serially
-    std::vector<cudaEvent_t> ev(3);
-    for (auto& e : ev) CK(cudaEventCreate(&e));
+    Events evs;
+    cudaEvent_t* ev = evs.e;
+    for (int i = 0; i < 3; i++) CK(cudaEventCreate(&ev[i]));
     double col_ms = 0, row_ms = 0;
     for (uint32_t s = 0; s < steps; s++) {
         for (auto& cl : ctx->classes) {
@@ -1041,7 +1053,6 @@ int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
             row_ms += b;
         }
     }
-    for (auto& e : ev) cudaEventDestroy(e);
     out3[0] = (float)(col_ms / steps);
     out3[1] = (float)(row_ms / steps);
     out3[2] = (float)((col_ms + row_ms) / steps);
@@ -1089,8 +1100,9 @@ int lenia_autotune(LeniaCtx* ctx) {
     // The trial steps advance the worlds, so every state is saved to a device buffer and restored.
     size_t total = 0;
     for (const auto& d : ctx->desc) total += state_count(d);
-    float* saved = nullptr;
-    CK(cudaMalloc(&saved, total * sizeof(float)));
+    DeviceBuffer save_buf;
+    CK(cudaMalloc(&save_buf.p, total * sizeof(float)));
+    float* saved = static_cast<float*>(save_buf.p);
     {
         size_t off = 0;
         for (size_t w = 0; w < ctx->desc.size(); w++) {
@@ -1101,9 +1113,10 @@ int lenia_autotune(LeniaCtx* ctx) {
             off += n;
         }
     }
-    cudaEvent_t a, b;
-    CK(cudaEventCreate(&a));
-    CK(cudaEventCreate(&b));
+    Events ev;
+    CK(cudaEventCreate(&ev.e[0]));
+    CK(cudaEventCreate(&ev.e[1]));
+    cudaEvent_t a = ev.e[0], b = ev.e[1];
     const int reps = 5;
     for (auto& cl : ctx->classes) {
         float tcol[2] = {1e30f, 1e30f}, trow[2] = {1e30f, 1e30f};
@@ -1139,8 +1152,6 @@ int lenia_autotune(LeniaCtx* ctx) {
         if (tcol[1 - cl.var_col] < 0.97f * tcol[cl.var_col]) cl.var_col = 1 - cl.var_col;
         if (trow[1 - cl.var_row] < 0.97f * trow[cl.var_row]) cl.var_row = 1 - cl.var_row;
     }
-    cudaEventDestroy(a);
-    cudaEventDestroy(b);
     {
         size_t off = 0;
         for (size_t w = 0; w < ctx->desc.size(); w++) {
@@ -1153,7 +1164,6 @@ int lenia_autotune(LeniaCtx* ctx) {
         }
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    cudaFree(saved);
     int rc = rebuild_graphs(ctx);
     if (rc) return rc;
     CK(cudaStreamSynchronize(ctx->stream));

@@ -463,6 +463,7 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
     void* d = nullptr;
     if (cudaMalloc(&d, host.size()) != cudaSuccess ||
         cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (d) cudaFree(d);
         if (err) *err = "DFT matrix upload failed";
         return LENIA_ECUDA;
     }
