@@ -42,13 +42,21 @@ bool launch_col_fp32(int H, int variant, const DevWorld* worlds, const ColItem* 
 
 bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* worlds, const RowItem* items,
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s) {
-    return launch_row_group_small(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s) ||
-           launch_row_group_large(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s);
+    if (general)
+        return launch_row_group_small_general(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s) ||
+               launch_row_group_large_general(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s);
+    return launch_row_group_small_simple(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s) ||
+           launch_row_group_large_simple(W, variant, mode, general, acc_planes, worlds, items, nitems, tw, s);
 }
 
 int fp32_local_bytes(int row, int n, int variant) {
-    const int a = row ? row_local_bytes_small(n, variant) : col_local_bytes_small(n, variant);
-    return a >= 0 ? a : (row ? row_local_bytes_large(n, variant) : col_local_bytes_large(n, variant));
+    if (!row) {
+        const int a = col_local_bytes_small(n, variant);
+        return a >= 0 ? a : col_local_bytes_large(n, variant);
+    }
+    // row: variant bit 1 asks for the general build
+    const int a = (variant & 2) ? row_local_bytes_small_general(n, variant) : row_local_bytes_small_simple(n, variant);
+    return a >= 0 ? a : ((variant & 2) ? row_local_bytes_large_general(n, variant) : row_local_bytes_large_simple(n, variant));
 }
 
 }  // namespace lenia

@@ -630,15 +630,16 @@ bool row_go(int mode, int general, int planes, const DevWorld* worlds, const Row
         return variant == 0 ? col_go<N, nt_of<N>(), minb_of<N, 0>()>(worlds, items, nitems, tw, s) \
                             : col_go<N, nt_of<N>(), minb_of<N, 1>()>(worlds, items, nitems, tw, s);
 
-// Row-pass variant: bit 0 selects the register cap (row_minb); the GEN build runs when `general`.
-#define LENIA_ROW_CASE(N)                                                                                        \
+// Row-pass builds: variant bit 0 selects the register cap (row_minb); the single-kernel (GEN =
+// false) and general (GEN = true) builds sit in separate translation units, which keeps each
+// unit's compile time down.
+#define LENIA_ROW_CASE_G(N, G)                                                                                   \
     case N:                                                                                                      \
-        switch ((variant & 1) | (general ? 2 : 0)) {                                                             \
-        case 0: return row_go<N, row_nt<N>(), row_minb<N, 0>(), false>(mode, general, planes, worlds, items, nitems, tw, s); \
-        case 1: return row_go<N, row_nt<N>(), row_minb<N, 1>(), false>(mode, general, planes, worlds, items, nitems, tw, s); \
-        case 2: return row_go<N, row_nt<N>(), row_minb<N, 0>(), true>(mode, general, planes, worlds, items, nitems, tw, s);  \
-        default: return row_go<N, row_nt<N>(), row_minb<N, 1>(), true>(mode, general, planes, worlds, items, nitems, tw, s); \
-        }
+        return (variant & 1)                                                                                     \
+                   ? row_go<N, row_nt<N>(), row_minb<N, 1>(), G>(mode, general, planes, worlds, items, nitems, tw, s) \
+                   : row_go<N, row_nt<N>(), row_minb<N, 0>(), G>(mode, general, planes, worlds, items, nitems, tw, s);
+#define LENIA_ROW_CASE_SIMPLE(N) LENIA_ROW_CASE_G(N, false)
+#define LENIA_ROW_CASE_GENERAL(N) LENIA_ROW_CASE_G(N, true)
 
 // Local memory (spills and stack) of one instantiation, bytes per thread; -1 if unknown.
 template <class F>
@@ -650,26 +651,30 @@ int local_bytes_of(F* f) {
     case N:                                                                        \
         return variant == 0 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>) \
                             : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
-#define LENIA_ROW_LOCAL_CASE(N)                                                             \
-    case N:                                                                                 \
-        switch (variant & 3) {                                                              \
-        case 0: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>(), false>);   \
-        case 1: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>(), false>);   \
-        case 2: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>(), true>);    \
-        default: return local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>(), true>);   \
-        }
+#define LENIA_ROW_LOCAL_CASE_G(N, G)                                                    \
+    case N:                                                                             \
+        return (variant & 1) ? local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>(), G>) \
+                             : local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>(), G>);
+#define LENIA_ROW_LOCAL_CASE_SIMPLE(N) LENIA_ROW_LOCAL_CASE_G(N, false)
+#define LENIA_ROW_LOCAL_CASE_GENERAL(N) LENIA_ROW_LOCAL_CASE_G(N, true)
 int col_local_bytes_small(int H, int variant);
 int col_local_bytes_large(int H, int variant);
-int row_local_bytes_small(int W, int variant);
-int row_local_bytes_large(int W, int variant);
+// row builds: one function per (size group, single-kernel or general) translation unit
+int row_local_bytes_small_simple(int W, int variant);
+int row_local_bytes_small_general(int W, int variant);
+int row_local_bytes_large_simple(int W, int variant);
+int row_local_bytes_large_general(int W, int variant);
 
 bool launch_col_group_small(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                             const float2* tw, cudaStream_t s);
 bool launch_col_group_large(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                             const float2* tw, cudaStream_t s);
-bool launch_row_group_small(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
-                            const RowItem* items, int nitems, const float2* tw, cudaStream_t s);
-bool launch_row_group_large(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
-                            const RowItem* items, int nitems, const float2* tw, cudaStream_t s);
+#define LENIA_ROW_GROUP_DECL(NAME)                                                                       \
+    bool NAME(int W, int variant, int mode, int general, int planes, const DevWorld* worlds, const RowItem* items, \
+              int nitems, const float2* tw, cudaStream_t s);
+LENIA_ROW_GROUP_DECL(launch_row_group_small_simple)
+LENIA_ROW_GROUP_DECL(launch_row_group_small_general)
+LENIA_ROW_GROUP_DECL(launch_row_group_large_simple)
+LENIA_ROW_GROUP_DECL(launch_row_group_large_general)
 
 }  // namespace lenia

@@ -1,16 +1,17 @@
-// Row-pass instantiations of the fused FP32 step, small sizes (templates in step_fp32.cuh).
+// Row-pass instantiations of the fused FP32 step, small sizes, one-channel, one-kernel Lenia step (templates in
+// step_fp32.cuh).
 #include "step_fp32.cuh"
 
 namespace lenia {
 
-bool launch_row_group_small(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
-                            const RowItem* items, int nitems, const float2* tw, cudaStream_t s) {
-    switch (W) { LENIA_SIZES_SMALL(LENIA_ROW_CASE) }
+bool launch_row_group_small_simple(int W, int variant, int mode, int general, int planes, const DevWorld* worlds,
+                                const RowItem* items, int nitems, const float2* tw, cudaStream_t s) {
+    switch (W) { LENIA_SIZES_SMALL(LENIA_ROW_CASE_SIMPLE) }
     return false;
 }
 
-int row_local_bytes_small(int W, int variant) {
-    switch (W) { LENIA_SIZES_SMALL(LENIA_ROW_LOCAL_CASE) }
+int row_local_bytes_small_simple(int W, int variant) {
+    switch (W) { LENIA_SIZES_SMALL(LENIA_ROW_LOCAL_CASE_SIMPLE) }
     return -1;
 }
 
