@@ -65,6 +65,8 @@ def parse(argv=None):
                    help="keep the default launch variants instead of timing both per size class")
     p.add_argument("--jsonl", default=None, help="also append a sample in the reference's results/*.jsonl format")
     p.add_argument("--no-paths", action="store_true", help="skip timing the other step paths side by side")
+    p.add_argument("--grids", action="store_true",
+                   help="the reference's own published programs and grids, measured its way: one line per grid")
     return p.parse_args(argv)
 
 
@@ -470,10 +472,10 @@ def run_ours(args, dist):
     sim.close()
 
 
-def append_reference_sample(path, sim, worlds, cfg, impl_path, seconds=2.0, warmup=32):
-    """One record in the reference's results/*.jsonl format (crates/auto-cli/src/bench.rs:39-55),
-    measured its way (bench.rs:112-166): warm up, grow the batch until one submit takes >= 20 ms,
-    then run batches for `seconds` and keep the median rate and the 10-90% spread."""
+def reference_rate(sim, seconds=2.0, warmup=32):
+    """Steps/s measured the reference's way (crates/auto-cli/src/bench.rs:112-166): warm up, grow the
+    batch until one submit takes >= 20 ms, then run batches for `seconds`; returns the median rate,
+    the 10-90% spread, the batch and the number of batches."""
     sim.step(warmup)
     sim.wait()
     batch = 1
@@ -496,14 +498,54 @@ def append_reference_sample(path, sim, worlds, cfg, impl_path, seconds=2.0, warm
     rates.sort()
     median = rates[len(rates) // 2]
     spread = (rates[len(rates) * 9 // 10] - rates[len(rates) // 10]) / median
+    return median, spread, batch, len(rates)
+
+
+def append_reference_sample(path, sim, worlds, cfg, impl_path):
+    """One record in the reference's results/*.jsonl format (crates/auto-cli/src/bench.rs:39-55),
+    measured its way (reference_rate)."""
+    median, spread, batch, nb = reference_rate(sim)
     cells = sim.cells_per_step
     w0 = worlds[0]
     rec = {"id": w0.id if len(worlds) == 1 else "batched", "tag": impl_path, "adapter": "NVIDIA GB300 (CUDA, sm_103a)",
            "checks": "Safe", "width": w0.width, "height": w0.height, "cells": cells, "memory_bytes": sim.memory_bytes,
            "steps_per_second": median, "generations_per_second": median, "cells_per_second": median * cells,
-           "batch_steps": batch, "batches": len(rates), "spread": spread}
+           "batch_steps": batch, "batches": nb, "spread": spread}
     with open(path, "a") as f:
         f.write(json.dumps(rec) + "\n")
+
+
+# The reference's published rows for its own programs (results/gpu.jsonl:78-91, RX 7900 XT,
+# wgpu/Vulkan): program, side, cells/s.
+REFERENCE_GRIDS = [("lenia", 512, 6.337e8), ("lenia", 1024, 6.834e8), ("lenia", 2048, 6.272e8),
+                   ("lenia", 4096, 3.174e8), ("lenia", 8192, 1.571e8), ("smoothlife", 1024, 4.561e8),
+                   ("smoothlife", 4096, 2.119e8), ("mnca", 1024, 4.560e8), ("mnca", 4096, 2.135e8)]
+
+
+def run_grids(args, dist):
+    """One JSON line per published grid: the same program and size here, measured the reference's
+    way, next to the reference's own number.  The lenia program starts from U[0,1] patches instead
+    of the reference's Orbium tiling (an FFT step's speed does not depend on the state's values);
+    SmoothLife and MNCA use their own on-device seeds."""
+    import auto_gb300 as ag
+    from auto_gb300 import Sim
+    if dist.rank != 0:
+        return
+    for prog, side, published in REFERENCE_GRIDS:
+        world = {"lenia": ag.lenia, "smoothlife": ag.smoothlife, "mnca": ag.mnca}[prog](side, side)
+        with Sim(world, seed=1, path=args.path) as sim:
+            if prog == "lenia":
+                q = side // 4
+                sim.seed_patches(0, 1, [(q, q, side // 2, side // 2)])
+            if not args.no_autotune:
+                sim.autotune()
+            rate, spread, batch, nb = reference_rate(sim)
+            cells = sim.cells_per_step
+        print(json.dumps({"grid": "%s %dx%d" % (prog, side, side), "path": args.path,
+                          "cells_per_second": rate * cells, "steps_per_second": rate, "spread": spread,
+                          "batch_steps": batch, "batches": nb,
+                          "reference_published": published, "over_reference": rate * cells / published,
+                          "reference_hardware": "AMD RX 7900 XT (wgpu/Vulkan)"}), flush=True)
 
 
 def main():
@@ -514,6 +556,8 @@ def main():
     try:
         if args.impl == "reference":
             run_reference(args, dist)
+        elif args.grids:
+            run_grids(args, dist)
         else:
             run_ours(args, dist)
     finally:
