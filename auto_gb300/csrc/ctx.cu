@@ -535,7 +535,7 @@ int setup_fused(LeniaCtx* ctx) {
                 for (uint32_t c = 0; c < split; c++) row.push_back(RowItem{wi, (int)r, (int)c, 0});
             const bool simple = d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA;
             if (!simple) general = 1;
-            planes = std::max(planes, (int)(simple ? 0 : (d.rule == LENIA_RULE_LENIA ? 1 : d.nkernels)));
+            planes = std::max(planes, simple ? 0 : 1);  // general step: one plane (see row_pass)
             WorldBuffers& b = ctx->wb[wi];
             b.ncol = (int)col.size() - first_col;
             b.nrow = (int)row.size() - first_row;

@@ -401,57 +401,101 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         }
     }
 
-    // General: several channels and/or kernels, or a rule that needs every U at once.  Lenia: the
-    // kernels that target this item's channel add their weighted growth into one plane; SmoothLife
-    // and MNCA keep each kernel's U.
+    // General: several channels and/or kernels, or SmoothLife / MNCA (one channel, two kernels).
+    // Every kernel of the item but the last leaves its result in one shared-memory plane, straight
+    // from the registers of its last inverse stage: Lenia adds its weighted growth, SmoothLife and
+    // MNCA keep the first kernel's U.  The last kernel runs chained (fft_fused): its last inverse
+    // stage, the rule's update with the plane and the state, and the first forward stage stay in
+    // registers.  A thread owns the same cells (sequence s, x = j + m*N/R) in all of these stages,
+    // so the plane needs no barrier of its own.
     if constexpr (!GEN) return;
     const int rule = wd.rule;
-    const int planes = (rule == LENIA_RULE_LENIA) ? 1 : K;
-    float* acc = extra;  // [planes][ROWS][W]
-    for (int e = threadIdx.x; e < planes * ROWS * W; e += NT) acc[e] = 0.0f;
-    for (int k = 0; k < K; k++) {
+    constexpr int R = plan_radix(W, 0), NB = W / R, LAST = plan_len(W) - 1;
+    static_assert(fusable<W>(), "row widths need a plan with equal first and last radix");
+    static_assert(S * NB <= NT, "one butterfly per thread in the chained stages");
+    float* acc = extra;  // [ROWS][W]
+    int nk = 0, klast = -1;
+    for (int k = 0; k < K; k++)
+        if (!per_chan || wd.kern[k].dst == d0) nk++, klast = k;
+    float* st = wd.state + d0 * plane + (size_t)r0 * W;
+    if (nk == 0) {
+        // no kernel targets this channel: the update is the clamp alone
+        for (int e = threadIdx.x; e < ROWS * W; e += NT) st[e] = clamp01(st[e]);
+        __syncthreads();
+        row_item_forward<W, NT>(Z, stw, wd, r0, d0, d0 + 1);
+        return;
+    }
+    if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, ROWS * W * (uint32_t)sizeof(float));
+    bool first = true;
+    for (int k = 0; k < klast; k++) {
         const DevKernel kp = wd.kern[k];
         if (per_chan && kp.dst != d0) continue;
         const Growth growth(kp.mu, kp.sigma);
         load_rows_spectrum<W, S, NT>(Z, wd.conv + k * cplane, H, r0);
         __syncthreads();
-        fft_seqs<W, S, NT, true>(Z, stw);
-        for (int e = threadIdx.x; e < S * W; e += NT) {
-            const int p = e / W, x = e - p * W;
-            const float2 u = Z[p * SEQ + pad(x)];
-            if (rule == LENIA_RULE_LENIA) {
-                float* a = acc;
-                a[(2 * p) * W + x] += kp.weight * growth(u.x);
-                a[(2 * p + 1) * W + x] += kp.weight * growth(u.y);
-            } else {
-                float* a = acc + (size_t)k * ROWS * W;
-                a[(2 * p) * W + x] = u.x;
-                a[(2 * p + 1) * W + x] = u.y;
-            }
-        }
-        __syncthreads();
-    }
-    for (int d = d0; d < d1; d++) {
-        float* st = wd.state + d * plane + (size_t)r0 * W;
-        for (int e = threadIdx.x; e < S * W; e += NT) {
-            const int p = e / W, x = e - p * W;
-            float n[2];
+        fft_stages<W, S, NT, true, 0, LAST>(Z, stw);
+        if ((int)threadIdx.x < S * NB) {
+            const int s = threadIdx.x / NB, j = threadIdx.x - s * NB;
+            float2 v[R];
+            stage_load<W, R, NB, true>(Z + s * SEQ, j, v, stw + stage_tw_offset(W, LAST));
+            float* a = acc + (2 * s) * W + j;
 #pragma unroll
-            for (int q = 0; q < 2; q++) {
-                const int r = 2 * p + q;
-                const float s = st[r * W + x];
-                if (rule == LENIA_RULE_LENIA) n[q] = clamp01(s + wd.dt * acc[r * W + x]);
-                else if (rule == LENIA_RULE_SMOOTHLIFE) n[q] = smoothlife_update(s, acc[r * W + x], acc[ROWS * W + r * W + x]);
-                else n[q] = mnca_update(s, acc[r * W + x], acc[ROWS * W + r * W + x]);
-                st[r * W + x] = n[q];
+            for (int m = 0; m < R; m++) {
+                if (rule == LENIA_RULE_LENIA) {
+                    const float g0 = kp.weight * growth(v[m].x), g1 = kp.weight * growth(v[m].y);
+                    a[m * NB] = first ? g0 : a[m * NB] + g0;
+                    a[W + m * NB] = first ? g1 : a[W + m * NB] + g1;
+                } else {
+                    a[m * NB] = v[m].x;
+                    a[W + m * NB] = v[m].y;
+                }
             }
-            Z[p * SEQ + pad(x)] = make_float2(n[0], n[1]);
         }
-        __syncthreads();
-        fft_seqs<W, S, NT, false>(Z, stw);
-        store_rows_spectrum<W, S, NT>(Z, wd.spec + d * cplane, H, r0);
-        __syncthreads();
+        first = false;
+        __syncthreads();  // Z is rewritten by the next kernel
     }
+    const DevKernel kp = wd.kern[klast];
+    const Growth growth(kp.mu, kp.sigma);
+    const float dt = wd.dt;
+    const bool have_acc = nk > 1;
+    const uint64_t stream = hint::policy_stream();
+    load_rows_spectrum<W, S, NT>(Z, wd.conv + klast * cplane, H, r0);
+    __syncthreads();
+    float sa[R], sb[R];
+    fft_fused<W, S, NT, true, false>(
+        Z, stw,
+        [&](int s, int j, float2* v) {
+            float* ga = st + (2 * s) * W + j;
+            const float* a = acc + (2 * s) * W + j;
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                float n0, n1;
+                if (rule == LENIA_RULE_LENIA) {
+                    float t0 = kp.weight * growth(v[m].x), t1 = kp.weight * growth(v[m].y);
+                    if (have_acc) t0 = a[m * NB] + t0, t1 = a[W + m * NB] + t1;
+                    n0 = clamp01(sa[m] + dt * t0);
+                    n1 = clamp01(sb[m] + dt * t1);
+                } else if (rule == LENIA_RULE_SMOOTHLIFE) {
+                    n0 = smoothlife_update(sa[m], a[m * NB], v[m].x);
+                    n1 = smoothlife_update(sb[m], a[W + m * NB], v[m].y);
+                } else {
+                    n0 = mnca_update(sa[m], a[m * NB], v[m].x);
+                    n1 = mnca_update(sb[m], a[W + m * NB], v[m].y);
+                }
+                hint::st1(ga + m * NB, n0, stream);
+                hint::st1(ga + W + m * NB, n1, stream);
+                v[m] = make_float2(n0, n1);
+            }
+        },
+        [&](int s, int j) {
+            const float* ga = st + (2 * s) * W + j;
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                sa[m] = hint::ld1(ga + m * NB, stream);
+                sb[m] = hint::ld1(ga + W + m * NB, stream);
+            }
+        });
+    store_rows_spectrum<W, S, NT>(Z, wd.spec + d0 * cplane, H, r0);
 }
 
 // ---------------------------------------------------------------------------- column pass
