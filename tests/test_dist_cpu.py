@@ -49,3 +49,20 @@ def test_two_gloo_ranks_shard_and_reduce():
     assert tot0 == tot1 == ca + cb
     assert abs(ca - cb) / (ca + cb) < 0.02
     assert max0 == max1 == 2.0
+
+
+def test_each_rank_sees_only_its_gpu(monkeypatch):
+    """bench.pin_gpu: under torchrun each rank gets CUDA_VISIBLE_DEVICES = its own GPU, picked from an
+    inherited list when there is one; a single process keeps its environment."""
+    import sys
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES", raising=False)
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    monkeypatch.setenv("LOCAL_RANK", "0")
+    assert bench.pin_gpu() == 0 and "CUDA_VISIBLE_DEVICES" not in os.environ
+    monkeypatch.setenv("WORLD_SIZE", "4")
+    monkeypatch.setenv("LOCAL_RANK", "2")
+    assert bench.pin_gpu() == 2 and os.environ["CUDA_VISIBLE_DEVICES"] == "2"
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "4,5,6,7")
+    assert bench.pin_gpu() == 6 and os.environ["CUDA_VISIBLE_DEVICES"] == "6"
