@@ -308,13 +308,13 @@ int flush_spectra(LeniaCtx* ctx) {
         if (n == 0) continue;
         bool ok = true;
         if (n == cl.worlds.size()) {
-            ok = launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, 0, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
+            ok = launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
                                  ctx->d_tw, ctx->stream);
         } else {
             for (int w : cl.worlds) {
                 if (!ctx->dirty[w]) continue;
                 const WorldBuffers& b = ctx->wb[w];
-                ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, 0, ctx->d_worlds, b.d_row, b.nrow,
+                ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_FORWARD, cl.general, ctx->d_worlds, b.d_row, b.nrow,
                                            cl.planes, ctx->d_tw, ctx->stream);
             }
         }
@@ -506,7 +506,15 @@ int setup_fused(LeniaCtx* ctx) {
     for (auto& cl : ctx->classes) {
         std::vector<ColItem> col, tcg;
         std::vector<RowItem> row;
-        int general = 0, planes = 0;
+        // a class takes the general step when any of its worlds needs it; every row launch of the class
+        // then uses the general build, whose items are two rows each from W = 2048 up
+        int general = 0;
+        for (int wi : cl.worlds) {
+            const LeniaWorldDesc& d = ctx->desc[wi];
+            if (!(d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA)) general = 1;
+        }
+        const int planes = general;  // the general step's one shared-memory plane
+        const uint32_t item_rows = (uint32_t)row_item_rows(cl.W, general);
         // tensor-core groups of CT columns, except the first group of every channel: column 0
         // packs the DC and Nyquist columns, which the FP32 pass pairs up (ky with H - ky)
         const bool use_tc = tc_path && tc_supports(cl.H);
@@ -531,11 +539,8 @@ int setup_fused(LeniaCtx* ctx) {
             // Lenia: one row item per target channel (its kernels, update and forward transform), so a
             // multichannel world has C times the row items; other rules: one item for every channel
             const uint32_t split = d.rule == LENIA_RULE_LENIA ? d.channels : 1;
-            for (uint32_t r = 0; r < d.height; r += (uint32_t)row_item_rows((int)d.width))
+            for (uint32_t r = 0; r < d.height; r += item_rows)
                 for (uint32_t c = 0; c < split; c++) row.push_back(RowItem{wi, (int)r, (int)c, 0});
-            const bool simple = d.channels == 1 && d.nkernels == 1 && d.rule == LENIA_RULE_LENIA;
-            if (!simple) general = 1;
-            planes = std::max(planes, simple ? 0 : 1);  // general step: one plane (see row_pass)
             WorldBuffers& b = ctx->wb[wi];
             b.ncol = (int)col.size() - first_col;
             b.nrow = (int)row.size() - first_row;
@@ -579,7 +584,8 @@ int setup_fused(LeniaCtx* ctx) {
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
             if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
-                !launch_row_fp32(cl.W, v, MODE_STEP, 0, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw, ctx->stream))
+                !launch_row_fp32(cl.W, v, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw,
+                                 ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
         }
         if (cl.ntcg > 0 && !launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_tcg, 0, ctx->d_tw, ctx->stream))
@@ -958,7 +964,8 @@ int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host
     const WorldBuffers& b = ctx->wb[world];
     const SizeClass& cl = ctx->classes[b.cls];
     bool ok = launch_columns(ctx, cl, b.d_col, b.ncol, b.d_tcg, b.ntcg, cl.var_col, ctx->stream);
-    ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_U, 0, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw, ctx->stream);
+    ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_U, cl.general, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw,
+                               ctx->stream);
     if (!ok) return fail(ctx, LENIA_ECUDA, "U launch failed");
     CK(cudaGetLastError());
     int rc = refresh_spectrum(ctx, world);

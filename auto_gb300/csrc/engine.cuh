@@ -60,7 +60,7 @@ bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* 
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s);
 size_t col_smem_bytes(int H);
 size_t row_smem_bytes(int W, int acc_planes);
-int row_item_rows(int W);  // rows per row-pass item (two per packed sequence)
+int row_item_rows(int W, int general);  // rows per row-pass item: 4, or 2 (general step, W >= 2048)
 int fp32_local_bytes(int row, int n, int variant);  // spill/stack bytes per thread of a pass instantiation
 int max_smem_optin();
 

@@ -133,7 +133,7 @@ LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, 
     ColItem* col = reinterpret_cast<ColItem*>(base + OFF_COL);
     RowItem* row = reinterpret_cast<RowItem*>(base + OFF_ROW);
     const float2* tw = reinterpret_cast<const float2*>(base + OFF_TW);
-    const int rows = row_item_rows((int)width);
+    const int rows = row_item_rows((int)width, 0);
     const int ncol = spec_tiles((int)width), nrow = (int)height / rows;
     const int n = ncol > nrow ? ncol : nrow;
     noalloc_prepare<<<(n + 255) / 256, 256, 0, s>>>(dw, w, col, ncol, row, nrow, rows);

@@ -18,14 +18,15 @@ size_t col_smem_bytes(int H) {
 }
 size_t row_smem_bytes(int W, int acc_planes) {
     switch (W) {
-#define RS_CASE(N) case N: return row_smem<N>(acc_planes > 0, acc_planes);
+#define RS_CASE(N) \
+    case N: return acc_planes > 0 ? row_smem<N, true>(1, acc_planes) : row_smem<N, false>(0, 0);
         LENIA_SIZES_SMALL(RS_CASE) LENIA_SIZES_LARGE(RS_CASE)
 #undef RS_CASE
     }
     return 0;
 }
 
-int row_item_rows(int W) { return 2 * row_seqs(W); }
+int row_item_rows(int W, int general) { return 2 * row_seqs(W, general != 0); }
 
 int max_smem_optin() {
     int dev = 0, v = 0;

@@ -188,22 +188,24 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 
 // ---------------------------------------------------------------------------- row pass
 //
-// One CTA per item of 2S rows (S packed sequences, row pairs), S = 2.  The code is written for
-// any S; measured at 4096 x 4096, S = 1 (256 threads, three or four CTAs per SM) was 5-30%
-// slower than S = 2 (512 threads, two CTAs per SM), whether the state rows were staged in shared
-// memory or loaded into registers.
-FFT_CHD constexpr int row_seqs(int) { return 2; }
-template <int W>
+// One CTA per item of 2S rows (S packed sequences, row pairs).  The single-kernel step uses S = 2:
+// measured at 4096 x 4096, S = 1 (256 threads, three or four CTAs per SM) was 5-30% slower than
+// S = 2 (512 threads, two CTAs per SM).  The general step keeps a plane of W x 2S floats besides
+// the sequences; from W = 2048 up it uses S = 1 (at S = 2 a 4096-wide item needed 138 KB of shared
+// memory, one CTA per SM; MNCA at 4096 x 4096 measured 7% faster at S = 1), below it S = 2 (the
+// 3-channel 1024 x 1024 world measured 5% slower at S = 1).
+FFT_CHD constexpr int row_seqs(int W, bool gen) { return gen && W >= 2048 ? 1 : 2; }
+template <int W, bool GEN>
 constexpr int row_nt() {
-    constexpr int n = row_seqs(W) * W / plan_radix(W, 0);
+    constexpr int n = row_seqs(W, GEN) * W / plan_radix(W, 0);
     return n < 64 ? 64 : (n > 1024 ? 1024 : n);
 }
 // variant 0: at most 1024 threads' worth of registers per SM (64 a thread at 512 threads);
 // variant 1: at most 128 a thread
-template <int W, int V>
+template <int W, int V, bool GEN>
 constexpr int row_minb() {
     constexpr int t = V == 0 ? 1024 : 512;
-    return t / row_nt<W>() < 1 ? 1 : t / row_nt<W>();
+    return t / row_nt<W, GEN>() < 1 ? 1 : t / row_nt<W, GEN>();
 }
 // Shared memory after the sequences and stage tables: the accumulation planes ([planes][2S][W]) of
 // the general path.
@@ -277,9 +279,9 @@ __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __r
 
 // Row-pass modes that run outside the step (after state writes, and for U-field reads).  Not
 // inlined, so that their registers do not add to the step path's.
-template <int W, int NT>
+template <int W, int NT, int S>
 __device__ __noinline__ void row_item_forward(float2* Z, const float2* stw, const DevWorld& wd, int r0, int d0, int d1) {
-    constexpr int S = row_seqs(W), SEQ = seq_stride(W);
+    constexpr int SEQ = seq_stride(W);
     const int H = wd.H;
     const size_t plane = (size_t)W * H, cplane = (size_t)(W / 2) * H;
     for (int d = d0; d < d1; d++) {
@@ -306,9 +308,9 @@ __device__ __noinline__ void row_item_forward(float2* Z, const float2* stw, cons
     }
 }
 
-template <int W, int NT>
+template <int W, int NT, int S>
 __device__ __noinline__ void row_item_u(float2* Z, const float2* stw, const DevWorld& wd, int r0, int d0, bool per_chan) {
-    constexpr int S = row_seqs(W), SEQ = seq_stride(W);
+    constexpr int SEQ = seq_stride(W);
     const int H = wd.H, K = wd.K;
     const size_t plane = (size_t)W * H, cplane = (size_t)(W / 2) * H;
     for (int k = 0; k < K; k++) {
@@ -334,7 +336,7 @@ __device__ __noinline__ void row_item_u(float2* Z, const float2* stw, const DevW
 template <int W, int NT, int MINB, bool GEN>
 __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items,
                                                 int mode, int general, const float2* __restrict__ tw) {
-    constexpr int S = row_seqs(W), ROWS = 2 * S;
+    constexpr int S = row_seqs(W, GEN), ROWS = 2 * S;
     extern __shared__ float4 smem_raw[];
     constexpr int SEQ = seq_stride(W);
     float2* Z = reinterpret_cast<float2*>(smem_raw);
@@ -350,16 +352,16 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     const int d0 = per_chan ? it.chan : 0, d1 = per_chan ? it.chan + 1 : C;
 
     if (mode == MODE_FORWARD) {
-        row_item_forward<W, NT>(Z, stw, wd, r0, d0, d1);
+        row_item_forward<W, NT, S>(Z, stw, wd, r0, d0, d1);
         return;
     }
     if (mode == MODE_U) {
-        row_item_u<W, NT>(Z, stw, wd, r0, d0, per_chan);
+        row_item_u<W, NT, S>(Z, stw, wd, r0, d0, per_chan);
         return;
     }
 
-    if (!GEN || !general) {
-        // One channel, one kernel, Lenia growth.
+    if constexpr (!GEN) {
+        // One channel, one kernel, Lenia growth (every world of a class that launches this build).
         const DevKernel kp = wd.kern[0];
         const float dtw = wd.dt * kp.weight;
         const Growth growth(kp.mu, kp.sigma);
@@ -401,14 +403,14 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         }
     }
 
-    // General: several channels and/or kernels, or SmoothLife / MNCA (one channel, two kernels).
+    // General: several channels and/or kernels, or SmoothLife / MNCA (one channel, two kernels); also
+    // any one-kernel world that shares a size class with such worlds.
     // Every kernel of the item but the last leaves its result in one shared-memory plane, straight
     // from the registers of its last inverse stage: Lenia adds its weighted growth, SmoothLife and
     // MNCA keep the first kernel's U.  The last kernel runs chained (fft_fused): its last inverse
     // stage, the rule's update with the plane and the state, and the first forward stage stay in
     // registers.  A thread owns the same cells (sequence s, x = j + m*N/R) in all of these stages,
     // so the plane needs no barrier of its own.
-    if constexpr (!GEN) return;
     const int rule = wd.rule;
     constexpr int R = plan_radix(W, 0), NB = W / R, LAST = plan_len(W) - 1;
     static_assert(fusable<W>(), "row widths need a plan with equal first and last radix");
@@ -422,7 +424,7 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
         // no kernel targets this channel: the update is the clamp alone
         for (int e = threadIdx.x; e < ROWS * W; e += NT) st[e] = clamp01(st[e]);
         __syncthreads();
-        row_item_forward<W, NT>(Z, stw, wd, r0, d0, d0 + 1);
+        row_item_forward<W, NT, S>(Z, stw, wd, r0, d0, d0 + 1);
         return;
     }
     if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, ROWS * W * (uint32_t)sizeof(float));
@@ -647,17 +649,17 @@ bool col_go(const DevWorld* worlds, const ColItem* items, int nitems, const floa
 
 // Shared memory of a row-pass launch: sequences, stage tables, then the general path's
 // accumulation planes.
-template <int W>
+template <int W, bool GEN>
 constexpr size_t row_smem(int general, int planes) {
-    const int rows = 2 * row_seqs(W);
-    return (size_t)row_seqs(W) * seq_stride(W) * sizeof(float2) + stage_table_bytes<W>() +
+    const int rows = 2 * row_seqs(W, GEN);
+    return (size_t)row_seqs(W, GEN) * seq_stride(W) * sizeof(float2) + stage_table_bytes<W>() +
            (size_t)(general ? planes : 0) * rows * W * sizeof(float);
 }
 
 template <int W, int NT, int MINB, bool GEN>
 bool row_go(int mode, int general, int planes, const DevWorld* worlds, const RowItem* items, int nitems,
             const float2* tw, cudaStream_t s) {
-    const size_t smem = row_smem<W>(general, planes);
+    const size_t smem = row_smem<W, GEN>(general, planes);
     static int attr_max = 0;
     if ((int)smem > attr_max) {
         if (cudaFuncSetAttribute(row_pass<W, NT, MINB, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -680,8 +682,8 @@ bool row_go(int mode, int general, int planes, const DevWorld* worlds, const Row
 #define LENIA_ROW_CASE_G(N, G)                                                                                   \
     case N:                                                                                                      \
         return (variant & 1)                                                                                     \
-                   ? row_go<N, row_nt<N>(), row_minb<N, 1>(), G>(mode, general, planes, worlds, items, nitems, tw, s) \
-                   : row_go<N, row_nt<N>(), row_minb<N, 0>(), G>(mode, general, planes, worlds, items, nitems, tw, s);
+                   ? row_go<N, row_nt<N, G>(), row_minb<N, 1, G>(), G>(mode, general, planes, worlds, items, nitems, tw, s) \
+                   : row_go<N, row_nt<N, G>(), row_minb<N, 0, G>(), G>(mode, general, planes, worlds, items, nitems, tw, s);
 #define LENIA_ROW_CASE_SIMPLE(N) LENIA_ROW_CASE_G(N, false)
 #define LENIA_ROW_CASE_GENERAL(N) LENIA_ROW_CASE_G(N, true)
 
@@ -697,8 +699,8 @@ int local_bytes_of(F* f) {
                             : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
 #define LENIA_ROW_LOCAL_CASE_G(N, G)                                                    \
     case N:                                                                             \
-        return (variant & 1) ? local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 1>(), G>) \
-                             : local_bytes_of(row_pass<N, row_nt<N>(), row_minb<N, 0>(), G>);
+        return (variant & 1) ? local_bytes_of(row_pass<N, row_nt<N, G>(), row_minb<N, 1, G>(), G>) \
+                             : local_bytes_of(row_pass<N, row_nt<N, G>(), row_minb<N, 0, G>(), G>);
 #define LENIA_ROW_LOCAL_CASE_SIMPLE(N) LENIA_ROW_LOCAL_CASE_G(N, false)
 #define LENIA_ROW_LOCAL_CASE_GENERAL(N) LENIA_ROW_LOCAL_CASE_G(N, true)
 int col_local_bytes_small(int H, int variant);
