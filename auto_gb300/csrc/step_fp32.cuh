@@ -165,12 +165,23 @@ struct Growth {
     }
 };
 
-// SmoothLife update (spectral.rs:396-407).
+// 1 / (1 + e^(x k)) for a compile-time k, with the hardware base-2 exponential and reciprocal (one
+// multiply, ex2, add, rcp).  A large x overflows e^(x k) to +inf, whose reciprocal is the 0 the
+// logistic tends to; a value below 2^-126 flushes to 0 and the result rounds to 1 either way.
+__device__ __forceinline__ float logistic_neg(float x, float k_log2e) {
+    float e, r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(x * k_log2e));
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(1.0f + e));
+    return r;
+}
+
+// SmoothLife update (spectral.rs:396-407): three logistic steps of width 4/AM and 4/AN.
 __device__ __forceinline__ float smoothlife_update(float s, float c0, float c1) {
-    const float B1 = 0.278f, B2 = 0.365f, D1 = 0.267f, D2 = 0.445f, AN = 0.028f, AM = 0.147f, DT = 0.1f;
-    float m = 1.0f / (1.0f + expf((0.5f - c0) * 4.0f / AM));
-    float lo = B1 * (1.0f - m) + D1 * m, hi = B2 * (1.0f - m) + D2 * m;
-    float target = (1.0f / (1.0f + expf((lo - c1) * 4.0f / AN))) * (1.0f - 1.0f / (1.0f + expf((hi - c1) * 4.0f / AN)));
+    const float B1 = 0.278f, B2 = 0.365f, D1 = 0.267f, D2 = 0.445f, DT = 0.1f;
+    const float KM = 39.257007915345945f, KN = 206.09929155556621f;  // (4 / AM) log2(e), (4 / AN) log2(e)
+    const float m = logistic_neg(0.5f - c0, KM);
+    const float lo = B1 * (1.0f - m) + D1 * m, hi = B2 * (1.0f - m) + D2 * m;
+    const float target = logistic_neg(lo - c1, KN) * (1.0f - logistic_neg(hi - c1, KN));
     return clamp01(s + DT * (2.0f * target - 1.0f));
 }
 
