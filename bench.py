@@ -230,30 +230,37 @@ def seed_all(sim, worlds, seeds):
 
 # ----------------------------------------------------------------------------- CPU leg
 
-def cpu_leg(worlds, seeds, max_seconds=20.0, min_steps=1):
+def cpu_leg(worlds, seeds, min_seconds=10.0):
     """The reference's f32 step restated in C (oracle/lenia_oracle.c) on all host cores: a bounded
-    sample of the workload.  Returns (cell-updates/s, cores, sample description)."""
+    sample of the workload, at least `min_seconds` of timed CPU work, one generation of one world at
+    a time, cycling through the workload's one-channel power-of-two worlds.  Returns (cell-updates/s,
+    cores, sample description)."""
     from oracle.oracle import RefF32
     cores = os.cpu_count() or 1
     ref = RefF32(threads=cores)
     todo = [(w, s) for w, s in zip(worlds, seeds)
             if w.channels == 1 and (w.width & (w.width - 1)) == 0 and (w.height & (w.height - 1)) == 0]
+    if not todo:
+        return None, cores, "no world the restated reference step supports"
+    prepared = {}
     cells = 0
     t_total = 0.0
     steps_done = 0
-    for w, s in todo:
-        st = ref.seed_patches(w.width, w.height, s, w.seed.patches)
-        spectra = ref.spectra(w)
+    i = 0
+    while t_total < min_seconds:
+        w, s = todo[i % len(todo)]
+        if i not in prepared:  # initial state and kernel spectrum, outside the timed region
+            prepared[i] = [ref.seed_patches(w.width, w.height, s, w.seed.patches), ref.spectra(w)]
+        st, spectra = prepared[i]
         t0 = time.perf_counter()
-        st = ref.step(w, st, steps=min_steps, spectra=spectra)
+        prepared[i][0] = ref.step(w, st, steps=1, spectra=spectra)
         t_total += time.perf_counter() - t0
-        cells += w.width * w.height * min_steps
-        steps_done += min_steps
-        if t_total > max_seconds:
-            break
-    sample = "%d world-step(s) of the restated reference step (%d power-of-two worlds available), %d threads" % (
-        steps_done, len(todo), cores)
-    return (cells / t_total if t_total > 0 else None), cores, sample
+        cells += w.width * w.height
+        steps_done += 1
+        i = (i + 1) % len(todo) if len(todo) > 1 else 0
+    sample = ("%d generation(s) over %d of the workload's world(s) (one-channel, power-of-two sides), %.1f s "
+              "of CPU time, %d threads" % (steps_done, min(len(todo), steps_done), t_total, cores))
+    return cells / t_total, cores, sample
 
 
 def run_reference(args, dist):
