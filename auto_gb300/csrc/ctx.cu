@@ -552,9 +552,11 @@ int setup_fused(LeniaCtx* ctx) {
         cl.general = general;
         cl.planes = planes;
         // Default launch variant: the 64-register form (more resident CTAs) unless it spills more
-        // than 128 bytes a thread and the 128-register form spills less than half as much.
+        // than 128 bytes a thread and the 128-register form spills less than half as much.  Columns
+        // of 4096 and more take the paired build (measured 8% faster at 4096 x 4096; at 128 to 1024
+        // the scalar builds were faster); the autotuner times all three.
         auto pick = [](int v0, int v1) { return (v0 > 128 && v1 >= 0 && v1 < v0 / 2) ? 1 : 0; };
-        cl.var_col = pick(fp32_local_bytes(0, cl.H, 0), fp32_local_bytes(0, cl.H, 1));
+        cl.var_col = cl.H >= 4096 ? 2 : pick(fp32_local_bytes(0, cl.H, 0), fp32_local_bytes(0, cl.H, 1));
         const int g2 = general ? 2 : 0;
         cl.var_row = pick(fp32_local_bytes(1, cl.W, g2), fp32_local_bytes(1, cl.W, 1 | g2));
         cl.ncol = (int)col.size();
@@ -1103,7 +1105,7 @@ int lenia_autotune(LeniaCtx* ctx) {
         int frc = flush_spectra(ctx);
         if (frc) return frc;
     }
-    // Try both built thread counts for each class's column and row launches; keep the fastest.
+    // Time every built variant of each class's column and row launches; keep the fastest.
     // The trial steps advance the worlds, so every state is saved to a device buffer and restored.
     size_t total = 0;
     for (const auto& d : ctx->desc) total += state_count(d);
@@ -1125,26 +1127,30 @@ int lenia_autotune(LeniaCtx* ctx) {
     CK(cudaEventCreate(&ev.e[1]));
     cudaEvent_t a = ev.e[0], b = ev.e[1];
     const int reps = 5;
+    // column variants: scalar at 64 and 128 registers, paired; row variants: 64 and 128 registers
+    constexpr int NVC = 3, NVR = 2;
     for (auto& cl : ctx->classes) {
-        float tcol[2] = {1e30f, 1e30f}, trow[2] = {1e30f, 1e30f};
-        for (int which = 0; which < 2; which++) {
-            const int ntc = which, ntr = which;
+        float tcol[NVC], trow[NVR];
+        for (int which = 0; which < NVC; which++) {
+            const bool row = which < NVR;
             float t_col = 0, t_row = 0;
             for (int r = 0; r < reps + 1; r++) {
                 CK(cudaEventRecord(a, ctx->stream));
-                bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, ntc, ctx->stream);
+                bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, which, ctx->stream);
                 CK(cudaEventRecord(b, ctx->stream));
                 CK(cudaEventSynchronize(b));
                 float ms = 0;
                 cudaEventElapsedTime(&ms, a, b);
                 if (r) t_col += ms;
-                CK(cudaEventRecord(a, ctx->stream));
-                ok = ok && launch_row_fp32(cl.W, ntr, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
-                                           ctx->d_tw, ctx->stream);
-                CK(cudaEventRecord(b, ctx->stream));
-                CK(cudaEventSynchronize(b));
-                cudaEventElapsedTime(&ms, a, b);
-                if (r) t_row += ms;
+                if (row) {
+                    CK(cudaEventRecord(a, ctx->stream));
+                    ok = ok && launch_row_fp32(cl.W, which, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow,
+                                               cl.planes, ctx->d_tw, ctx->stream);
+                    CK(cudaEventRecord(b, ctx->stream));
+                    CK(cudaEventSynchronize(b));
+                    cudaEventElapsedTime(&ms, a, b);
+                    if (r) t_row += ms;
+                }
                 if (!ok) {
                     cudaGetLastError();
                     t_col = t_row = 1e30f;
@@ -1152,12 +1158,18 @@ int lenia_autotune(LeniaCtx* ctx) {
                 }
             }
             tcol[which] = t_col;
-            trow[which] = t_row;
+            if (row) trow[which] = t_row;
         }
-        // the default variant stays unless the other is at least 3% faster, so that timing noise does
+        // the default variant stays unless another is at least 3% faster, so that timing noise does
         // not flip the choice
-        if (tcol[1 - cl.var_col] < 0.97f * tcol[cl.var_col]) cl.var_col = 1 - cl.var_col;
-        if (trow[1 - cl.var_row] < 0.97f * trow[cl.var_row]) cl.var_row = 1 - cl.var_row;
+        auto choose = [](const float* t, int n, int cur) {
+            int best = cur;
+            for (int i = 0; i < n; i++)
+                if (t[i] < t[best]) best = i;
+            return t[best] < 0.97f * t[cur] ? best : cur;
+        };
+        cl.var_col = choose(tcol, NVC, cl.var_col);
+        cl.var_row = choose(trow, NVR, cl.var_row);
     }
     {
         size_t off = 0;

@@ -52,8 +52,10 @@ enum RowMode { MODE_STEP = 0, MODE_FORWARD = 1, MODE_U = 2 };
 
 // Fused FP32 path (step_fp32_*.cu).  Every size is built in two launch variants with the same
 // threads per CTA: variant 0 caps registers at 64 per thread (more resident CTAs), variant 1 at
-// 128.  The autotuner picks per size class.  The row launcher picks its general build from its
-// `general` argument.  Launchers return false if the size is not built.
+// 128.  The column pass has a third, variant 2: the paired build (both columns of a tile in one
+// sequence of f32x2 pairs, half the threads).  The autotuner picks per size class.  The row
+// launcher picks its general build from its `general` argument.  Launchers return false if the
+// size is not built.
 bool launch_col_fp32(int H, int variant, const DevWorld* worlds, const ColItem* items, int nitems,
                      const float2* tw, cudaStream_t s);
 bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* worlds, const RowItem* items,

@@ -20,6 +20,7 @@
 #define FFT_HD __host__ __device__ __forceinline__
 #define FFT_CHD __host__ __device__
 #else
+#include <math.h>
 #define FFT_HD inline
 #define FFT_CHD
 #ifndef FFT_HOST_FLOAT2
@@ -53,8 +54,71 @@ FFT_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.
 FFT_HD float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); } // a*conj(b)
 FFT_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 FFT_HD float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+FFT_HD float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
 // multiply by exp(sign * i * pi/2): -i for the forward transform, +i for the inverse
 template <bool INV> FFT_HD float2 rot90(float2 z) { return INV ? make_float2(-z.y, z.x) : make_float2(z.y, -z.x); }
+
+// ------------------------------------------------------------------ paired sequences
+// Two sequences transformed side by side, component-paired: re = (a.re, b.re), im = (a.im, b.im).
+// The two always share their twiddles (same butterfly of the same stage), so on sm_100 and later
+// every add, multiply and fma of a pair is one f32x2 instruction, and one 16-byte shared-memory
+// access moves an element of both sequences: the instruction count of one sequence for two.
+struct alignas(16) cpair {
+    float2 re, im;
+};
+// a twiddle held in both halves: rr = (wr, wr), ii = (wi, wi)
+struct alignas(16) tw2 {
+    float2 rr, ii;
+};
+// largest radix of a plan by element type (float2 scalar, cpair paired) and by twiddle type
+template <class T> FFT_CHD constexpr int max_radix() { return 16; }
+template <> FFT_CHD constexpr int max_radix<cpair>() { return 16; }
+template <> FFT_CHD constexpr int max_radix<tw2>() { return 16; }
+FFT_HD float2 f2(float v) { return make_float2(v, v); }
+FFT_HD float2 f2add(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fadd2_rn(a, b);
+#else
+    return make_float2(a.x + b.x, a.y + b.y);
+#endif
+}
+FFT_HD float2 f2sub(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(*reinterpret_cast<unsigned long long*>(&a)),
+        "l"(*reinterpret_cast<unsigned long long*>(&b)));
+    return *reinterpret_cast<float2*>(&r);
+#else
+    return make_float2(a.x - b.x, a.y - b.y);
+#endif
+}
+FFT_HD float2 f2mul(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __fmul2_rn(a, b);
+#else
+    return make_float2(a.x * b.x, a.y * b.y);
+#endif
+}
+FFT_HD float2 f2fma(float2 a, float2 b, float2 c) {  // a * b + c, one rounding
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+    return __ffma2_rn(a, b, c);
+#else
+    return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
+#endif
+}
+FFT_HD cpair cadd(cpair a, cpair b) { return {f2add(a.re, b.re), f2add(a.im, b.im)}; }
+FFT_HD cpair csub(cpair a, cpair b) { return {f2sub(a.re, b.re), f2sub(a.im, b.im)}; }
+FFT_HD cpair cscale(cpair a, float s) { return {f2mul(a.re, f2(s)), f2mul(a.im, f2(s))}; }
+FFT_HD cpair cscale2(cpair a, float2 s) { return {f2mul(a.re, s), f2mul(a.im, s)}; }  // sequence a by s.x, b by s.y
+FFT_HD cpair cneg(cpair a) { return {f2sub(f2(0.0f), a.re), f2sub(f2(0.0f), a.im)}; }
+template <bool INV> FFT_HD cpair rot90(cpair z) {
+    return INV ? cpair{f2sub(f2(0.0f), z.im), z.re} : cpair{z.im, f2sub(f2(0.0f), z.re)};
+}
+FFT_HD tw2 splat(float2 w) { return {f2(w.x), f2(w.y)}; }
+FFT_HD cpair cmul(cpair a, tw2 w) { return {f2sub(f2mul(a.re, w.rr), f2mul(a.im, w.ii)), f2fma(a.re, w.ii, f2mul(a.im, w.rr))}; }
+FFT_HD cpair cmulc(cpair a, tw2 w) { return {f2fma(a.im, w.ii, f2mul(a.re, w.rr)), f2sub(f2mul(a.im, w.rr), f2mul(a.re, w.ii))}; }
+FFT_HD cpair cmul(cpair a, float2 w) { return cmul(a, splat(w)); }
+FFT_HD tw2 cmul(tw2 a, tw2 b) { return {f2sub(f2mul(a.rr, b.rr), f2mul(a.ii, b.ii)), f2fma(a.rr, b.ii, f2mul(a.ii, b.rr))}; }
 
 // exp(sign*2*pi*i*j/R) for compile-time R in {2,4,8,16} and j, via the 16-entry table
 template <int R, bool INV> FFT_HD float2 wR(int j) {
@@ -64,10 +128,10 @@ template <int R, bool INV> FFT_HD float2 wR(int j) {
 
 // z * exp(sign*2*pi*i*j/R) for compile-time j: quarter turns are exact swaps and negations
 // (a general complex multiply by 0 and +-1 would cost four instructions under IEEE rules).
-template <int R, bool INV> FFT_HD float2 cmul_wR(float2 z, int j) {
+template <int R, bool INV, class T> FFT_HD T cmul_wR(T z, int j) {
     const int t = (j * (16 / R)) & 15;
     if (t == 0) return z;
-    if (t == 8) return make_float2(-z.x, -z.y);
+    if (t == 8) return cneg(z);
     if (t == 4) return rot90<INV>(z);
     if (t == 12) return rot90<!INV>(z);
     return cmul(z, wR<R, INV>(j));
@@ -77,11 +141,19 @@ template <int R, bool INV> FFT_HD float2 cmul_wR(float2 z, int j) {
 template <int R, bool INV> struct Dft;
 
 template <bool INV> struct Dft<2, INV> {
-    FFT_HD static void run(float2* v) {
-        float2 a = v[0], b = v[1];
+    template <class T> FFT_HD static void run(T* v) {
+        T a = v[0], b = v[1];
         v[0] = cadd(a, b); v[1] = csub(a, b);
     }
 };
+
+// t -/+ sign*i*c*d for a complex pair of sequences, without a separate negation
+template <bool INV> FFT_HD void rot_pm(cpair t, cpair d, float c, cpair& p, cpair& q) {
+    // forward: sign*i*c*d = (c d.im, -c d.re); inverse: (-c d.im, c d.re)
+    const float2 cc = f2(INV ? -c : c);
+    p = {f2fma(d.im, cc, t.re), f2sub(t.im, f2mul(d.re, cc))};
+    q = {f2sub(t.re, f2mul(d.im, cc)), f2fma(d.re, cc, t.im)};
+}
 
 template <bool INV> struct Dft<3, INV> {
     FFT_HD static void run(float2* v) {
@@ -93,6 +165,12 @@ template <bool INV> struct Dft<3, INV> {
         v[1] = cadd(t, r);
         v[2] = csub(t, r);
     }
+    FFT_HD static void run(cpair* v) {
+        const cpair s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+        const cpair t = {f2fma(s.re, f2(-0.5f), v[0].re), f2fma(s.im, f2(-0.5f), v[0].im)};
+        v[0] = cadd(v[0], s);
+        rot_pm<INV>(t, d, SQRT3_2, v[1], v[2]);
+    }
 };
 
 template <bool INV> struct Dft<4, INV> {
@@ -102,16 +180,29 @@ template <bool INV> struct Dft<4, INV> {
         v[0] = cadd(t0, t2); v[2] = csub(t0, t2);
         v[1] = cadd(t1, t3); v[3] = csub(t1, t3);
     }
+    FFT_HD static void run(cpair* v) {
+        const cpair t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+        const cpair t2 = cadd(v[1], v[3]), d = csub(v[1], v[3]);
+        v[0] = cadd(t0, t2); v[2] = csub(t0, t2);
+        // v1 = t1 + sign*i*d, v3 = t1 - sign*i*d: adds and subtracts of swapped planes
+        if (INV) {
+            v[1] = {f2sub(t1.re, d.im), f2add(t1.im, d.re)};
+            v[3] = {f2add(t1.re, d.im), f2sub(t1.im, d.re)};
+        } else {
+            v[1] = {f2add(t1.re, d.im), f2sub(t1.im, d.re)};
+            v[3] = {f2sub(t1.re, d.im), f2add(t1.im, d.re)};
+        }
+    }
 };
 
 // R = R1 * R2 with m = R2*m1 + m2 and q = q1 + R1*q2:
 //   u[m2][q1] = DFT_R1 over m1 of v[R2*m1 + m2];  u *= w_R^(m2*q1);  y[q1 + R1*q2] = DFT_R2 over m2.
-template <int R1, int R2, bool INV> FFT_HD void dft_split(float2* v) {
+template <int R1, int R2, bool INV, class T> FFT_HD void dft_split(T* v) {
     constexpr int R = R1 * R2;
-    float2 u[R];
+    T u[R];
 #pragma unroll
     for (int m2 = 0; m2 < R2; m2++) {
-        float2 a[R1];
+        T a[R1];
 #pragma unroll
         for (int m1 = 0; m1 < R1; m1++) a[m1] = v[R2 * m1 + m2];
         Dft<R1, INV>::run(a);
@@ -120,7 +211,7 @@ template <int R1, int R2, bool INV> FFT_HD void dft_split(float2* v) {
     }
 #pragma unroll
     for (int q1 = 0; q1 < R1; q1++) {
-        float2 b[R2];
+        T b[R2];
 #pragma unroll
         for (int m2 = 0; m2 < R2; m2++) b[m2] = u[m2 * R1 + q1];
         Dft<R2, INV>::run(b);
@@ -129,8 +220,8 @@ template <int R1, int R2, bool INV> FFT_HD void dft_split(float2* v) {
     }
 }
 
-template <bool INV> struct Dft<8, INV> { FFT_HD static void run(float2* v) { dft_split<4, 2, INV>(v); } };
-template <bool INV> struct Dft<16, INV> { FFT_HD static void run(float2* v) { dft_split<4, 4, INV>(v); } };
+template <bool INV> struct Dft<8, INV> { template <class T> FFT_HD static void run(T* v) { dft_split<4, 2, INV>(v); } };
+template <bool INV> struct Dft<16, INV> { template <class T> FFT_HD static void run(T* v) { dft_split<4, 4, INV>(v); } };
 
 // ------------------------------------------------------------------ radix plans
 // N = 2^a * 3^b (b <= 1).  Every plan starts and ends with the same "outer" radix -- 16 when the
@@ -138,37 +229,40 @@ template <bool INV> struct Dft<16, INV> { FFT_HD static void run(float2* v) { df
 // remaining factor of two and any further 16s in between: 4096 = 16.16.16, 3072 = 16.3.4.16,
 // 384 = 8.3.2.8, 96 = 4.3.2.4.  Equal first and last radix let two transforms be chained in
 // registers (fft_fused), which every size then does.
+// maxr caps the radix (16: 4096 = 16.16.16; 8: 4096 = 8.8.8.8, 2048 = 8.4.8.8).
 struct Plan {
     int len;
-    int r[12];
+    int r[14];
 };
-FFT_CHD constexpr Plan make_plan(int n) {
-    Plan P = {0, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
+FFT_CHD constexpr Plan make_plan(int n, int maxr = 16) {
+    Plan P = {0, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
     const bool three = n % 3 == 0;
     const int p = three ? n / 3 : n;
-    const int outer = p >= 256 ? 16 : p >= 64 ? 8 : p >= 16 ? 4 : p >= 4 ? 2 : 0;
+    int outer = 0;
+    for (int r = 2; r <= maxr; r *= 2)
+        if (r * r <= p) outer = r;
     if (outer == 0) {  // p = 1 or 2: no pair of equal radices
         if (three) P.r[P.len++] = 3;
         if (p == 2) P.r[P.len++] = 2;
         return P;
     }
-    int q = p / (outer * outer), inner16 = 0;
-    while (outer == 16 && q >= 16 && q % 16 == 0) {
-        inner16++;
-        q /= 16;
+    int q = p / (outer * outer), inner = 0;
+    while (outer == maxr && q >= maxr && q % maxr == 0) {
+        inner++;
+        q /= maxr;
     }
     P.r[P.len++] = outer;
     if (three) P.r[P.len++] = 3;
-    if (q > 1) P.r[P.len++] = q;  // 2, 4 or 8
-    for (int i = 0; i < inner16; i++) P.r[P.len++] = 16;
+    if (q > 1) P.r[P.len++] = q;  // below maxr
+    for (int i = 0; i < inner; i++) P.r[P.len++] = maxr;
     P.r[P.len++] = outer;
     return P;
 }
-FFT_CHD constexpr int plan_len(int n) { return make_plan(n).len; }
-FFT_CHD constexpr int plan_radix(int n, int i) { return make_plan(n).r[i]; }
-FFT_CHD constexpr int plan_L(int n, int i) {  // product of the radices before stage i
+FFT_CHD constexpr int plan_len(int n, int maxr = 16) { return make_plan(n, maxr).len; }
+FFT_CHD constexpr int plan_radix(int n, int i, int maxr = 16) { return make_plan(n, maxr).r[i]; }
+FFT_CHD constexpr int plan_L(int n, int i, int maxr = 16) {  // product of the radices before stage i
     int l = 1;
-    for (int s = 0; s < i; s++) l *= plan_radix(n, s);
+    for (int s = 0; s < i; s++) l *= plan_radix(n, s, maxr);
     return l;
 }
 FFT_CHD constexpr bool size_ok(int n) {
@@ -178,26 +272,30 @@ FFT_CHD constexpr bool size_ok(int n) {
 
 // Per-stage twiddle tables.  A stage with L > 1 needs w = exp(-2 pi i k / (L R)) for k < L and,
 // when R >= 8, w^4; they are copied once per CTA from the global table into shared memory.
-FFT_CHD constexpr int stage_tw_count(int n, int i) {
-    return plan_L(n, i) > 1 ? (plan_radix(n, i) >= 8 ? 2 : 1) * plan_L(n, i) : 0;
+FFT_CHD constexpr int stage_tw_count(int n, int i, int maxr = 16) {
+    return plan_L(n, i, maxr) > 1 ? (plan_radix(n, i, maxr) >= 8 ? 2 : 1) * plan_L(n, i, maxr) : 0;
 }
-FFT_CHD constexpr int stage_tw_offset(int n, int i) {
+FFT_CHD constexpr int stage_tw_offset(int n, int i, int maxr = 16) {
     int o = 0;
-    for (int s = 0; s < i; s++) o += stage_tw_count(n, s);
+    for (int s = 0; s < i; s++) o += stage_tw_count(n, s, maxr);
     return o;
 }
-FFT_CHD constexpr int tw_table_size(int n) { return stage_tw_offset(n, plan_len(n)); }
+FFT_CHD constexpr int tw_table_size(int n, int maxr = 16) { return stage_tw_offset(n, plan_len(n, maxr), maxr); }
 
-// Fill the per-stage tables of transform length N from the global table (threads tid of nth).
-template <int N>
-FFT_HD void fill_stage_twiddles(float2* stw, const float2* tw, int tid, int nth) {
-    for (int i = 0; i < plan_len(N); i++) {
-        const int L = plan_L(N, i), R = plan_radix(N, i), off = stage_tw_offset(N, i);
+// Fill the per-stage tables of transform length N from the global table (threads tid of nth);
+// a tw2 table holds each twiddle in both halves, for paired sequences.
+FFT_HD void set_twiddle(float2& d, float2 w) { d = w; }
+FFT_HD void set_twiddle(tw2& d, float2 w) { d = splat(w); }
+template <int N, class W>
+FFT_HD void fill_stage_twiddles(W* stw, const float2* tw, int tid, int nth) {
+    constexpr int MR = max_radix<W>();
+    for (int i = 0; i < plan_len(N, MR); i++) {
+        const int L = plan_L(N, i, MR), R = plan_radix(N, i, MR), off = stage_tw_offset(N, i, MR);
         if (L == 1) continue;
         const int step = TWN / (L * R);
         for (int k = tid; k < L; k += nth) {
-            stw[off + k] = tw[k * step];
-            if (R >= 8) stw[off + L + k] = tw[4 * k * step];
+            set_twiddle(stw[off + k], tw[k * step]);
+            if (R >= 8) set_twiddle(stw[off + L + k], tw[4 * k * step]);
         }
     }
 }
@@ -211,8 +309,8 @@ FFT_CHD constexpr int seq_stride(int n) { return n + n / 16 + 4; }
 // Twiddles w^m, m = 1..R-1, of one butterfly from w and (R >= 8) w^4; the other powers are
 // products of at most three factors, so each stays within a few float ulps of the exactly rounded
 // value (checked against numpy by the host test).
-template <int R>
-FFT_HD void twiddle_powers(float2 w1, float2 w4, float2* w) {
+template <int R, class W>
+FFT_HD void twiddle_powers(W w1, W w4, W* w) {
     w[1] = w1;
     if (R >= 3) w[2] = cmul(w[1], w[1]);
     if (R >= 4) w[3] = cmul(w[2], w[1]);
@@ -234,14 +332,14 @@ FFT_HD void twiddle_powers(float2 w1, float2 w4, float2* w) {
 
 // Load butterfly j of a stage (with its inter-stage twiddle) from one sequence; stw is the
 // stage's twiddle table (see fill_stage_twiddles).
-template <int N, int R, int L, bool INV>
-FFT_HD void stage_load(const float2* seq, int j, float2* v, const float2* stw) {
+template <int N, int R, int L, bool INV, class T, class W>
+FFT_HD void stage_load(const T* seq, int j, T* v, const W* stw) {
     constexpr int NB = N / R;
     const int k = j % L;
 #pragma unroll
     for (int m = 0; m < R; m++) v[m] = seq[pad(j + m * NB)];
     if (L > 1) {
-        float2 w[R];
+        W w[R];
         twiddle_powers<R>(stw[k], R >= 8 ? stw[L + k] : stw[k], w);
 #pragma unroll
         for (int m = 1; m < R; m++) v[m] = INV ? cmulc(v[m], w[m]) : cmul(v[m], w[m]);
@@ -249,8 +347,8 @@ FFT_HD void stage_load(const float2* seq, int j, float2* v, const float2* stw) {
     Dft<R, INV>::run(v);
 }
 
-template <int N, int R, int L>
-FFT_HD void stage_store(float2* seq, int j, const float2* v) {
+template <int N, int R, int L, class T>
+FFT_HD void stage_store(T* seq, int j, const T* v) {
     const int k = j % L;
     const int base = (j - k) * R + k;
 #pragma unroll

@@ -12,8 +12,12 @@ static size_t col_khat_bytes_of(int H) {
     return 0;
 }
 
+// the larger of the scalar and paired builds (same sequence bytes; the paired stage tables hold
+// each twiddle twice)
 size_t col_smem_bytes(int H) {
-    return (size_t)TC * lfft::seq_stride(H) * sizeof(float2) + (lfft::tw_table_size(H) + 1) * sizeof(float2) +
+    const size_t scalar_tables = (lfft::tw_table_size(H) + 1) * sizeof(float2);
+    const size_t paired_tables = (lfft::tw_table_size(H, PMR) + 1) * sizeof(lfft::tw2);
+    return (size_t)TC * lfft::seq_stride(H) * sizeof(float2) + (scalar_tables > paired_tables ? scalar_tables : paired_tables) +
            col_khat_bytes_of(H);
 }
 size_t row_smem_bytes(int W, int acc_planes) {

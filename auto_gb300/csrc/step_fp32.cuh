@@ -49,22 +49,23 @@ __device__ __forceinline__ void static_for(F&& f) {
 // Stages [I, I1) of the transform of S sequences of length N in shared memory (stride
 // seq_stride(N)), in place, by NT threads; stw holds the per-stage twiddle tables
 // (fill_stage_twiddles).  Starts after the caller's barrier; ends with a barrier.
-template <int N, int S, int NT, bool INV, int I, int I1>
-__device__ __forceinline__ void fft_stages(float2* buf, const float2* stw) {
+template <int N, int S, int NT, bool INV, int I, int I1, class T, class W>
+__device__ __forceinline__ void fft_stages(T* buf, const W* stw) {
     if constexpr (I < I1) {
-        constexpr int R = plan_radix(N, I);
-        constexpr int L = plan_L(N, I);
+        constexpr int MR = max_radix<T>();
+        constexpr int R = plan_radix(N, I, MR);
+        constexpr int L = plan_L(N, I, MR);
         constexpr int NB = N / R;
         constexpr int TOT = NB * S;
         constexpr int PER = (TOT + NT - 1) / NT;
         constexpr int SEQ = seq_stride(N);
-        float2 v[PER][R];
+        T v[PER][R];
 #pragma unroll
         for (int p = 0; p < PER; p++) {
             const int b = threadIdx.x + p * NT;
             if ((TOT % NT) == 0 || b < TOT) {
                 const int s = b / NB, j = b - s * NB;
-                stage_load<N, R, L, INV>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, I));
+                stage_load<N, R, L, INV>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, I, MR));
             }
         }
         __syncthreads();
@@ -81,9 +82,9 @@ __device__ __forceinline__ void fft_stages(float2* buf, const float2* stw) {
     }
 }
 
-template <int N, int S, int NT, bool INV>
-__device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
-    fft_stages<N, S, NT, INV, 0, plan_len(N)>(buf, stw);
+template <int N, int S, int NT, bool INV, class T, class W>
+__device__ __forceinline__ void fft_seqs(T* buf, const W* stw) {
+    fft_stages<N, S, NT, INV, 0, plan_len(N, max_radix<T>())>(buf, stw);
 }
 
 // Two transforms back to back (A, then B) with work on the values in between.  When the plan's
@@ -92,30 +93,31 @@ __device__ __forceinline__ void fft_seqs(float2* buf, const float2* stw) {
 // `mid(s, j, v)` runs on those registers (sequence s, elements j + m*N/R) and B's first stage
 // follows without a round trip through shared memory: two barriers and one shared-memory
 // read/write sweep fewer than A, mid-pass, B.  `pre(s, j)` runs just before the last stage of A.
-template <int N>
+template <int N, int MR = 16>
 FFT_CHD constexpr bool fusable() {
-    return plan_len(N) >= 2 && plan_radix(N, 0) == plan_radix(N, plan_len(N) - 1);
+    return plan_len(N, MR) >= 2 && plan_radix(N, 0, MR) == plan_radix(N, plan_len(N, MR) - 1, MR);
 }
 
 struct NoPre {
     __device__ void operator()(int, int) const {}
 };
 
-template <int N, int S, int NT, bool INV_A, bool INV_B, class Mid, class Pre = NoPre>
-__device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Mid mid, Pre pre = Pre()) {
-    constexpr int LAST = plan_len(N) - 1;
-    constexpr int R = plan_radix(N, LAST), L = plan_L(N, LAST), NB = N / R;
-    static_assert(L == NB && plan_radix(N, 0) == R, "fusable plans only");
+template <int N, int S, int NT, bool INV_A, bool INV_B, class T, class W, class Mid, class Pre = NoPre>
+__device__ __forceinline__ void fft_fused(T* buf, const W* stw, Mid mid, Pre pre = Pre()) {
+    constexpr int MR = max_radix<T>();
+    constexpr int LAST = plan_len(N, MR) - 1;
+    constexpr int R = plan_radix(N, LAST, MR), L = plan_L(N, LAST, MR), NB = N / R;
+    static_assert(L == NB && plan_radix(N, 0, MR) == R, "fusable plans only");
     constexpr int TOT = NB * S, PER = (TOT + NT - 1) / NT, SEQ = seq_stride(N);
     fft_stages<N, S, NT, INV_A, 0, LAST>(buf, stw);
-    float2 v[PER][R];
+    T v[PER][R];
 #pragma unroll
     for (int p = 0; p < PER; p++) {
         const int b = threadIdx.x + p * NT;
         if ((TOT % NT) == 0 || b < TOT) {
             const int s = b / NB, j = b - s * NB;
             pre(s, j);  // global loads that mid needs, issued before the last stage of A
-            stage_load<N, R, L, INV_A>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, LAST));
+            stage_load<N, R, L, INV_A>(buf + s * SEQ, j, v[p], stw + stage_tw_offset(N, LAST, MR));
             mid(s, j, v[p]);
             Dft<R, INV_B>::run(v[p]);  // B's first stage: L = 1, no twiddle
         }
@@ -127,7 +129,7 @@ __device__ __forceinline__ void fft_fused(float2* buf, const float2* stw, Mid mi
         if ((TOT % NT) == 0 || b < TOT) stage_store<N, R, 1>(buf + (b / NB) * SEQ, b % NB, v[p]);
     }
     __syncthreads();
-    fft_stages<N, S, NT, INV_B, 1, plan_len(N)>(buf, stw);
+    fft_stages<N, S, NT, INV_B, 1, plan_len(N, MR)>(buf, stw);
 }
 
 // Shared memory of a pass: the sequences, then (float2-aligned) the stage twiddle tables.
@@ -631,6 +633,117 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
                               wd.khat + (size_t)k * (W / 2 + 1) * HQ, HQ, W, t);
 }
 
+// ------------------------------------------------------------------ paired column pass
+// The tile's two spectrum columns as one sequence of cpair elements (re = (c0.re, c1.re),
+// im = (c0.im, c1.im)): one thread runs butterfly j of both columns with f32x2 arithmetic and
+// 16-byte shared-memory accesses, so the item needs half the threads and about half the
+// instructions of the scalar build.  Shared memory: the sequence, the tw2 stage tables, the khat
+// columns.
+constexpr int PMR = max_radix<cpair>();  // largest radix of the paired builds' plans
+template <int H>
+__device__ __forceinline__ float* col_khat_smem_pair(tw2* stw) {
+    return reinterpret_cast<float*>(stw + tw_table_size(H, PMR) + 1);
+}
+
+template <int H, int NT>
+__device__ __forceinline__ void load_tile_pair(cpair* X, const float2* __restrict__ src) {
+    constexpr int IT = (H + NT - 1) / NT;
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float4 v[IT];
+#pragma unroll
+    for (int i = 0; i < IT; i++) {
+        const int y = threadIdx.x + i * NT;
+        if (IT * NT == H || y < H) v[i] = hint::ld4(s4 + y, hint::policy_keep());
+    }
+#pragma unroll
+    for (int i = 0; i < IT; i++) {
+        const int y = threadIdx.x + i * NT;
+        if (IT * NT == H || y < H) X[pad(y)] = cpair{make_float2(v[i].x, v[i].z), make_float2(v[i].y, v[i].w)};
+    }
+}
+
+template <int H, int NT>
+__device__ __forceinline__ void store_tile_pair(const cpair* X, float2* __restrict__ dst) {
+    float4* d4 = reinterpret_cast<float4*>(dst);
+    for (int y = threadIdx.x; y < H; y += NT) {
+        const cpair a = X[pad(y)];
+        hint::st4(d4 + y, make_float4(a.re.x, a.im.x, a.re.y, a.im.y), hint::policy_keep());
+    }
+}
+
+// The khat multiply of an unchained item (see multiply_khat): column 1 (lane y) by its khat
+// column; in tile 0, column 0 (lane x) packs the DC and Nyquist columns and pairs ky with H - ky.
+template <int H, int NT>
+__device__ __forceinline__ void multiply_khat_pair(cpair* X, const float* __restrict__ kh, int HQ, int W, int t) {
+    const float* k0 = kh + (size_t)(TC * t) * HQ;
+    const float* k1 = k0 + HQ;
+    if (t != 0) {
+        for (int ky = threadIdx.x; ky < H; ky += NT) {
+            const int kk = ky <= H / 2 ? ky : H - ky;
+            X[pad(ky)] = cscale2(X[pad(ky)], make_float2(k0[kk], k1[kk]));
+        }
+        return;
+    }
+    for (int ky = threadIdx.x; ky <= H / 2; ky += NT) {
+        const float K0 = kh[ky], KN = kh[(size_t)(W / 2) * HQ + ky], kv = k1[ky];
+        const float a = 0.5f * (K0 + KN), b = 0.5f * (K0 - KN);
+        const int km = (H - ky) % H;
+        const cpair z = X[pad(ky)], zm = X[pad(km)];
+        X[pad(ky)] = cpair{make_float2(z.re.x * a + zm.re.x * b, z.re.y * kv),
+                           make_float2(z.im.x * a - zm.im.x * b, z.im.y * kv)};
+        if (km != ky)
+            X[pad(km)] = cpair{make_float2(zm.re.x * a + z.re.x * b, zm.re.y * kv),
+                               make_float2(zm.im.x * a - z.im.x * b, zm.im.y * kv)};
+    }
+}
+
+template <int H, int NT>
+__device__ __noinline__ void col_item_unchained_pair(cpair* X, const tw2* stw, const float2* src, float2* dst,
+                                                     const float* kh, int HQ, int W, int t) {
+    load_tile_pair<H, NT>(X, src);
+    __syncthreads();
+    fft_seqs<H, 1, NT, false>(X, stw);
+    multiply_khat_pair<H, NT>(X, kh, HQ, W, t);
+    __syncthreads();
+    fft_seqs<H, 1, NT, true>(X, stw);
+    store_tile_pair<H, NT>(X, dst);
+}
+
+template <int H, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) col_pass_pair(const DevWorld* __restrict__ worlds,
+                                                     const ColItem* __restrict__ items, const float2* __restrict__ tw) {
+    extern __shared__ float4 smem_raw[];
+    cpair* X = reinterpret_cast<cpair*>(smem_raw);
+    tw2* stw = reinterpret_cast<tw2*>(X + seq_stride(H));
+    fill_stage_twiddles<H>(stw, tw, threadIdx.x, NT);
+    const ColItem it = items[blockIdx.x];
+    const DevWorld& wd = worlds[it.world];
+    const int W = wd.W, c = it.chan, t = it.tile, k = it.kernel, HQ = wd.HQ;
+    const size_t cplane = (size_t)(W / 2) * H;
+    const float2* src = wd.spec + c * cplane + (size_t)t * H * TC;
+    float2* dst = wd.conv + k * cplane + (size_t)t * H * TC;
+    constexpr int HQC = khat_cols_stride<H>();
+    const float* kh = wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)TC * t) * HQC;
+    if (fusable<H, PMR>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
+        float* ksm = col_khat_smem_pair<H>(stw);
+        for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
+        load_tile_pair<H, NT>(X, src);
+        cp_async_wait_all();
+        __syncthreads();
+        fft_fused<H, 1, NT, false, true>(X, stw, [&](int, int j, cpair* v) {
+            constexpr int R = plan_radix(H, 0, PMR), NB = H / R;
+#pragma unroll
+            for (int m = 0; m < R; m++) {
+                const int ky = j + m * NB, kk = ky <= H / 2 ? ky : H - ky;
+                v[m] = cscale2(v[m], make_float2(ksm[kk], ksm[HQC + kk]));
+            }
+        });
+        store_tile_pair<H, NT>(X, dst);
+        return;
+    }
+    col_item_unchained_pair<H, NT>(X, stw, src, dst, wd.khat + (size_t)k * (W / 2 + 1) * HQ, HQ, W, t);
+}
+
 // Sizes built: each TU instantiates one group.  Threads per CTA: one first-stage butterfly per
 // thread for the two sequences a CTA holds (2N / first radix), between 64 and 1024.
 #define LENIA_SIZES_SMALL(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768)
@@ -641,6 +754,13 @@ template <int N> constexpr int nt_of() {
 }
 // variant 0: at most 64 registers per thread; variant 1: at most 128
 template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) / nt_of<N>() < 1 ? 1 : (V == 0 ? 1024 : 512) / nt_of<N>(); }
+// paired column build: one first-stage butterfly per thread for the one (paired) sequence, at most
+// 128 registers a thread
+template <int N> constexpr int nt_pair_of() {
+    constexpr int n = N / plan_radix(N, 0, PMR);
+    return n < 64 ? 64 : (n > 1024 ? 1024 : n);
+}
+template <int N> constexpr int minb_pair_of() { return 512 / nt_pair_of<N>() < 1 ? 1 : 512 / nt_pair_of<N>(); }
 
 // Launch one instantiation.  Dynamic shared memory above 48 KB must be enabled per kernel before
 // its first launch and before any stream capture that contains it; a zero-item call does just that.
@@ -655,6 +775,25 @@ bool col_go(const DevWorld* worlds, const ColItem* items, int nitems, const floa
         attr_max = (int)smem;
     }
     if (nitems > 0) col_pass<H, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, tw);
+    return true;
+}
+
+template <int H>
+constexpr size_t col_pair_smem() {
+    return (size_t)seq_stride(H) * sizeof(cpair) + (size_t)(tw_table_size(H, PMR) + 1) * sizeof(tw2) + col_khat_bytes<H>();
+}
+
+template <int H, int NT, int MINB>
+bool col_go_pair(const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
+    const size_t smem = col_pair_smem<H>();
+    static int attr_max = 0;
+    if ((int)smem > attr_max) {
+        if (cudaFuncSetAttribute(col_pass_pair<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return false;
+        attr_max = (int)smem;
+    }
+    if (nitems > 0) col_pass_pair<H, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, tw);
     return true;
 }
 
@@ -682,10 +821,13 @@ bool row_go(int mode, int general, int planes, const DevWorld* worlds, const Row
     return true;
 }
 
-#define LENIA_COL_CASE(N)                                                                      \
-    case N:                                                                                    \
-        return variant == 0 ? col_go<N, nt_of<N>(), minb_of<N, 0>()>(worlds, items, nitems, tw, s) \
-                            : col_go<N, nt_of<N>(), minb_of<N, 1>()>(worlds, items, nitems, tw, s);
+// Column-pass builds: variant 0 and 1 are the scalar build at 64 and 128 registers a thread,
+// variant 2 the paired build.
+#define LENIA_COL_CASE(N)                                                                                   \
+    case N:                                                                                                 \
+        return variant == 2   ? col_go_pair<N, nt_pair_of<N>(), minb_pair_of<N>()>(worlds, items, nitems, tw, s) \
+               : variant == 1 ? col_go<N, nt_of<N>(), minb_of<N, 1>()>(worlds, items, nitems, tw, s)           \
+                              : col_go<N, nt_of<N>(), minb_of<N, 0>()>(worlds, items, nitems, tw, s);
 
 // Row-pass builds: variant bit 0 selects the register cap (row_minb); the single-kernel (GEN =
 // false) and general (GEN = true) builds sit in separate translation units, which keeps each
@@ -704,10 +846,11 @@ int local_bytes_of(F* f) {
     cudaFuncAttributes a;
     return cudaFuncGetAttributes(&a, f) == cudaSuccess ? (int)a.localSizeBytes : -1;
 }
-#define LENIA_COL_LOCAL_CASE(N)                                                    \
-    case N:                                                                        \
-        return variant == 0 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>) \
-                            : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
+#define LENIA_COL_LOCAL_CASE(N)                                                                 \
+    case N:                                                                                     \
+        return variant == 2   ? local_bytes_of(col_pass_pair<N, nt_pair_of<N>(), minb_pair_of<N>()>) \
+               : variant == 1 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>)              \
+                              : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>);
 #define LENIA_ROW_LOCAL_CASE_G(N, G)                                                    \
     case N:                                                                             \
         return (variant & 1) ? local_bytes_of(row_pass<N, row_nt<N, G>(), row_minb<N, 1, G>(), G>) \

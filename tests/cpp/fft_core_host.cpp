@@ -32,7 +32,39 @@ static int fft_n(int inverse, const float* in, float* out, const float2* tw) {
     return 0;
 }
 
-extern "C" int fft_host(int n, int inverse, const float* in, float* out) {
+// Two sequences at once, component-paired (cpair elements, tw2 stage tables), as the paired
+// GPU builds run them.
+template <int N, int I, bool INV>
+static void run_stage_pair(cpair* seq, const tw2* tw) {
+    constexpr int MR = max_radix<cpair>();
+    if constexpr (I < plan_len(N, MR)) {
+        constexpr int R = plan_radix(N, I, MR);
+        constexpr int L = plan_L(N, I, MR);
+        std::vector<cpair> v((N / R) * R);
+        for (int j = 0; j < N / R; j++) stage_load<N, R, L, INV>(seq, j, &v[j * R], tw + stage_tw_offset(N, I, MR));
+        for (int j = 0; j < N / R; j++) stage_store<N, R, L>(seq, j, &v[j * R]);
+        run_stage_pair<N, I + 1, INV>(seq, tw);
+    }
+}
+
+template <int N>
+static int fft_pair_n(int inverse, const float* a, const float* b, float* oa, float* ob, const float2* tw) {
+    std::vector<cpair> seq(seq_stride(N));
+    std::vector<tw2> stw(tw_table_size(N, max_radix<cpair>()) + 1);
+    fill_stage_twiddles<N>(stw.data(), tw, 0, 1);
+    for (int i = 0; i < N; i++)
+        seq[pad(i)] = cpair{make_float2(a[2 * i], b[2 * i]), make_float2(a[2 * i + 1], b[2 * i + 1])};
+    if (inverse) run_stage_pair<N, 0, true>(seq.data(), stw.data());
+    else run_stage_pair<N, 0, false>(seq.data(), stw.data());
+    for (int i = 0; i < N; i++) {
+        const cpair z = seq[pad(i)];
+        oa[2 * i] = z.re.x; oa[2 * i + 1] = z.im.x;
+        ob[2 * i] = z.re.y; ob[2 * i + 1] = z.im.y;
+    }
+    return 0;
+}
+
+static const float2* table() {
     static std::vector<float2> tw;
     if (tw.empty()) {
         tw.resize(TWN);
@@ -41,10 +73,26 @@ extern "C" int fft_host(int n, int inverse, const float* in, float* out) {
             tw[t] = make_float2((float)std::cos(a), (float)std::sin(a));
         }
     }
+    return tw.data();
+}
+
+#define FFT_SIZES(CASE)                                                                                 \
+    CASE(16) CASE(32) CASE(48) CASE(64) CASE(96) CASE(128) CASE(192) CASE(256) CASE(384) CASE(512) \
+    CASE(768) CASE(1024) CASE(1536) CASE(2048) CASE(3072) CASE(4096) CASE(8192)
+
+extern "C" int fft_host(int n, int inverse, const float* in, float* out) {
     switch (n) {
-#define CASE(N) case N: return fft_n<N>(inverse, in, out, tw.data());
-        CASE(16) CASE(32) CASE(48) CASE(64) CASE(96) CASE(128) CASE(192) CASE(256) CASE(384) CASE(512)
-        CASE(768) CASE(1024) CASE(1536) CASE(2048) CASE(3072) CASE(4096) CASE(8192)
+#define CASE(N) case N: return fft_n<N>(inverse, in, out, table());
+        FFT_SIZES(CASE)
+#undef CASE
+    }
+    return -1;
+}
+
+extern "C" int fft_host_pair(int n, int inverse, const float* a, const float* b, float* oa, float* ob) {
+    switch (n) {
+#define CASE(N) case N: return fft_pair_n<N>(inverse, a, b, oa, ob, table());
+        FFT_SIZES(CASE)
 #undef CASE
     }
     return -1;

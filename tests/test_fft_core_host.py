@@ -33,3 +33,20 @@ def test_stockham_plan_matches_numpy(fft_host, n, inverse):
     x64 = x.astype(np.complex128)
     want = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
     assert np.abs(out - want).max() / np.abs(want).max() < 2e-7
+
+
+@pytest.mark.parametrize("n", SIZES)
+@pytest.mark.parametrize("inverse", [0, 1])
+def test_paired_sequences_match_numpy(fft_host, n, inverse):
+    """Two sequences through the same stages as cpair elements (re and im planes of both in one
+    16-byte element, twiddles held twice): each must come out as its own FFT."""
+    rng = np.random.default_rng(1000 + n + inverse)
+    a = (rng.random(n) + 1j * rng.random(n)).astype(np.complex64)
+    b = (rng.random(n) - 1j * rng.random(n)).astype(np.complex64)
+    oa, ob = np.zeros(n, np.complex64), np.zeros(n, np.complex64)
+    ptr = lambda x: x.ctypes.data_as(ctypes.c_void_p)
+    assert fft_host.fft_host_pair(n, inverse, ptr(a), ptr(b), ptr(oa), ptr(ob)) == 0
+    for x, out in ((a, oa), (b, ob)):
+        x64 = x.astype(np.complex128)
+        want = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
+        assert np.abs(out - want).max() / np.abs(want).max() < 2e-7

@@ -212,6 +212,31 @@ def test_largest_sides_teacher_forced_vs_fp64(w, h, nk):
     assert np.abs(got - fp64_step(world, s)).max() < 1e-4
 
 
+SIDES = [32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536, 2048, 3072, 4096, 6144, 8192]
+
+
+@pytest.mark.parametrize("nk,tune", [(1, False), (2, False), (1, True), (2, True)])
+def test_every_side_on_both_axes_teacher_forced_vs_fp64(nk, tune):
+    """Every supported side as the width (the row pass at that length) and as the height (the
+    column pass), the other side 32, all in one context, one step from a random state.  nk = 1
+    runs the single-kernel builds, nk = 2 the general ones; with tune the autotuner first times
+    both launch variants of every size class and keeps the faster."""
+    kernels = [ag.Kernel(radius=5.0, beta=[1.0, 0.5])] + [ag.Kernel(radius=3.0, mu=0.2, sigma=0.03, weight=0.5)] * (nk - 1)
+    worlds = [ag.World(n, 32, kernels, dt=0.1) for n in SIDES] + [ag.World(32, n, kernels, dt=0.1) for n in SIDES[1:]]
+    rng = np.random.default_rng(17 + nk)
+    states = [rng.random((1, w.height, w.width), dtype=np.float32) for w in worlds]
+    with Sim(worlds) as sim:
+        for i, s in enumerate(states):
+            sim.write_state(i, s)
+        if tune:
+            sim.autotune()
+            assert all(np.array_equal(sim.read_state(i), s) for i, s in enumerate(states))
+        sim.step(1)
+        for i, w in enumerate(worlds):
+            err = float(np.abs(sim.read_state(i) - fp64_step(w, states[i])).max())
+            assert err < 1e-4, (w.width, w.height, err)
+
+
 def test_batched_worlds_teacher_forced_vs_fp64():
     worlds = configs.batched(32)
     with Sim(worlds, seed=0) as sim:
