@@ -48,8 +48,6 @@ FFT_CHD constexpr float c16(int t) {
 FFT_CHD constexpr float s16(int t) { return c16((t + 12) & 15); }  // sin(x) = cos(x - pi/2)
 constexpr float SQRT3_2 = 0.86602540378443865f;
 
-FFT_HD float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-FFT_HD float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 FFT_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 FFT_HD float2 cmulc(float2 a, float2 b) { return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); } // a*conj(b)
 FFT_HD float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
@@ -106,6 +104,10 @@ FFT_HD float2 f2fma(float2 a, float2 b, float2 c) {  // a * b + c, one rounding
     return make_float2(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y));
 #endif
 }
+// a complex add or subtract of one float2 is one f32x2 instruction (two IEEE adds, so the results
+// are those of the two scalar adds)
+FFT_HD float2 cadd(float2 a, float2 b) { return f2add(a, b); }
+FFT_HD float2 csub(float2 a, float2 b) { return f2add(a, make_float2(-b.x, -b.y)); }
 FFT_HD cpair cadd(cpair a, cpair b) { return {f2add(a.re, b.re), f2add(a.im, b.im)}; }
 FFT_HD cpair csub(cpair a, cpair b) { return {f2sub(a.re, b.re), f2sub(a.im, b.im)}; }
 FFT_HD cpair cscale(cpair a, float s) { return {f2mul(a.re, f2(s)), f2mul(a.im, f2(s))}; }
