@@ -1098,6 +1098,23 @@ int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const 
     return 0;
 }
 
+int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) {
+    if (!ctx) return LENIA_EINVAL;
+    if (col_variant < -1 || col_variant > 2 || row_variant < -1 || row_variant > 1)
+        return fail(ctx, LENIA_EINVAL, "launch variants are -1..2 (column) and -1..1 (row), got %d and %d", col_variant,
+                    row_variant);
+    if (ctx->path == LENIA_PATH_RADIX2) return 0;  // one build per stage: nothing to choose
+    for (auto& cl : ctx->classes) {
+        if (col_variant >= 0) cl.var_col = col_variant;
+        if (row_variant >= 0) cl.var_row = row_variant;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
 int lenia_autotune(LeniaCtx* ctx) {
     if (!ctx) return LENIA_EINVAL;
     if (ctx->path == LENIA_PATH_RADIX2) return 0;

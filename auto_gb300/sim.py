@@ -176,6 +176,10 @@ class Sim:
     def autotune(self):
         self._check(self._L.lenia_autotune(self._ctx))
 
+    def set_variants(self, column: int = -1, row: int = -1):
+        """Pin every size class's launch variants (see lenia_set_variants); -1 keeps one."""
+        self._check(self._L.lenia_set_variants(self._ctx, int(column), int(row)))
+
     def profile(self, steps: int = 10):
         """Event-timed (column ms, row ms, step ms) per step."""
         out = np.zeros(3, np.float32)

@@ -170,6 +170,13 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
  * and keeps the fastest.  Rebuilds the step graphs.  Optional; defaults are reasonable. */
 LENIA_API int lenia_autotune(LeniaCtx* ctx);
 
+/* Pins the launch variant of every size class, in place of the defaults or the autotuner's
+ * choice: column 0 and 1 are the scalar build at 64 and 128 registers a thread, 2 the paired
+ * build (both columns of a tile as f32x2 pairs); row 0 and 1 the two register caps; -1 keeps a
+ * pass's current choice.  Results do not depend on the variant beyond float rounding.  Rebuilds
+ * the step graphs.  No reference counterpart: the reference has one launch shape per pass. */
+LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant);
+
 /* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
  * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.
  * out[kx * (height/2+1) + ky] for kx in [0, width/2], ky in [0, height/2]; count must be
