@@ -58,6 +58,18 @@ struct TcShape {
 };
 
 // ------------------------------------------------------------------ operand stores
+// BF16x3 split of two values at once: hi = bf16(v) and lo = bf16(v - hi) for a and b, packed as
+// bf16x2 (a in the low half).  One paired conversion for both his, one f32x2 subtract for both
+// (exact) residuals, one paired conversion for both los: the same bits as the per-value split.
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const float2 r = lfft::f2sub(make_float2(a, b), hf);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(r.x, r.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
 template <bool X3>
 __device__ __forceinline__ void store_elem(uint8_t* op, int opnd_bytes, int r, int k, int K, float v) {
     if (X3) {
@@ -77,13 +89,7 @@ __device__ __forceinline__ void store_chunk(uint8_t* op, int opnd_bytes, int r, 
     if (X3) {
         uint32_t hi[4], lo[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
-            const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
-            const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
-            hi[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-            lo[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-        }
+        for (int i = 0; i < 4; i++) split_bf16x2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
         const uint32_t off = kmajor_offset(r, k0, K, 2);
         *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
         *reinterpret_cast<uint4*>(op + opnd_bytes + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);

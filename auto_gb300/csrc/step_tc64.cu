@@ -45,6 +45,16 @@ struct Tc64 {
     static_assert(SMEM <= 232448, "shared memory");
 };
 
+// BF16x3 split of two values at once (see step_tc.cu): the same bits as the per-value split.
+__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    const float2 hf = __bfloat1622float2(h);
+    const float2 r = lfft::f2sub(make_float2(a, b), hf);
+    const __nv_bfloat162 l = __floats2bfloat162_rn(r.x, r.y);
+    hi = *reinterpret_cast<const uint32_t*>(&h);
+    lo = *reinterpret_cast<const uint32_t*>(&l);
+}
+
 template <bool X3>
 __device__ __forceinline__ void store16(uint8_t* op, int r, int k0, const float* v) {
     // 16 bytes of K starting at k0 (8 bf16 hi and lo, or 4 tf32), row r of a 128 x 128 operand
@@ -52,13 +62,7 @@ __device__ __forceinline__ void store16(uint8_t* op, int r, int k0, const float*
     if (X3) {
         uint32_t hi[4], lo[4];
 #pragma unroll
-        for (int i = 0; i < 4; i++) {
-            const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * i]), h1 = __float2bfloat16_rn(v[2 * i + 1]);
-            const __nv_bfloat16 l0 = __float2bfloat16_rn(v[2 * i] - __bfloat162float(h0));
-            const __nv_bfloat16 l1 = __float2bfloat16_rn(v[2 * i + 1] - __bfloat162float(h1));
-            hi[i] = (uint32_t)__bfloat16_as_ushort(h0) | ((uint32_t)__bfloat16_as_ushort(h1) << 16);
-            lo[i] = (uint32_t)__bfloat16_as_ushort(l0) | ((uint32_t)__bfloat16_as_ushort(l1) << 16);
-        }
+        for (int i = 0; i < 4; i++) split_bf16x2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
         const uint32_t off = kmajor_offset(r, k0, 128, 2);
         *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
         *reinterpret_cast<uint4*>(op + OP + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
@@ -132,13 +136,19 @@ __global__ void __launch_bounds__(256, 1)
     // Both hand-overs that need a twiddle (A -> B and C -> D) use exp(-2 pi i f j / 4096) with
     // f = t >> 1 fixed per thread and j in [0, 64) the column index: with j = 8a + b it is
     // P8[a] * P1[b], two exactly rounded table values and one product.
+    // A thread whose lane holds the real part keeps both tables conjugated: the product is then
+    // conj(w), and the hand-over's output is v * w.x + p * w.y on either lane (v its own
+    // component, p the neighbour's), with no per-element select.
     float2 P8[8], P1[8];
     {
         const int fidx = t >> 1;
+        const float sgn = (t & 1) ? 1.0f : -1.0f;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
             P1[i] = tw[((fidx * i) & 4095) * (lfft::TWN / 4096)];
             P8[i] = tw[((fidx * 8 * i) & 4095) * (lfft::TWN / 4096)];
+            P1[i].y *= sgn;
+            P8[i].y *= sgn;
         }
     }
     bool ok = mbar_wait(bar_f, 0);
@@ -213,9 +223,8 @@ __global__ void __launch_bounds__(256, 1)
 #pragma unroll
                 for (int j = 0; j < 32; j++) {
                     const float p = __shfl_xor_sync(0xffffffffu, v[j], 1);
-                    const float re = ro ? p : v[j], im = ro ? v[j] : p;
                     const float2 w = lfft::cmul(P8[(ybase + j) >> 3], P1[(ybase + j) & 7]);
-                    o[j] = ro ? (re * w.y + im * w.x) : (re * w.x - im * w.y);
+                    o[j] = fmaf(p, w.y, v[j] * w.x);
                 }
                 store32<X3>(op, c * 64 + k2, ro * 64 + ybase, o);
             }
@@ -264,9 +273,8 @@ __global__ void __launch_bounds__(256, 1)
 #pragma unroll
                     for (int j = 0; j < 32; j++) {
                         const float p = __shfl_xor_sync(0xffffffffu, v[j], 1);
-                        const float re = ro ? p : v[j], im = ro ? v[j] : p;
                         const float2 w = lfft::cmul(P8[(kbase + j) >> 3], P1[(kbase + j) & 7]);
-                        o[j] = ro ? (re * w.y + im * w.x) : (re * w.x - im * w.y);
+                        o[j] = fmaf(p, w.y, v[j] * w.x);
                     }
                     store32<X3>(op, c * 64 + y1, ro * 64 + kbase, o);
                 }
