@@ -57,7 +57,11 @@ struct LeniaCtx {
     std::string err;
     int device = 0;
     int path = 0;
+    int sms = 0;
     cudaStream_t stream = nullptr;
+    // the tensor-core paths run a class's few FP32 column items beside the tensor-core launch
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::vector<LeniaWorldDesc> desc;
     std::vector<DevWorld> hw;
     DevWorld* d_worlds = nullptr;
@@ -329,9 +333,22 @@ int flush_spectra(LeniaCtx* ctx) {
 // The column pass of one class (or one world's slice of it).
 bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int ncol, const ColItem* tcg, int ntcg,
                     int variant, cudaStream_t s) {
-    bool ok = true;
-    if (ntcg > 0) ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
-    return ok && launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
+    if (ntcg <= 0) return launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
+    // Tensor-core paths: the FP32 items (each channel's first tile group, which holds the packed
+    // DC/Nyquist column) are few.  After the tensor-core launch they ran on an otherwise idle GPU
+    // (a 4096-point column item takes about as long as a quarter of the whole tensor-core launch),
+    // so they run beside it on a side stream, on SMs the persistent tensor-core grid leaves free.
+    const int reserve = (ncol + 1) / 2;
+    if (ncol <= 0 || reserve > ctx->sms / 16) {
+        const bool ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
+        return ok && launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
+    }
+    if (cudaEventRecord(ctx->ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0) != cudaSuccess)
+        return false;
+    bool ok = launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, ctx->side);
+    ok = ok && cudaEventRecord(ctx->ev_join, ctx->side) == cudaSuccess;
+    ok = ok && launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s, reserve);
+    return ok && cudaStreamWaitEvent(s, ctx->ev_join, 0) == cudaSuccess;
 }
 
 // Enqueue `steps` steps of every world on the context's streams (captured into graphs).
@@ -688,7 +705,11 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         g_create_error = msg;
         return code;
     };
-    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess) {
         fail(ctx, LENIA_ECUDA, "stream creation failed");
         return bail(LENIA_ECUDA);
     }
@@ -739,6 +760,9 @@ int lenia_destroy(LeniaCtx* ctx) {
     if (ctx->graph_one) cudaGraphExecDestroy(ctx->graph_one);
     tc_release(ctx->tc);
     for (void* p : ctx->allocs) cudaFree(p);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return 0;

@@ -411,7 +411,7 @@ const ShapeInfo* shape_for(int H) {
 
 template <class S>
 bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups, int ngroups, const float2* tw,
-                  int* err, cudaStream_t st) {
+                  int* err, cudaStream_t st, int reserve_sms) {
     static int attr = 0;
     if (!attr) {
         if (cudaFuncSetAttribute(col_pass_tc<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess)
@@ -426,8 +426,9 @@ bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups,
         return false;
     // TMEM: co-resident CTAs must fit in 512 columns
     if (per_sm * S::TCOLS > 512) per_sm = 512 / S::TCOLS;
-    int grid = sms * per_sm;
+    int grid = (sms - reserve_sms) * per_sm;
     if (grid > ngroups) grid = ngroups;
+    if (grid < 1) grid = 1;
     col_pass_tc<S><<<grid, 128, S::SMEM, st>>>(worlds, groups, ngroups, (const uint8_t*)fm, tw, err);
     return true;
 }
@@ -482,7 +483,7 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
 bool tc_supports(int H) { return shape_for(H) != nullptr; }
 
 bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
-                   const float2* tw, cudaStream_t s) {
+                   const float2* tw, cudaStream_t s, int reserve_sms) {
     const void* fm = nullptr;
     for (int i = 0; i < plan.nsizes; i++)
         if (plan.sizes[i] == H) fm = plan.mats[i];
@@ -490,15 +491,15 @@ bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, 
     const bool x3 = path == LENIA_PATH_BF16X3;
     int* e = (int*)plan.d_err;
     switch (H) {
-    case 4096: return launch_col_tc64(x3, fm, worlds, groups, ngroups, tw, e, s);
-    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s)
-                         : launch_shape<TcShape<64, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s);
-    case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s)
-                         : launch_shape<TcShape<32, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s);
-    case 512: return x3 ? launch_shape<TcShape<32, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s)
-                        : launch_shape<TcShape<32, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s);
-    case 256: return x3 ? launch_shape<TcShape<16, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s)
-                        : launch_shape<TcShape<16, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s);
+    case 4096: return launch_col_tc64(x3, fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                         : launch_shape<TcShape<64, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                         : launch_shape<TcShape<32, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 512: return x3 ? launch_shape<TcShape<32, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                        : launch_shape<TcShape<32, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 256: return x3 ? launch_shape<TcShape<16, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                        : launch_shape<TcShape<16, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
     }
     return false;
 }

@@ -26,12 +26,13 @@ int tc_columns_per_group(int H);
 int tc_setup(TcPlan& plan, int path, std::string* err);
 int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err);
 // groups: (world, channel, first tile) items, each covering tc_columns_per_group(H) columns.
+// reserve_sms: SMs the persistent grid leaves free for a launch that runs beside it.
 bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
-                   const float2* tw, cudaStream_t s);
+                   const float2* tw, cudaStream_t s, int reserve_sms = 0);
 int tc_check_error(TcPlan& plan, std::string* err);
 // The 4096-point column pass with two pipelines per SM (step_tc64.cu); fmat = the 64-point DFT matrix.
 bool launch_col_tc64(bool x3, const void* fmat, const DevWorld* worlds, const ColItem* groups, int ngroups,
-                     const float2* tw, int* err, cudaStream_t s);
+                     const float2* tw, int* err, cudaStream_t s, int reserve_sms = 0);
 void tc_release(TcPlan& plan);
 // One GEMM through the same operand layouts and descriptors (diagnostic).
 int tc_selftest(int path, int n, int k, const float* a, const float* b, float* d, std::string* err);

@@ -317,7 +317,7 @@ __global__ void __launch_bounds__(256, 1)
 }
 
 bool launch_col_tc64(bool x3, const void* fmat, const DevWorld* worlds, const ColItem* groups, int ngroups,
-                     const float2* tw, int* err, cudaStream_t s) {
+                     const float2* tw, int* err, cudaStream_t s, int reserve_sms) {
     static int attr[2] = {0, 0};
     const int smem = x3 ? Tc64<true>::SMEM : Tc64<false>::SMEM;
     if (!attr[x3]) {
@@ -331,7 +331,8 @@ bool launch_col_tc64(bool x3, const void* fmat, const DevWorld* worlds, const Co
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     int grid = (ngroups + 1) / 2;
-    if (grid > sms) grid = sms;
+    if (grid > sms - reserve_sms) grid = sms - reserve_sms;
+    if (grid < 1) grid = 1;
     if (x3) col_pass_tc64<true><<<grid, 256, smem, s>>>(worlds, groups, ngroups, (const uint8_t*)fmat, tw, err);
     else col_pass_tc64<false><<<grid, 256, smem, s>>>(worlds, groups, ngroups, (const uint8_t*)fmat, tw, err);
     return true;
