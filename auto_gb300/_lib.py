@@ -20,7 +20,7 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "l
 # Every function the header declares, for the export check.
 EXPORTS = [
     "lenia_last_error", "lenia_create", "lenia_destroy", "lenia_write_state", "lenia_read_state",
-    "lenia_write_state_device", "lenia_read_state_device", "lenia_write_states", "lenia_read_states", "lenia_step", "lenia_step_timed", "lenia_sync",
+    "lenia_write_state_device", "lenia_read_state_device", "lenia_write_states", "lenia_read_states", "lenia_write_states_async", "lenia_read_states_async", "lenia_step", "lenia_step_timed", "lenia_sync",
     "lenia_tick", "lenia_seed_tiles", "lenia_seed_patches", "lenia_cells_per_step", "lenia_memory_bytes",
     "lenia_read_field_u", "lenia_read_spectrum", "lenia_world_stats", "lenia_autotune", "lenia_set_variants", "lenia_profile_step",
     "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_step_noalloc",
@@ -71,7 +71,9 @@ def _declare(L):
         "lenia_write_state_device": [vp, i32, vp, sz],
         "lenia_read_state_device": [vp, i32, vp, sz],
         "lenia_write_states": [vp, _c_float_p, sz],
+        "lenia_write_states_async": [vp, _c_float_p, sz],
         "lenia_read_states": [vp, _c_float_p, sz],
+        "lenia_read_states_async": [vp, _c_float_p, sz],
         "lenia_step": [vp, u32],
         "lenia_step_timed": [vp, u32, _c_float_p],
         "lenia_sync": [vp],

@@ -62,6 +62,14 @@ struct LeniaCtx {
     // the tensor-core paths run a class's few FP32 column items beside the tensor-core launch
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // asynchronous state copies (lenia_write_states_async / lenia_read_states_async): uploads on
+    // `up`, downloads on `down`, through device staging buffers, so that they overlap the
+    // generations on `stream` (one copy stream would queue the next upload behind the last
+    // download, which waits for the last step)
+    cudaStream_t up = nullptr, down = nullptr;
+    float* stage_in = nullptr;
+    float* stage_out = nullptr;
+    cudaEvent_t ev_in_ready = nullptr, ev_in_free = nullptr, ev_out_ready = nullptr, ev_out_free = nullptr;
     std::vector<LeniaWorldDesc> desc;
     std::vector<DevWorld> hw;
     DevWorld* d_worlds = nullptr;
@@ -709,6 +717,12 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->down, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_in_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_in_free, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_out_ready, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_out_free, cudaEventDisableTiming) != cudaSuccess ||
         cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess) {
         fail(ctx, LENIA_ECUDA, "stream creation failed");
         return bail(LENIA_ECUDA);
@@ -756,10 +770,16 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
 int lenia_destroy(LeniaCtx* ctx) {
     if (!ctx) return 0;
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->up) cudaStreamSynchronize(ctx->up);
+    if (ctx->down) cudaStreamSynchronize(ctx->down);
     if (ctx->graph_big) cudaGraphExecDestroy(ctx->graph_big);
     if (ctx->graph_one) cudaGraphExecDestroy(ctx->graph_one);
     tc_release(ctx->tc);
     for (void* p : ctx->allocs) cudaFree(p);
+    for (cudaEvent_t e : {ctx->ev_in_ready, ctx->ev_in_free, ctx->ev_out_ready, ctx->ev_out_free})
+        if (e) cudaEventDestroy(e);
+    if (ctx->up) cudaStreamDestroy(ctx->up);
+    if (ctx->down) cudaStreamDestroy(ctx->down);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->side) cudaStreamDestroy(ctx->side);
@@ -841,6 +861,49 @@ int lenia_read_states(LeniaCtx* ctx, float* host, size_t count) {
     return tc_check_error(ctx->tc, &ctx->err);
 }
 
+// Asynchronous whole-context state copies.  The host copy runs on the upload (download) stream
+// into (out of) a device staging buffer; the compute stream moves the staging buffer into (or out of) the
+// states with one device-to-device copy, in stream order with the steps.  So the upload of the
+// next input and the download of the last result overlap the generations in between.
+static int states_async_check(LeniaCtx* ctx, const void* host, size_t count) {
+    size_t total = 0;
+    for (const auto& d : ctx->desc) total += state_count(d);
+    if (!host || count != total) return fail(ctx, LENIA_EINVAL, "the worlds hold %zu state values, got %zu", total, count);
+    if (!ctx->states) return fail(ctx, LENIA_EINVAL, "asynchronous state copies need the fused paths' state arena");
+    return 0;
+}
+
+int lenia_write_states_async(LeniaCtx* ctx, const float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    int rc = states_async_check(ctx, host, count);
+    if (rc) return rc;
+    if (!ctx->stage_in && (rc = dalloc(ctx, &ctx->stage_in, count))) return rc;
+    const size_t bytes = count * sizeof(float);
+    CK(cudaStreamWaitEvent(ctx->up, ctx->ev_in_free, 0));  // the previous input has left the buffer
+    CK(cudaMemcpyAsync(ctx->stage_in, host, bytes, cudaMemcpyHostToDevice, ctx->up));
+    CK(cudaEventRecord(ctx->ev_in_ready, ctx->up));
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in_ready, 0));
+    CK(cudaMemcpyAsync(ctx->states, ctx->stage_in, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->ev_in_free, ctx->stream));
+    for (size_t w = 0; w < ctx->desc.size(); w++) refresh_spectrum(ctx, (int)w);
+    return 0;
+}
+
+int lenia_read_states_async(LeniaCtx* ctx, float* host, size_t count) {
+    if (!ctx) return LENIA_EINVAL;
+    int rc = states_async_check(ctx, host, count);
+    if (rc) return rc;
+    if (!ctx->stage_out && (rc = dalloc(ctx, &ctx->stage_out, count))) return rc;
+    const size_t bytes = count * sizeof(float);
+    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_out_free, 0));  // the previous result has left the buffer
+    CK(cudaMemcpyAsync(ctx->stage_out, ctx->states, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaEventRecord(ctx->ev_out_ready, ctx->stream));
+    CK(cudaStreamWaitEvent(ctx->down, ctx->ev_out_ready, 0));
+    CK(cudaMemcpyAsync(host, ctx->stage_out, bytes, cudaMemcpyDeviceToHost, ctx->down));
+    CK(cudaEventRecord(ctx->ev_out_free, ctx->down));
+    return 0;
+}
+
 int lenia_step(LeniaCtx* ctx, uint32_t steps) {
     if (!ctx) return LENIA_EINVAL;
     int frc = flush_spectra(ctx);
@@ -871,6 +934,8 @@ int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms) {
 int lenia_sync(LeniaCtx* ctx) {
     if (!ctx) return LENIA_EINVAL;
     CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaStreamSynchronize(ctx->up));
+    CK(cudaStreamSynchronize(ctx->down));
     int rc = tc_check_error(ctx->tc, &ctx->err);
     return rc;
 }

@@ -117,6 +117,20 @@ class Sim:
         self._check(self._L.lenia_write_states(self._ctx, fptr(a), a.size))
         self.wait()
 
+    def write_states_async(self, states: np.ndarray):
+        """write_states without blocking: `states` (contiguous float32, page-locked for the copy to
+        overlap the steps) must stay untouched until wait()."""
+        if states.dtype != np.float32 or not states.flags.c_contiguous:
+            raise ValueError("write_states_async needs a contiguous float32 array that outlives the copy")
+        self._check(self._L.lenia_write_states_async(self._ctx, fptr(states), states.size))
+
+    def read_states_async(self, out: np.ndarray):
+        """read_states without blocking into `out` (contiguous float32, page-locked for the copy to
+        overlap the steps), complete after wait()."""
+        if out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise ValueError("read_states_async needs a contiguous float32 array")
+        self._check(self._L.lenia_read_states_async(self._ctx, fptr(out), out.size))
+
     def write_state(self, world: int, state: np.ndarray):
         a = np.ascontiguousarray(state, np.float32).ravel()
         self._check(self._L.lenia_write_state(self._ctx, world, fptr(a), a.size))

@@ -8,8 +8,10 @@ Printed JSON (one line, rank 0):
   value   cell-updates/s with the state resident in HBM, from CUDA events on the engine stream
           around the K timed bench steps, max over ranks
   e2e     the same metric through the public C ABI with host buffers: every bench step writes
-          every world's state from one pinned host buffer (lenia_write_states), runs G generations
-          and reads every state back (lenia_read_states)
+          every world's state from a pinned host buffer (lenia_write_states_async), runs G
+          generations and reads every state back into another (lenia_read_states_async); the
+          copies overlap the neighbouring steps' generations.  blocking_value: the same with the
+          blocking calls (lenia_write_states / lenia_read_states)
   roofline  12 algorithmic bytes per cell-update (state read and written, one complex f32
           half-spectrum value) over the event-timed generation time, against the measured HBM
           copy bandwidth; traffic = DRAM bytes per generation from an ncu capture
@@ -388,25 +390,43 @@ def run_ours(args, dist):
     e2e = None
     if not args.no_e2e:
         import torch
-        # every world's state in one pinned host buffer, world after world
-        pinned = torch.empty(sum(w.channels * w.height * w.width for w in worlds), dtype=torch.float32,
-                             pin_memory=True)
-        a = pinned.numpy()
-        sim.read_states(a)
+        # every world's state in pinned host buffers, world after world: the steps' input and result
+        n = sum(w.channels * w.height * w.width for w in worlds)
+        a_in = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+        a_out = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+        sim.read_states(a_in)
         L = sim._L
         from auto_gb300._lib import check, fptr
+        # Every bench step uploads every state, runs G generations and downloads every state,
+        # through the public C ABI.  Streamed: the copies run on the engine's copy stream and
+        # overlap the generations of the neighbouring steps.
+        sim.write_states_async(a_in)  # staging buffers allocated outside the timed region
+        sim.read_states_async(a_out)
+        sim.wait()
         device_sync()
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            check(L.lenia_write_states(sim._ctx, fptr(a), a.size), sim._ctx)
+            check(L.lenia_write_states_async(sim._ctx, fptr(a_in), a_in.size), sim._ctx)
             check(L.lenia_step(sim._ctx, G), sim._ctx)
-            check(L.lenia_read_states(sim._ctx, fptr(a), a.size), sim._ctx)
+            check(L.lenia_read_states_async(sim._ctx, fptr(a_out), a_out.size), sim._ctx)
+        sim.wait()
         device_sync()
         t_e2e = dist.max(time.perf_counter() - t0)
-        nbytes = a.nbytes
-        e2e = {"value": total_cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": nbytes,
-               "d2h_bytes_per_step": nbytes, "gens_per_step": G}
+        # the same with blocking copies, each step waiting for its own download
+        device_sync()
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            check(L.lenia_write_states(sim._ctx, fptr(a_in), a_in.size), sim._ctx)
+            check(L.lenia_step(sim._ctx, G), sim._ctx)
+            check(L.lenia_read_states(sim._ctx, fptr(a_out), a_out.size), sim._ctx)
+        device_sync()
+        t_block = dist.max(time.perf_counter() - t0)
+        e2e = {"value": total_cells * G * args.steps / t_e2e, "unit": UNIT, "h2d_bytes_per_step": a_in.nbytes,
+               "d2h_bytes_per_step": a_out.nbytes, "gens_per_step": G,
+               "copies": "streamed: lenia_write_states_async / lenia_read_states_async overlap the steps",
+               "blocking_value": total_cells * G * args.steps / t_block}
 
     # every step path on the same workload, side by side (event-timed, state resident)
     paths = {}

@@ -110,6 +110,15 @@ LENIA_API int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, 
  * one world per Sim, so its nearest equivalent is a loop of write_field / read_field calls. */
 LENIA_API int lenia_write_states(LeniaCtx* ctx, const float* host, size_t count);
 LENIA_API int lenia_read_states(LeniaCtx* ctx, float* host, size_t count);
+/* The same two copies without blocking, for streaming batches of worlds through the engine:
+ * the host copies run on two more streams through device staging buffers, so the upload of the
+ * next input and the download of the last result overlap the steps in between.  Both are
+ * stream-ordered with lenia_step (a write takes effect before the next step; a read returns the
+ * states after every step enqueued before it).  The host buffer must stay valid and untouched
+ * until lenia_sync returns; page-locked host memory is needed for the copies to overlap.  Fused
+ * paths only (LENIA_EINVAL on the radix-2 path). */
+LENIA_API int lenia_write_states_async(LeniaCtx* ctx, const float* host, size_t count);
+LENIA_API int lenia_read_states_async(LeniaCtx* ctx, float* host, size_t count);
 
 /* Sim::step (sim.rs:297-309): advance every world by `steps`, asynchronously.  Steps are
  * replayed from CUDA graphs of up to 64 steps each. */

@@ -237,6 +237,41 @@ def test_every_side_on_both_axes_teacher_forced_vs_fp64(nk, tune):
             assert err < 1e-4, (w.width, w.height, err)
 
 
+def test_async_state_copies_match_blocking_ones():
+    """lenia_write_states_async / lenia_read_states_async, with two downloads in flight and an
+    upload between steps, give the same bits as the blocking calls in the same order."""
+    worlds = configs.batched(24)
+    rng = np.random.default_rng(8)
+    flat = np.concatenate([rng.random(w.channels * w.height * w.width, dtype=np.float32) for w in worlds])
+    flat2 = flat[::-1].copy()
+    outs = [np.empty_like(flat) for _ in range(3)]
+    with Sim(worlds, seed=0) as a, Sim(worlds, seed=0) as b:
+        a.write_states_async(flat)
+        a.step(2)
+        a.read_states_async(outs[0])
+        a.step(3)
+        a.read_states_async(outs[1])
+        a.write_states_async(flat2)
+        a.step(1)
+        a.read_states_async(outs[2])
+        a.wait()
+        b.write_states(flat)
+        b.step(2)
+        want = [b.read_states().copy()]
+        b.step(3)
+        want.append(b.read_states().copy())
+        b.write_states(flat2)
+        b.step(1)
+        want.append(b.read_states().copy())
+        for got, w in zip(outs, want):
+            assert np.array_equal(got, w)
+        with pytest.raises(LeniaError):
+            a.read_states_async(np.empty(flat.size + 1, np.float32))
+    with Sim(configs.single_256(), path="radix2") as r:
+        with pytest.raises(LeniaError):
+            r.write_states_async(np.zeros(256 * 256, np.float32))
+
+
 @pytest.mark.parametrize("nk", [1, 2])
 def test_every_launch_variant_on_every_side(nk):
     """Each pinned pair of launch variants (column: scalar at 64 and 128 registers, paired; row:
