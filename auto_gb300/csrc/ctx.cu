@@ -1187,6 +1187,21 @@ int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const 
     return 0;
 }
 
+int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses) {
+    if (!ctx || !nclasses) return LENIA_EINVAL;
+    *nclasses = ctx->classes.size();
+    if (!out) return 0;
+    if (count < 4 * ctx->classes.size()) return LENIA_EINVAL;
+    for (size_t i = 0; i < ctx->classes.size(); i++) {
+        const auto& cl = ctx->classes[i];
+        out[4 * i] = cl.W;
+        out[4 * i + 1] = cl.H;
+        out[4 * i + 2] = cl.var_col;
+        out[4 * i + 3] = cl.var_row;
+    }
+    return 0;
+}
+
 int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) {
     if (!ctx) return LENIA_EINVAL;
     if (col_variant < -1 || col_variant > 2 || row_variant < -1 || row_variant > 1)

@@ -288,17 +288,21 @@ FFT_CHD constexpr int tw_table_size(int n, int maxr = 16) { return stage_tw_offs
 // a tw2 table holds each twiddle in both halves, for paired sequences.
 FFT_HD void set_twiddle(float2& d, float2 w) { d = w; }
 FFT_HD void set_twiddle(tw2& d, float2 w) { d = splat(w); }
-template <int N, class W>
+// One stage per template instance, so that each stage's L, R and table offset are compile-time
+// constants (a runtime loop over the stages would evaluate the plan in every thread).
+template <int N, class W, int I = 0>
 FFT_HD void fill_stage_twiddles(W* stw, const float2* tw, int tid, int nth) {
     constexpr int MR = max_radix<W>();
-    for (int i = 0; i < plan_len(N, MR); i++) {
-        const int L = plan_L(N, i, MR), R = plan_radix(N, i, MR), off = stage_tw_offset(N, i, MR);
-        if (L == 1) continue;
-        const int step = TWN / (L * R);
-        for (int k = tid; k < L; k += nth) {
-            set_twiddle(stw[off + k], tw[k * step]);
-            if (R >= 8) set_twiddle(stw[off + L + k], tw[4 * k * step]);
+    if constexpr (I < plan_len(N, MR)) {
+        constexpr int L = plan_L(N, I, MR), R = plan_radix(N, I, MR), off = stage_tw_offset(N, I, MR);
+        if constexpr (L > 1) {
+            constexpr int step = TWN / (L * R);
+            for (int k = tid; k < L; k += nth) {
+                set_twiddle(stw[off + k], tw[k * step]);
+                if (R >= 8) set_twiddle(stw[off + L + k], tw[4 * k * step]);
+            }
         }
+        fill_stage_twiddles<N, W, I + 1>(stw, tw, tid, nth);
     }
 }
 

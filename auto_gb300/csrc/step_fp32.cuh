@@ -143,7 +143,8 @@ template <int H>
 constexpr size_t col_khat_bytes() { return fusable<H>() ? (size_t)TC * khat_cols_stride<H>() * sizeof(float) : 0; }
 template <int H>
 __device__ __forceinline__ float* col_khat_smem(float2* stw) {
-    return reinterpret_cast<float*>(((uintptr_t)(stw + tw_table_size(H)) + 15) & ~(uintptr_t)15);
+    constexpr int TWS = tw_table_size(H);
+    return reinterpret_cast<float*>(((uintptr_t)(stw + TWS) + 15) & ~(uintptr_t)15);
 }
 
 __device__ __forceinline__ float clamp01(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
@@ -224,7 +225,8 @@ constexpr int row_minb() {
 // the general path.
 template <int W>
 __device__ __forceinline__ float* row_extra_smem(float2* stw) {
-    return reinterpret_cast<float*>(((uintptr_t)(stw + tw_table_size(W)) + 15) & ~(uintptr_t)15);
+    constexpr int TWS = tw_table_size(W);
+    return reinterpret_cast<float*>(((uintptr_t)(stw + TWS) + 15) & ~(uintptr_t)15);
 }
 
 // Half-spectra of rows r0..r0+2S-1 (tile layout) -> S packed complex sequences
@@ -642,7 +644,8 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
 constexpr int PMR = max_radix<cpair>();  // largest radix of the paired builds' plans
 template <int H>
 __device__ __forceinline__ float* col_khat_smem_pair(tw2* stw) {
-    return reinterpret_cast<float*>(stw + tw_table_size(H, PMR) + 1);
+    constexpr int TWS = tw_table_size(H, PMR);
+    return reinterpret_cast<float*>(stw + TWS + 1);
 }
 
 template <int H, int NT>

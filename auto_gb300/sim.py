@@ -190,6 +190,14 @@ class Sim:
     def autotune(self):
         self._check(self._L.lenia_autotune(self._ctx))
 
+    def variants(self):
+        """{(width, height): (column variant, row variant)} for every size class."""
+        n = ctypes.c_size_t(0)
+        self._check(self._L.lenia_class_variants(self._ctx, None, 0, ctypes.byref(n)))
+        out = (ctypes.c_int32 * (4 * n.value))()
+        self._check(self._L.lenia_class_variants(self._ctx, out, 4 * n.value, ctypes.byref(n)))
+        return {(out[4 * i], out[4 * i + 1]): (out[4 * i + 2], out[4 * i + 3]) for i in range(n.value)}
+
     def set_variants(self, column: int = -1, row: int = -1):
         """Pin every size class's launch variants (see lenia_set_variants); -1 keeps one."""
         self._check(self._L.lenia_set_variants(self._ctx, int(column), int(row)))

@@ -331,7 +331,9 @@ def run_ours(args, dist):
     sim = Sim(worlds, seed=0, path=args.path)
     seed_all(sim, worlds, seeds)
     if not args.no_autotune:
-        sim.autotune()  # the engine's autotuner: times both launch variants per size class
+        sim.autotune()  # the engine's autotuner: times every launch variant per size class
+    # launch variant per size class (column: 0/1 scalar at 64/128 registers, 2 paired; row: 0/1)
+    variants = {"%dx%d" % wh: {"column": v[0], "row": v[1]} for wh, v in sim.variants().items()}
     G = args.gens
     cells = sim.cells_per_step
     for _ in range(args.warmup):
@@ -491,6 +493,7 @@ def run_ours(args, dist):
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches_per_gen * G * args.steps,
+               "launch_variants": variants,
                "paths": paths,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
         print(json.dumps(out))

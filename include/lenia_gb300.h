@@ -185,6 +185,9 @@ LENIA_API int lenia_autotune(LeniaCtx* ctx);
  * pass's current choice.  Results do not depend on the variant beyond float rounding.  Rebuilds
  * the step graphs.  No reference counterpart: the reference has one launch shape per pass. */
 LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant);
+/* The size classes and their current launch variants: *nclasses = the number of classes; with
+ * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
+LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
 
 /* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
  * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.

@@ -285,6 +285,7 @@ def test_every_launch_variant_on_every_side(nk):
         for col in (0, 1, 2):
             for row in (0, 1):
                 sim.set_variants(col, row)
+                assert set(sim.variants().values()) == {(col, row)}
                 for i, s in enumerate(states):
                     sim.write_state(i, s)
                 sim.step(1)
