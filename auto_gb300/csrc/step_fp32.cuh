@@ -250,6 +250,13 @@ __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __re
             B[i] = hint::ld2(src + TC, keep);
         }
     }
+    // When every iteration moves kx by the same multiple of 16 (D), the padded positions of kx and
+    // W - kx move by D + D/16: two base pointers and compile-time offsets.
+    constexpr int D = NT / S;
+    constexpr bool STEP = NT % (S * TC) == 0 && D % 16 == 0;
+    const int kx0 = TC * (threadIdx.x / (S * TC)) + threadIdx.x % TC, p0 = (threadIdx.x / TC) % S;
+    float2* za = Z + p0 * SEQ + pad(kx0);
+    float2* zb = Z + p0 * SEQ + pad(W - kx0);
 #pragma unroll
     for (int i = 0; i < IT; i++) {
         const int e = threadIdx.x + i * NT;
@@ -259,6 +266,9 @@ __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __re
             if (kx == 0) {
                 z[pad(0)] = make_float2(A[i].x, B[i].x);
                 z[pad(W / 2)] = make_float2(A[i].y, B[i].y);
+            } else if constexpr (STEP) {
+                za[i * (D + D / 16)] = make_float2(A[i].x - B[i].y, A[i].y + B[i].x);
+                zb[-i * (D + D / 16)] = make_float2(A[i].x + B[i].y, B[i].x - A[i].y);
             } else {
                 z[pad(kx)] = make_float2(A[i].x - B[i].y, A[i].y + B[i].x);
                 z[pad(W - kx)] = make_float2(A[i].x + B[i].y, B[i].x - A[i].y);
@@ -272,7 +282,13 @@ template <int W, int S, int NT>
 __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __restrict__ sp, int H, int r0) {
     constexpr int SEQ = seq_stride(W);
     constexpr int E = W / 2 * S;
-    for (int e = threadIdx.x; e < E; e += NT) {
+    // as in load_rows_spectrum: the padded positions of kx and W - kx move by a constant
+    constexpr int D = NT / S;
+    constexpr bool STEP = NT % (S * TC) == 0 && D % 16 == 0;
+    const int kx0 = TC * (threadIdx.x / (S * TC)) + threadIdx.x % TC, p0 = (threadIdx.x / TC) % S;
+    const float2* za = Z + p0 * SEQ + pad(kx0);
+    const float2* zb = Z + p0 * SEQ + pad(W - kx0);
+    for (int e = threadIdx.x; e < E; e += NT, za += STEP ? D + D / 16 : 0, zb -= STEP ? D + D / 16 : 0) {
         const int t = e / (S * TC), p = (e / TC) % S, c = e % TC, kx = TC * t + c;
         const float2* z = Z + p * SEQ;
         float2 A, B;
@@ -281,7 +297,7 @@ __device__ __forceinline__ void store_rows_spectrum(const float2* Z, float2* __r
             A = make_float2(z0.x, zn.x);
             B = make_float2(z0.y, zn.y);
         } else {
-            const float2 a = z[pad(kx)], b = z[pad(W - kx)];
+            const float2 a = STEP ? *za : z[pad(kx)], b = STEP ? *zb : z[pad(W - kx)];
             A = make_float2(0.5f * (a.x + b.x), 0.5f * (a.y - b.y));
             B = make_float2(0.5f * (a.y + b.y), -0.5f * (a.x - b.x));
         }
@@ -556,12 +572,15 @@ __device__ __forceinline__ void load_tile(float2* X, const float2* __restrict__ 
         const int y = threadIdx.x + i * NT;
         if (IT * NT == H || y < H) v[i] = hint::ld4(s4 + y, hint::policy_keep());
     }
+    // pad(tid + i NT) = pad(tid) + i (NT + NT / 16) when NT is a multiple of 16
+    float2* x0 = X + pad(threadIdx.x);
 #pragma unroll
     for (int i = 0; i < IT; i++) {
         const int y = threadIdx.x + i * NT;
         if (IT * NT == H || y < H) {
-            X[pad(y)] = make_float2(v[i].x, v[i].y);
-            X[SEQ + pad(y)] = make_float2(v[i].z, v[i].w);
+            float2* x = NT % 16 == 0 ? x0 + i * (NT + NT / 16) : X + pad(y);
+            x[0] = make_float2(v[i].x, v[i].y);
+            x[SEQ] = make_float2(v[i].z, v[i].w);
         }
     }
 }
@@ -570,8 +589,10 @@ template <int H, int NT>
 __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__ dst) {
     constexpr int SEQ = seq_stride(H);
     float4* d4 = reinterpret_cast<float4*>(dst);
-    for (int y = threadIdx.x; y < H; y += NT) {
-        const float2 a = X[pad(y)], b = X[SEQ + pad(y)];
+    const float2* x = X + pad(threadIdx.x);
+    for (int y = threadIdx.x; y < H; y += NT, x += NT + NT / 16) {
+        if (NT % 16 != 0) x = X + pad(y);
+        const float2 a = x[0], b = x[SEQ];
         hint::st4(d4 + y, make_float4(a.x, a.y, b.x, b.y), hint::policy_keep());
     }
 }
@@ -658,18 +679,22 @@ __device__ __forceinline__ void load_tile_pair(cpair* X, const float2* __restric
         const int y = threadIdx.x + i * NT;
         if (IT * NT == H || y < H) v[i] = hint::ld4(s4 + y, hint::policy_keep());
     }
+    cpair* x0 = X + pad(threadIdx.x);
 #pragma unroll
     for (int i = 0; i < IT; i++) {
         const int y = threadIdx.x + i * NT;
-        if (IT * NT == H || y < H) X[pad(y)] = cpair{make_float2(v[i].x, v[i].z), make_float2(v[i].y, v[i].w)};
+        if (IT * NT == H || y < H)
+            (NT % 16 == 0 ? x0[i * (NT + NT / 16)] : X[pad(y)]) =
+                cpair{make_float2(v[i].x, v[i].z), make_float2(v[i].y, v[i].w)};
     }
 }
 
 template <int H, int NT>
 __device__ __forceinline__ void store_tile_pair(const cpair* X, float2* __restrict__ dst) {
     float4* d4 = reinterpret_cast<float4*>(dst);
-    for (int y = threadIdx.x; y < H; y += NT) {
-        const cpair a = X[pad(y)];
+    const cpair* x = X + pad(threadIdx.x);
+    for (int y = threadIdx.x; y < H; y += NT, x += NT + NT / 16) {
+        const cpair a = NT % 16 == 0 ? *x : X[pad(y)];
         hint::st4(d4 + y, make_float4(a.re.x, a.im.x, a.re.y, a.im.y), hint::policy_keep());
     }
 }
