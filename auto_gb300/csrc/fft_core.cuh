@@ -68,10 +68,10 @@ struct alignas(16) cpair {
 struct alignas(16) tw2 {
     float2 rr, ii;
 };
-// largest radix of a plan by element type (float2 scalar, cpair paired) and by twiddle type
+// Largest radix of a plan, by element (or twiddle) type: 16 for scalar and paired elements alike
+// (paired elements with radix-8 plans, 8 registers of data a thread instead of 16, measured 50%
+// slower at 4096: more stages, spills at 64 registers, bank conflicts of 16-byte elements).
 template <class T> FFT_CHD constexpr int max_radix() { return 16; }
-template <> FFT_CHD constexpr int max_radix<cpair>() { return 16; }
-template <> FFT_CHD constexpr int max_radix<tw2>() { return 16; }
 FFT_HD float2 f2(float v) { return make_float2(v, v); }
 FFT_HD float2 f2add(float2 a, float2 b) {
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
