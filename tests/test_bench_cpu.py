@@ -42,3 +42,22 @@ def test_algorithmic_bytes():
     assert bench.alg_bytes_per_gen([multi]) == (8.0 * 3 + 4.0 * 9) * 1024 * 1024  # 20 B per channel-cell
     ws = configs.batched(8)
     assert bench.alg_bytes_per_gen(ws) == sum(12.0 * w.width * w.height for w in ws)
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """Under torchrun (two gloo ranks here) rank 0 alone times the reference arm and prints its line;
+    the other rank exits 0 without work."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                          "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
+                          "--impl", "reference", "--config", "single_256", "--steps", "1", "--warmup", "0",
+                          "--gpus", "2"],
+                         cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, out.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
