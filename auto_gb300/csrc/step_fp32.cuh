@@ -14,6 +14,10 @@
 // so one step reads and writes the half-spectrum twice and the state once.  Two real rows
 // share one complex FFT (z = a + i b), and the real DC and Nyquist columns share spectrum
 // column 0, so the half-spectrum takes exactly W*H*4 bytes per channel.
+//
+// The column pass is built twice: scalar (col_pass: a thread runs a butterfly of one column) and
+// paired (col_pass_pair: a thread runs the same butterfly of both columns of the tile as f32x2
+// pairs, half the threads and instructions); launch variant 2 selects the paired build.
 #pragma once
 #include <cuda_runtime.h>
 
