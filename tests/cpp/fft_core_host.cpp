@@ -97,3 +97,11 @@ extern "C" int fft_host_pair(int n, int inverse, const float* a, const float* b,
     }
     return -1;
 }
+
+// The radix plan of length n with radix cap maxr: its radices into out (at most 14); returns the
+// number of stages.
+extern "C" int plan_host(int n, int maxr, int* out) {
+    const Plan p = make_plan(n, maxr);
+    for (int i = 0; i < p.len; i++) out[i] = p.r[i];
+    return p.len;
+}

@@ -50,3 +50,22 @@ def test_paired_sequences_match_numpy(fft_host, n, inverse):
         x64 = x.astype(np.complex128)
         want = np.fft.ifft(x64) * n if inverse else np.fft.fft(x64)
         assert np.abs(out - want).max() / np.abs(want).max() < 2e-7
+
+
+@pytest.mark.parametrize("maxr", [16, 8])
+def test_radix_plans(fft_host, maxr):
+    """Every plan multiplies out to its length, uses only built radices within the cap, and starts
+    and ends with the same radix (the chained transforms rely on it)."""
+    for n in SIZES:
+        out = (ctypes.c_int * 14)()
+        k = fft_host.plan_host(n, maxr, out)
+        r = list(out[:k])
+        assert int(np.prod(r)) == n, (n, r)
+        assert all(x in (2, 3, 4, 8, 16) and x <= maxr for x in r), (n, r)
+        if n >= 16:
+            assert k >= 2 and r[0] == r[-1], (n, r)
+    out = (ctypes.c_int * 14)()
+    k = fft_host.plan_host(4096, 16, out)
+    assert list(out[:k]) == [16, 16, 16]
+    k = fft_host.plan_host(3072, 16, out)
+    assert list(out[:k]) == [16, 3, 4, 16]
