@@ -1187,6 +1187,18 @@ int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const 
     return 0;
 }
 
+int lenia_tc_set_wait_limit(LeniaCtx* ctx, int32_t polls_plus_one) {
+    if (!ctx) return LENIA_EINVAL;
+    if (polls_plus_one < 0) return fail(ctx, LENIA_EINVAL, "polls_plus_one must be >= 0");
+    if (ctx->path != LENIA_PATH_TF32 && ctx->path != LENIA_PATH_BF16X3)
+        return fail(ctx, LENIA_ESTATE, "the context has no tensor-core path");
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::string err;
+    int rc = tc_set_wait_limit(ctx->tc, polls_plus_one, &err);
+    if (rc) return fail(ctx, rc, "%s", err.c_str());
+    return 0;
+}
+
 int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses) {
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();

@@ -16,7 +16,13 @@
 //     fills the twiddle table; make that first call before any stream capture;
 //   * every call shares the array and it keeps the last call's contents; each call rewrites all of
 //     it that it reads, so nothing carries over, but calls that overlap on the GPU (different
-//     streams, or threads racing) race on it and must be serialised by the caller.
+//     streams, or threads racing) race on it and must be serialised by the caller;
+//   * the address is cached per device ordinal for the life of the process: the primary context
+//     is assumed, so cudaDeviceReset, or a non-primary driver-API context made current, is not
+//     supported between calls;
+//   * the kernel spectrum arrives with lenia_kernel_spectrum's row stride H/2+1, not the 16-byte
+//     aligned stride the engine's own contexts use, so every column item takes the column pass's
+//     unchained form (transform, multiply, transform in three sweeps) instead of the chained one.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -136,6 +142,10 @@ LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, 
     const int rows = row_item_rows((int)width, 0);
     const int ncol = spec_tiles((int)width), nrow = (int)height / rows;
     const int n = ncol > nrow ? ncol : nrow;
+    // Zero-item launches configure both passes (shared-memory limits) before anything is enqueued,
+    // so a size the passes cannot run is reported without having advanced the state.
+    if (!launch_col_fp32((int)height, 0, dw, col, 0, tw, s) || !launch_row_fp32((int)width, 0, MODE_STEP, 0, dw, row, 0, 0, tw, s))
+        return set_error(LENIA_ECUDA, "launch configuration failed; the state is unchanged");
     noalloc_prepare<<<(n + 255) / 256, 256, 0, s>>>(dw, w, col, ncol, row, nrow, rows);
     bool ok = launch_row_fp32((int)width, 0, MODE_FORWARD, 0, dw, row, nrow, 0, tw, s);
     for (uint32_t i = 0; ok && i < steps; i++) {

@@ -128,10 +128,16 @@ __device__ __forceinline__ float2 twid(const float2* __restrict__ tw, int a, int
 }
 
 // A group is (world, channel, first tile); it covers CT columns = CT / TC consecutive tiles.
+//
+// Every barrier wait is bounded, and the decision to give up is made for the whole CTA at once
+// (__syncthreads_or), so that no thread is left at a barrier the others skipped.  A CTA that gives
+// up leaves the group loop, waits (bounded again) for whatever it still has in flight -- the
+// DFT-matrix load, a tile-group load, issued MMAs, its output stores -- then sets the error flag
+// (ctl[CTL_ERR]), frees its TMEM and returns.
 template <class S>
 __global__ void __launch_bounds__(128, 1)
     col_pass_tc(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ groups, int ngroups,
-                const uint8_t* __restrict__ fmats, const float2* __restrict__ tw, int* err) {
+                const uint8_t* __restrict__ fmats, const float2* __restrict__ tw, int* ctl) {
     extern __shared__ __align__(128) uint8_t smem[];
     uint8_t* op = smem;
     uint8_t* f2 = smem + S::OFF_F2;
@@ -141,7 +147,6 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t* bar_mma = bar_ld + 1;
     uint64_t* bar_f = bar_ld + 2;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_ld + 3);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
     constexpr uint32_t IDESC_A = instr_desc(S::X3 ? 1 : 2, 128, S::NA);
     constexpr uint32_t IDESC_B = instr_desc(S::X3 ? 1 : 2, 128, S::NB);
@@ -150,7 +155,6 @@ __global__ void __launch_bounds__(128, 1)
         mbar_init(bar_ld, 1);
         mbar_init(bar_mma, 1);
         mbar_init(bar_f, 1);
-        *abort_flag = 0;
         fence_barrier_init();
     }
     if (warp == 0) tmem_alloc(tmem_slot, S::TCOLS);
@@ -176,20 +180,39 @@ __global__ void __launch_bounds__(128, 1)
         bulk_g2s(stg, src, S::STG, bar_ld);
     };
     if (tid == 0 && blockIdx.x < ngroups) load_group(blockIdx.x);
-    bool ok = mbar_wait(bar_f, 0);
+    // asynchronous work in flight that an early exit has to wait for (uniform across the CTA)
+    bool ld_pending = blockIdx.x < ngroups, mma_pending = false;
+    const bool f_failed = __syncthreads_or(!mbar_wait_n(bar_f, 0, f_wait_polls(ctl)));
+    bool abort = f_failed;
     uint32_t ph_ld = 0, ph_mma = 0;
+    // issue one GEMM from an elected thread and wait for it; false (on every thread) if the wait gave up
+    auto gemm = [&](uint32_t d, uint32_t a_off, int M, int K, uint32_t f_addr, uint32_t f_lo, int N, uint32_t idesc) {
+        if (tid == 0) {
+            tc_fence_after();
+            issue_gemm<S::X3>(d, smem_u32(op), a_off, M, K, f_addr, f_lo, N, idesc);
+            mma_commit(bar_mma);
+        }
+        if (__syncthreads_or(!mbar_wait(bar_mma, ph_mma))) {
+            mma_pending = true;
+            return false;
+        }
+        ph_mma ^= 1;
+        tc_fence_after();
+        return true;
+    };
 
-    for (int g = blockIdx.x; g < ngroups && ok; g += gridDim.x) {
+    for (int g = blockIdx.x; g < ngroups && !abort; g += gridDim.x) {
         const ColItem it = groups[g];
         const DevWorld& wd = worlds[it.world];
         const int W = wd.W, HQ = wd.HQ, K = wd.K;
         const int kx0 = it.tile * TC;
-        if (!mbar_wait(bar_ld, ph_ld)) ok = false;
-        ph_ld ^= 1;
         if (tid == 0) bulk_wait_read0();  // the previous group's output has left the operand area
-        __syncthreads();
-        if (!ok) *abort_flag = 1;
-        if (*abort_flag) break;
+        if (__syncthreads_or(!mbar_wait(bar_ld, ph_ld))) {
+            abort = true;
+            break;
+        }
+        ld_pending = false;
+        ph_ld ^= 1;
 
         // ---- stage 0: tile group (fp32, [tile][y][c][re,im]) -> A_A rows (c, y1), K (re/im, y2)
         for (int b = 0; b < S::MA / 128; b++) {
@@ -212,17 +235,16 @@ __global__ void __launch_bounds__(128, 1)
         fence_async_smem();
         __syncthreads();
         // the staging buffer is free: fetch the next group while this one computes
-        if (tid == 0 && g + (int)gridDim.x < ngroups) load_group(g + gridDim.x);
+        if (g + (int)gridDim.x < ngroups) {
+            if (tid == 0) load_group(g + gridDim.x);
+            ld_pending = true;
+        }
 
         // ---- GEMM A
-        if (tid == 0) {
-            tc_fence_after();
-            issue_gemm<S::X3>(t_x, smem_u32(op), S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A);
-            mma_commit(bar_mma);
+        if (!gemm(t_x, S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A)) {
+            abort = true;
+            break;
         }
-        if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
-        ph_mma ^= 1;
-        tc_fence_after();
 
         // ---- A -> B: twiddle exp(-2 pi i y1 k2 / H), rows (c, k2), K (re/im, y1)
         for (int b = 0; b < S::MA / 128; b++) {
@@ -247,16 +269,12 @@ __global__ void __launch_bounds__(128, 1)
         __syncthreads();
 
         // ---- GEMM B -> spectrum of the channel along y, kept in TMEM region t_b
-        if (tid == 0) {
-            tc_fence_after();
-            issue_gemm<S::X3>(t_b, smem_u32(op), S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B);
-            mma_commit(bar_mma);
+        if (!gemm(t_b, S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B)) {
+            abort = true;
+            break;
         }
-        if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
-        ph_mma ^= 1;
-        tc_fence_after();
 
-        for (int k = 0; k < K; k++) {
+        for (int k = 0; k < K && !abort; k++) {
             if (wd.kern[k].src != it.chan) continue;
             const float* kh = wd.khat + (size_t)k * (W / 2 + 1) * HQ;
             // ---- B -> C: x khat (real, even), conjugate; rows (c, k2), K (re/im, k1)
@@ -286,14 +304,10 @@ __global__ void __launch_bounds__(128, 1)
             fence_async_smem();
             __syncthreads();
             // ---- GEMM C
-            if (tid == 0) {
-                tc_fence_after();
-                issue_gemm<S::X3>(t_x, smem_u32(op), S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B);
-                mma_commit(bar_mma);
+            if (!gemm(t_x, S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B)) {
+                abort = true;
+                break;
             }
-            if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
-            ph_mma ^= 1;
-            tc_fence_after();
             // ---- C -> D: twiddle exp(-2 pi i k2 y1 / H); rows (c, y1), K (re/im, k2)
             for (int b = 0; b < S::MB / 128; b++) {
                 const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
@@ -316,14 +330,10 @@ __global__ void __launch_bounds__(128, 1)
             fence_async_smem();
             __syncthreads();
             // ---- GEMM D
-            if (tid == 0) {
-                tc_fence_after();
-                issue_gemm<S::X3>(t_x, smem_u32(op), S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A);
-                mma_commit(bar_mma);
+            if (!gemm(t_x, S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A)) {
+                abort = true;
+                break;
             }
-            if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
-            ph_mma ^= 1;
-            tc_fence_after();
             // ---- output: conjugate, natural order y = y1 + H1*y2, into the operand area
             float2* out = reinterpret_cast<float2*>(op);
             for (int b = 0; b < S::MA / 128; b++) {
@@ -347,15 +357,18 @@ __global__ void __launch_bounds__(128, 1)
                 bulk_wait_read0();  // the next kernel (if any) rebuilds the operand area
             }
             __syncthreads();
-            if (*abort_flag) break;
         }
-        if (*abort_flag) break;
     }
-    if (*abort_flag && tid == 0) atomicExch(err, 1);
+    // Early exit: wait (bounded) for this CTA's own asynchronous work before its shared memory and
+    // TMEM are released, then report.
     if (tid == 0) {
+        if (abort) {
+            if (f_failed) mbar_wait(bar_f, 0);
+            if (ld_pending) mbar_wait(bar_ld, ph_ld);
+            if (mma_pending) mbar_wait(bar_mma, ph_mma);
+            atomicExch(ctl + CTL_ERR, 1);
+        }
         bulk_wait0();
-        // a group load may still be in flight if this CTA stopped early; wait for it (bounded)
-        if (*abort_flag) mbar_wait(bar_ld, ph_ld);
     }
     tc_fence_before();
     __syncthreads();
@@ -445,11 +458,14 @@ int tc_setup(TcPlan& plan, int path, std::string* err) {
     plan.path = path;
     plan.ready = 1;
     if (!plan.d_err) {
-        if (cudaMalloc(&plan.d_err, sizeof(int)) != cudaSuccess) {
-            if (err) *err = "tensor-core error flag allocation failed";
+        if (cudaMalloc(&plan.d_err, CTL_WORDS * sizeof(int)) != cudaSuccess) {
+            if (err) *err = "tensor-core control words allocation failed";
             return LENIA_ENOMEM;
         }
-        cudaMemset(plan.d_err, 0, sizeof(int));
+        if (cudaMemset(plan.d_err, 0, CTL_WORDS * sizeof(int)) != cudaSuccess) {
+            if (err) *err = "tensor-core control words initialisation failed";
+            return LENIA_ECUDA;
+        }
     }
     return 0;
 }
@@ -507,10 +523,22 @@ bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, 
 int tc_check_error(TcPlan& plan, std::string* err) {
     if (!plan.d_err) return 0;
     int h = 0;
-    if (cudaMemcpy(&h, plan.d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return LENIA_ECUDA;
+    if (cudaMemcpy(&h, (int*)plan.d_err + CTL_ERR, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return LENIA_ECUDA;
     if (h) {
-        cudaMemset(plan.d_err, 0, sizeof(int));
+        cudaMemset((int*)plan.d_err + CTL_ERR, 0, sizeof(int));
         if (err) *err = "a tensor-core column pass gave up waiting on a barrier; results of that step are invalid";
+        return LENIA_ECUDA;
+    }
+    return 0;
+}
+
+int tc_set_wait_limit(TcPlan& plan, int limit_plus_one, std::string* err) {
+    if (!plan.d_err) {
+        if (err) *err = "the context has no tensor-core pass";
+        return LENIA_ESTATE;
+    }
+    if (cudaMemcpy((int*)plan.d_err + CTL_F_POLLS, &limit_plus_one, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (err) *err = "tensor-core control word update failed";
         return LENIA_ECUDA;
     }
     return 0;
@@ -556,9 +584,12 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
         issue_gemm<X3>(t, smem_u32(sa), abytes, 128, k, smem_u32(sb), bbytes, n, instr_desc(X3 ? 1 : 2, 128, n));
         mma_commit(bar);
     }
-    const bool ok = mbar_wait(bar, 0);
+    const bool ok = !__syncthreads_or(!mbar_wait(bar, 0));
     tc_fence_after();
-    if (!ok && tid == 0) atomicExch(err, 1);
+    if (!ok && tid == 0) {
+        mbar_wait(bar, 0);  // the MMAs still in flight write TMEM: wait for them (bounded) before freeing it
+        atomicExch(err, 1);
+    }
     for (int q = 0; q < n / 32 && ok; q++) {
         float v[32];
         tmem_ld32(t + ((uint32_t)(warp * 32) << 16) + 32 * q, v);

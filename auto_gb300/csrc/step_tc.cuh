@@ -8,8 +8,9 @@
 
 namespace lenia {
 
-// Per-context device data of the tensor-core path: the DFT matrices per column length, and a
-// flag a kernel sets if it gives up waiting on a barrier.
+// Per-context device data of the tensor-core path: the DFT matrices per column length, and the
+// control words (tc_ptx.cuh: CTL_*): an error flag a kernel sets if it gives up waiting on a
+// barrier, and a test hook on the poll limit of one wait.
 struct TcPlan {
     int ready = 0;
     int path = 0;
@@ -30,6 +31,9 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err);
 bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
                    const float2* tw, cudaStream_t s, int reserve_sms = 0);
 int tc_check_error(TcPlan& plan, std::string* err);
+// Test hook: limit_plus_one = 0 keeps the default poll limit of the DFT-matrix wait, n > 0 makes it
+// n - 1 polls (1: the wait gives up at once and the pass exits early with the error flag set).
+int tc_set_wait_limit(TcPlan& plan, int limit_plus_one, std::string* err);
 // The 4096-point column pass with two pipelines per SM (step_tc64.cu); fmat = the 64-point DFT matrix.
 bool launch_col_tc64(bool x3, const void* fmat, const DevWorld* worlds, const ColItem* groups, int ngroups,
                      const float2* tw, int* err, cudaStream_t s, int reserve_sms = 0);

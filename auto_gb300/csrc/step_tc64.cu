@@ -102,7 +102,7 @@ __device__ __forceinline__ void gemm128(uint32_t d, uint32_t a, uint32_t b) {
 template <bool X3>
 __global__ void __launch_bounds__(256, 1)
     col_pass_tc64(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ groups, int ngroups,
-                  const uint8_t* __restrict__ fmat, const float2* __restrict__ tw, int* err) {
+                  const uint8_t* __restrict__ fmat, const float2* __restrict__ tw, int* ctl) {
     using S = Tc64<X3>;
     extern __shared__ __align__(128) uint8_t smem[];
     const int tid = threadIdx.x, wg = tid >> 7, t = tid & 127, warp = tid >> 5;
@@ -114,13 +114,10 @@ __global__ void __launch_bounds__(256, 1)
     uint64_t* bar_mma = bars + 1 + wg;    // this warpgroup's MMAs done
     uint64_t* bar_kh = bars + 3 + wg;     // this warpgroup's kernel-spectrum rows arrived
     uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 5);
-    volatile int* abort_flag = reinterpret_cast<volatile int*>(tslot + 1) + wg;
     const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
 
     if (tid == 0) {
         for (int i = 0; i < 5; i++) mbar_init(bars + i, 1);
-        abort_flag[0] = 0;
-        abort_flag[1] = 0;
         fence_barrier_init();
     }
     if (warp == 0) tmem_alloc(tslot, 512);
@@ -151,11 +148,18 @@ __global__ void __launch_bounds__(256, 1)
             P8[i].y *= sgn;
         }
     }
-    bool ok = mbar_wait(bar_f, 0);
-    uint32_t ph_mma = 0, ph_kh = 0;
-    const uint32_t fa = smem_u32(f), oa = smem_u32(op);
+    // Every wait is bounded and each warpgroup decides to give up as a whole (named_sync_or), so
+    // that no thread is left at a barrier the others skipped.  A warpgroup that gives up leaves its
+    // group loop and, before TMEM is freed, waits (bounded again) for what it still has in flight:
+    // the DFT-matrix load, its kernel-spectrum load, its issued MMAs and its output stores.
     const int bar_id = 1 + wg;
     auto wg_sync = [&]() { named_sync(bar_id, 128); };
+    auto wg_any = [&](bool p) { return named_sync_or(bar_id, 128, p); };
+    const bool f_failed = wg_any(!mbar_wait_n(bar_f, 0, f_wait_polls(ctl)));
+    bool abort = f_failed, kh_pending = false, mma_pending = false;
+    uint32_t ph_mma = 0, ph_kh = 0;
+    const uint32_t fa = smem_u32(f), oa = smem_u32(op);
+    // one GEMM from an elected thread; false (on the whole warpgroup) if its wait gave up
     auto gemm_wait = [&](uint32_t d, uint32_t a, uint32_t b) {
         tc_fence_before();
         fence_async_smem();
@@ -165,13 +169,17 @@ __global__ void __launch_bounds__(256, 1)
             gemm128<X3>(d, a, b);
             mma_commit(bar_mma);
         }
-        if (!mbar_wait(bar_mma, ph_mma)) *abort_flag = 1;
+        if (wg_any(!mbar_wait(bar_mma, ph_mma))) {
+            mma_pending = true;
+            return false;
+        }
         ph_mma ^= 1;
         tc_fence_after();
+        return true;
     };
 
     const int stride = 2 * gridDim.x;
-    for (int g = 2 * blockIdx.x + wg; g < ngroups && ok; g += stride) {
+    for (int g = 2 * blockIdx.x + wg; g < ngroups && !abort; g += stride) {
         const ColItem it = groups[g];
         const DevWorld& wd = worlds[it.world];
         const int W = wd.W, K = wd.K;
@@ -186,9 +194,12 @@ __global__ void __launch_bounds__(256, 1)
         // kernel-spectrum rows of the first kernel that reads this channel, in flight during the transforms
         int kfirst = 0;
         while (kfirst < K && wd.kern[kfirst].src != it.chan) kfirst++;
-        if (t == 0 && kfirst < K) {
-            mbar_arrive_expect_tx(bar_kh, S::KH);
-            bulk_g2s(kh, wd.khat + ((size_t)kfirst * (W / 2 + 1) + (size_t)it.tile * TC) * S::HQ, S::KH, bar_kh);
+        if (kfirst < K) {
+            if (t == 0) {
+                mbar_arrive_expect_tx(bar_kh, S::KH);
+                bulk_g2s(kh, wd.khat + ((size_t)kfirst * (W / 2 + 1) + (size_t)it.tile * TC) * S::HQ, S::KH, bar_kh);
+            }
+            kh_pending = true;
         }
         // ---- stage 0: X rows (c, y1) = t, K (re/im, y2), straight from global memory
         {
@@ -211,7 +222,10 @@ __global__ void __launch_bounds__(256, 1)
                 }
             }
         }
-        gemm_wait(t_x, fa, oa);  // GEMM A: D[(k2, ro)][(c, y1)]
+        if (!gemm_wait(t_x, fa, oa)) {  // GEMM A: D[(k2, ro)][(c, y1)]
+            abort = true;
+            break;
+        }
         // ---- A -> B: lane (k2, ro); twiddle exp(-2 pi i y1 k2 / 4096); X_B row (c, k2), K (ro, y1)
         {
             const int k2 = t >> 1, ro = t & 1;
@@ -229,14 +243,24 @@ __global__ void __launch_bounds__(256, 1)
                 store32<X3>(op, c * 64 + k2, ro * 64 + ybase, o);
             }
         }
-        gemm_wait(t_b, oa, fa);  // GEMM B: D[(c, k2)][(k1, ro)]
-        for (int k = 0; k < K && ok; k++) {
+        if (!gemm_wait(t_b, oa, fa)) {  // GEMM B: D[(c, k2)][(k1, ro)]
+            abort = true;
+            break;
+        }
+        for (int k = 0; k < K && !abort; k++) {
             if (wd.kern[k].src != it.chan) continue;
-            if (t == 0 && k != kfirst) {
-                mbar_arrive_expect_tx(bar_kh, S::KH);
-                bulk_g2s(kh, wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)it.tile * TC) * S::HQ, S::KH, bar_kh);
+            if (k != kfirst) {
+                if (t == 0) {
+                    mbar_arrive_expect_tx(bar_kh, S::KH);
+                    bulk_g2s(kh, wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)it.tile * TC) * S::HQ, S::KH, bar_kh);
+                }
+                kh_pending = true;
             }
-            if (!mbar_wait(bar_kh, ph_kh)) *abort_flag = 1;
+            if (wg_any(!mbar_wait(bar_kh, ph_kh))) {
+                abort = true;
+                break;
+            }
+            kh_pending = false;
             ph_kh ^= 1;
             // ---- B -> C: lane (c, k2); x khat, conjugate; X_C row (c, k2) = t, K (ro, k1)
             {
@@ -261,7 +285,10 @@ __global__ void __launch_bounds__(256, 1)
                     }
                 }
             }
-            gemm_wait(t_x, fa, oa);  // GEMM C: D[(y1, ro)][(c, k2)]
+            if (!gemm_wait(t_x, fa, oa)) {  // GEMM C: D[(y1, ro)][(c, k2)]
+                abort = true;
+                break;
+            }
             // ---- C -> D: lane (y1, ro); twiddle exp(-2 pi i k2 y1 / 4096); X_D row (c, y1), K (ro, k2)
             {
                 const int y1 = t >> 1, ro = t & 1;
@@ -279,7 +306,10 @@ __global__ void __launch_bounds__(256, 1)
                     store32<X3>(op, c * 64 + y1, ro * 64 + kbase, o);
                 }
             }
-            gemm_wait(t_x, oa, fa);  // GEMM D: D[(c, y1)][(y2, ro)]
+            if (!gemm_wait(t_x, oa, fa)) {  // GEMM D: D[(c, y1)][(y2, ro)]
+                abort = true;
+                break;
+            }
             // ---- output: lane (c, y1); conjugate; y = y1 + 64 y2 into the free operand buffer, then one
             // bulk copy to the convolved-spectrum tile
             {
@@ -302,12 +332,17 @@ __global__ void __launch_bounds__(256, 1)
             }
             tc_fence_before();
             wg_sync();
-            if (*abort_flag) ok = false;
         }
-        if (*abort_flag) ok = false;
     }
-    if (*abort_flag && t == 0) atomicExch(err, 1);
-    if (t == 0) bulk_wait0();
+    if (t == 0) {
+        if (abort) {
+            if (f_failed) mbar_wait(bar_f, 0);
+            if (kh_pending) mbar_wait(bar_kh, ph_kh);
+            if (mma_pending) mbar_wait(bar_mma, ph_mma);
+            atomicExch(ctl + CTL_ERR, 1);
+        }
+        bulk_wait0();
+    }
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {

@@ -54,11 +54,38 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// Polls of a bounded barrier wait before the waiter gives up and reports an error.
+constexpr uint32_t WAIT_POLLS = 1u << 22;
 // Bounded wait: returns false (and the caller reports an error) instead of spinning forever.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (uint32_t i = 0; i < (1u << 22); i++)
+__device__ __forceinline__ bool mbar_wait_n(uint64_t* bar, uint32_t parity, uint32_t polls) {
+    for (uint32_t i = 0; i < polls; i++)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) { return mbar_wait_n(bar, parity, WAIT_POLLS); }
+
+// Barrier over `count` threads with hardware barrier `id` that also ORs a predicate: every
+// participating thread gets true if any of them passed true.  Keeps give-up decisions uniform
+// across a warpgroup, so that no thread is left at a barrier the others skipped.
+__device__ __forceinline__ bool named_sync_or(int id, int count, bool pred) {
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, %2, %3, p;\n\tselp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred), "r"(id), "r"(count)
+        : "memory");
+    return r != 0;
+}
+
+// Device-side control words of the tensor-core passes (one int array per context):
+//   [0] error flag: set to 1 by a pass that gave up waiting on a barrier
+//   [1] test hook: 0 keeps the default poll limit of the DFT-matrix wait; n > 0 sets it to n - 1
+//       polls (1 makes that wait give up at once, before any MMA is issued)
+constexpr int CTL_ERR = 0, CTL_F_POLLS = 1, CTL_WORDS = 2;
+__device__ __forceinline__ uint32_t f_wait_polls(const int* ctl) {
+    const int v = ctl[CTL_F_POLLS];
+    return v > 0 ? (uint32_t)(v - 1) : WAIT_POLLS;
 }
 
 // ----------------------------------------------------------------- bulk copies (TMA engine)

@@ -1,8 +1,10 @@
 """Lenia cell-updates/s on one GB300 (and N independent replicas under torchrun).
 
 One bench step = one ``lenia_step(ctx, G)`` call: G generations (default 64, one CUDA-graph replay)
-of every world in the workload.  The default workload is the single 4096x4096 world with a
-three-shell R=52 kernel; ``--config batched`` runs the 384 uneven worlds in one context.
+of every world in the workload.  The default workload is the metric's own: 384 uneven worlds
+(sides 128..1024, per-world R, mu, sigma, dt) batched in one context; ``--config single_4096`` runs
+the single 4096x4096 world with a three-shell R=52 kernel, ``--config multichannel`` the 3-channel
+1024x1024 world with 9 kernels.
 
 Printed JSON (one line, rank 0):
   value   cell-updates/s with the state resident in HBM, from CUDA events on the engine stream
@@ -14,7 +16,8 @@ Printed JSON (one line, rank 0):
           blocking calls (lenia_write_states / lenia_read_states)
   roofline  12 algorithmic bytes per cell-update (state read and written, one complex f32
           half-spectrum value) over the event-timed generation time, against the measured HBM
-          copy bandwidth; traffic = DRAM bytes per generation from an ncu capture
+          copy bandwidth; traffic = DRAM bytes per generation from an ncu capture of one
+          graph replay with warm caches (``--profile-window``, summarised by ``--traffic-from``)
   cpu_baseline  the CPU restatement of the reference step on the host cores, bounded sample
   clocks  SM clock and throttle reasons sampled with nvidia-smi during the timed region
   gpu_launches  kernel launches in the timed region (two per size class per generation)
@@ -58,7 +61,7 @@ def parse(argv=None):
     p.add_argument("--steps", type=int, default=60)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--config", default="single_4096", choices=["single_4096", "batched", "single_256", "multichannel"])
+    p.add_argument("--config", default="batched", choices=["batched", "single_4096", "single_256", "multichannel"])
     p.add_argument("--path", default="fp32", choices=["fp32", "tf32", "bf16x3", "radix2"])
     p.add_argument("--gens", type=int, default=64, help="generations per bench step")
     p.add_argument("--no-e2e", action="store_true")
@@ -69,6 +72,13 @@ def parse(argv=None):
     p.add_argument("--no-paths", action="store_true", help="skip timing the other step paths side by side")
     p.add_argument("--grids", action="store_true",
                    help="the reference's own published programs and grids, measured its way: one line per grid")
+    p.add_argument("--profile-window", action="store_true",
+                   help="set up, autotune and warm up the workload, then run exactly one bench step (one graph "
+                        "replay) between cudaProfilerStart and cudaProfilerStop and exit: for ncu "
+                        "--profile-from-start off")
+    p.add_argument("--traffic-from", default=None, metavar="CSV",
+                   help="summarise an ncu --csv capture of --profile-window (dram__bytes_read.sum, "
+                        "dram__bytes_write.sum, gpu__time_duration.sum) into profiles/traffic.json and exit")
     return p.parse_args(argv)
 
 
@@ -309,12 +319,105 @@ def run_reference(args, dist):
 
 # ----------------------------------------------------------------------------- our arm
 
+TRAFFIC_JSON = os.path.join(ROOT, "profiles", "traffic.json")
+
+
 def read_traffic():
-    p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
-        return json.load(open(p))
+        return json.load(open(TRAFFIC_JSON))
     except Exception:
         return {}
+
+
+_UNIT_SCALE = {"byte": 1.0, "kbyte": 1e3, "mbyte": 1e6, "gbyte": 1e9, "kibyte": 1024.0, "mibyte": 1024.0 ** 2,
+               "gibyte": 1024.0 ** 3, "nsecond": 1e-9, "usecond": 1e-6, "msecond": 1e-3, "second": 1.0,
+               "ns": 1e-9, "us": 1e-6, "ms": 1e-3}
+
+
+def parse_ncu_csv(path):
+    """Per-launch metrics of an ``ncu --csv`` log: a list of (kernel name, {metric: value in bytes or
+    seconds}) in launch order."""
+    import csv
+    rows = []
+    with open(path, newline="") as f:
+        lines = [l for l in f if l.startswith('"')]  # drop ncu's own ==PROF== lines
+    launches = {}
+    order = []
+    for r in csv.DictReader(lines):
+        lid = r.get("ID")
+        if lid is None or r.get("Metric Name") is None:
+            continue
+        if lid not in launches:
+            launches[lid] = (r.get("Kernel Name", ""), {})
+            order.append(lid)
+        try:
+            v = float(r["Metric Value"].replace(",", ""))
+        except ValueError:
+            continue
+        v *= _UNIT_SCALE.get((r.get("Metric Unit") or "byte").strip().lower(), 1.0)
+        launches[lid][1][r["Metric Name"]] = v
+    for lid in order:
+        rows.append(launches[lid])
+    return rows
+
+
+def summarise_traffic(csv_path, config, path, gens):
+    """DRAM bytes per generation of one graph replay (``--profile-window``): every launch's
+    dram__bytes_read.sum + dram__bytes_write.sum summed and divided by the generations the replay
+    ran, with the share of each kernel family.  Written to profiles/traffic.json under
+    "<config>/<path>"."""
+    rows = parse_ncu_csv(csv_path)
+    if not rows:
+        raise SystemExit("no launches in %s" % csv_path)
+    fam = {}
+    total_b = total_t = 0.0
+    for name, m in rows:
+        b = m.get("dram__bytes_read.sum", 0.0) + m.get("dram__bytes_write.sum", 0.0)
+        t = m.get("gpu__time_duration.sum", 0.0)
+        key = name.split("<")[0].split("(")[0].strip()
+        f = fam.setdefault(key, {"launches": 0, "dram_bytes": 0.0, "time_s": 0.0})
+        f["launches"] += 1
+        f["dram_bytes"] += b
+        f["time_s"] += t
+        total_b += b
+        total_t += t
+    for f in fam.values():
+        f["share_of_bytes"] = f["dram_bytes"] / total_b if total_b else None
+        f["share_of_time"] = f["time_s"] / total_t if total_t else None
+    data = read_traffic()
+    key = "%s/%s" % (config, path)
+    data[key] = total_b / gens
+    details = data.setdefault("details", {})
+    details[key] = {"launches": len(rows), "generations": gens, "dram_bytes_per_generation": total_b / gens,
+                    "cache": "warm (ncu --cache-control none, one graph replay after warm-up)", "kernels": fam}
+    data["note"] = ("DRAM bytes per generation: dram__bytes_read.sum + dram__bytes_write.sum over every launch "
+                    "of one graph replay, divided by its generations; command in profiles/traffic.md")
+    with open(TRAFFIC_JSON, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+        f.write("\n")
+    return data[key], details[key]
+
+
+def profile_window(args, dist):
+    """One bench step between cudaProfilerStart / cudaProfilerStop, after the same set-up,
+    autotuning and warm-up as the timed run, for ``ncu --profile-from-start off``."""
+    import torch
+    from auto_gb300 import Sim
+    worlds, seeds, cfg = workload(args.config)
+    sim = Sim(worlds, seed=0, path=args.path)
+    seed_all(sim, worlds, seeds)
+    if not args.no_autotune:
+        sim.autotune()
+    for _ in range(args.warmup):
+        sim.step(args.gens)
+    sim.wait()
+    torch.cuda.init()
+    torch.cuda.profiler.start()
+    sim.step(args.gens)
+    sim.wait()
+    torch.cuda.profiler.stop()
+    sim.close()
+    print(json.dumps({"profile_window": args.config, "path": args.path, "generations": args.gens}))
 
 
 def run_ours(args, dist):
@@ -531,16 +634,17 @@ def reference_rate(sim, seconds=2.0, warmup=32):
     return median, spread, batch, len(rates)
 
 
-def append_reference_sample(path, sim, worlds, cfg, impl_path):
+def append_reference_sample(path, sim, worlds, cfg, impl_path, seconds=2.0):
     """One record in the reference's results/*.jsonl format (crates/auto-cli/src/bench.rs:39-55),
     measured its way (reference_rate)."""
-    median, spread, batch, nb = reference_rate(sim)
-    cells = sim.cells_per_step
+    median, spread, batch, nb = reference_rate(sim, seconds=seconds)
+    cells = int(sim.cells_per_step)
     w0 = worlds[0]
     rec = {"id": w0.id if len(worlds) == 1 else "batched", "tag": impl_path, "adapter": "NVIDIA GB300 (CUDA, sm_103a)",
-           "checks": "Safe", "width": w0.width, "height": w0.height, "cells": cells, "memory_bytes": sim.memory_bytes,
-           "steps_per_second": median, "generations_per_second": median, "cells_per_second": median * cells,
-           "batch_steps": batch, "batches": nb, "spread": spread}
+           "checks": "Safe", "width": int(w0.width), "height": int(w0.height), "cells": cells,
+           "memory_bytes": int(sim.memory_bytes), "steps_per_second": float(median),
+           "generations_per_second": float(median), "cells_per_second": float(median * cells),
+           "batch_steps": int(batch), "batches": int(nb), "spread": float(spread)}
     with open(path, "a") as f:
         f.write(json.dumps(rec) + "\n")
 
@@ -584,7 +688,12 @@ def main():
     dist = Dist()
     dist.gpu_index = gpu
     try:
-        if args.impl == "reference":
+        if args.traffic_from:
+            per_gen, det = summarise_traffic(args.traffic_from, args.config, args.path, args.gens)
+            print(json.dumps({"traffic_per_generation": per_gen, "details": det}))
+        elif args.profile_window:
+            profile_window(args, dist)
+        elif args.impl == "reference":
             run_reference(args, dist)
         elif args.grids:
             run_grids(args, dist)

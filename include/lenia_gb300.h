@@ -204,6 +204,17 @@ LENIA_API int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, u
  * reference (it has no tensor-core code). */
 LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const float* b, float* d);
 
+/* Failure-detection test hook: every barrier wait in the tensor-core column passes gives up
+ * after a bounded number of polls, exits early (after waiting, bounded again, for its own copies
+ * and MMAs in flight, and freeing its TMEM) and raises the context's error flag, which
+ * lenia_sync / lenia_read_state / lenia_step_timed report as LENIA_ECUDA.  polls_plus_one = 0
+ * keeps the default limit of the pass's first wait (the DFT-matrix load); n > 0 sets it to n - 1
+ * polls, so 1 makes that wait give up at once, before any MMA is issued.  Takes effect at the next
+ * launch (no graph rebuild).  LENIA_ESTATE on a context without a tensor-core path.  The reference
+ * surfaces failures as Err(String) rather than panics (crates/auto-core/src/sim.rs:208-219); it has
+ * no device-side waits. */
+LENIA_API int lenia_tc_set_wait_limit(LeniaCtx* ctx, int32_t polls_plus_one);
+
 /* Steps one world of one channel and one Lenia kernel `steps` times, in place, without allocating
  * device memory.  For callers that cannot call cudaMalloc when they step: an application that
  * has given all device memory to its own pool allocator, or a real-time frame loop where an
@@ -216,7 +227,11 @@ LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float*
  * 4.2 MiB that every GPU loading this library holds until exit, so width*height is limited to
  * 1,048,576 cells (larger returns LENIA_ESIZE).  The first call on a device finds the array's
  * address and fills its twiddle table: make it before any stream capture.  All calls share the
- * array, so calls that overlap on the GPU race; serialise them.  Errors: lenia_last_error(NULL). */
+ * array, so calls that overlap on the GPU race; serialise them.  The address is cached per device
+ * ordinal, so cudaDeviceReset or a non-primary context between calls is not supported.  A size or
+ * launch-configuration error is reported before anything is enqueued; after a launch error (a
+ * CUDA error after enqueueing) the state may have been advanced by some of the steps.  Errors:
+ * lenia_last_error(NULL). */
 LENIA_API int lenia_step_noalloc(float* state, uint32_t width, uint32_t height, const float* khat, float mu,
                                  float sigma, float dt, uint32_t steps, void* stream);
 

@@ -1,7 +1,7 @@
 """Generate the golden fixtures under tests/golden/ from the reference project's own sources.
 
-Run in a container where the reference checkout is mounted (default /root/reference, or pass a
-path).  The reference is Rust + WGSL and cannot run here, so this script restates in pure
+Run where the reference checkout is available: pass its path as the first argument, or set
+AUTO_REFERENCE to it (there is no default).  The reference is Rust + WGSL and cannot run here, so this script restates in pure
 Python/numpy -- independently of oracle/lenia_oracle.c -- exactly what its one Lenia test does:
 
 * crates/auto-core/src/automata/spectral.rs:287       the Orbium table (u8, 20x20)
@@ -111,4 +111,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AUTO_REFERENCE")
+    if not ref:
+        sys.exit("usage: gen_golden.py REFERENCE_CHECKOUT (or set AUTO_REFERENCE)")
+    main(ref)

@@ -61,3 +61,60 @@ def test_reference_arm_under_torchrun_prints_once():
     assert len(lines) == 1, out.stdout[-2000:]
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+# The fields of the reference's results/*.jsonl record, in order, with their types: `Sample` in
+# crates/auto-cli/src/bench.rs:39-55 (String x 4, u32 x 2, u64 x 2, f64 x 3, u32 x 2, f64).
+SAMPLE_FIELDS = [("id", str), ("tag", str), ("adapter", str), ("checks", str), ("width", int), ("height", int),
+                 ("cells", int), ("memory_bytes", int), ("steps_per_second", float),
+                 ("generations_per_second", float), ("cells_per_second", float), ("batch_steps", int),
+                 ("batches", int), ("spread", float)]
+
+
+class _FakeSim:
+    """Stands in for Sim in the harness: each step of `batch` generations takes batch * 0.5 ms."""
+    cells_per_step = 65536
+    memory_bytes = 1234567
+
+    def __init__(self):
+        self.stepped = 0
+
+    def step(self, n):
+        import time
+        self.stepped += n
+        time.sleep(n * 0.0005)
+
+    def wait(self):
+        pass
+
+
+def test_jsonl_sample_has_exactly_the_reference_fields(tmp_path):
+    """bench.append_reference_sample writes one record with the reference's Sample fields, in its
+    order and types, and the record's rates agree with each other."""
+    import bench
+    from auto_gb300 import configs
+    path = tmp_path / "gpu.jsonl"
+    sim = _FakeSim()
+    w = configs.single_256()
+    bench.append_reference_sample(str(path), sim, [w], {}, "fp32", seconds=0.3)
+    lines = path.read_text().splitlines()
+    assert len(lines) == 1
+    rec = json.loads(lines[0])
+    assert list(rec) == [f for f, _ in SAMPLE_FIELDS]
+    for f, t in SAMPLE_FIELDS:
+        assert isinstance(rec[f], t) and not isinstance(rec[f], bool), (f, rec[f])
+    assert rec["width"] == w.width and rec["height"] == w.height and rec["cells"] == sim.cells_per_step
+    assert rec["memory_bytes"] == sim.memory_bytes and rec["checks"] == "Safe"
+    assert rec["generations_per_second"] == rec["steps_per_second"]
+    assert abs(rec["cells_per_second"] - rec["steps_per_second"] * rec["cells"]) < 1e-6 * rec["cells_per_second"]
+
+
+def test_reference_rate_grows_the_batch_to_20ms_and_takes_the_median():
+    """crates/auto-cli/src/bench.rs:112-166: the batch grows until one submit takes >= 20 ms, then
+    batches run for the measuring time and the median rate is reported."""
+    import bench
+    sim = _FakeSim()
+    median, spread, batch, nb = bench.reference_rate(sim, seconds=0.3, warmup=4)
+    assert batch * 0.0005 >= 0.02 * 0.8  # the submit that ended the search took about 20 ms or more
+    assert nb >= 3 and 0.0 <= spread < 1.0
+    assert 0.5 / 0.0005 * 0.5 < median <= 1.0 / 0.0005  # about 2000 generations/s, sleep overhead aside

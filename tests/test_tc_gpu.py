@@ -78,3 +78,43 @@ def test_tc_batched_and_multichannel_run(path):
         for i, w in enumerate(worlds):
             err = np.abs(sim.read_state(i) - fp64_step(w, before[i])).max()
             assert err < (1e-4 if path == "bf16x3" else 1e-2), (i, w.width, err)
+
+
+def test_wait_timeout_reports_error_and_leaves_gpu_usable():
+    """A tensor-core column pass whose first barrier wait gives up (the test hook sets its poll
+    limit to zero, so it gives up before any MMA is issued) exits early -- after waiting, bounded,
+    for its own DFT-matrix and tile loads and freeing its TMEM -- and raises the context's error
+    flag: lenia_sync returns LENIA_ECUDA with a message, as the reference returns Err(String)
+    (crates/auto-core/src/sim.rs:208-219).  Nothing is left waiting, so the same GPU then runs a
+    fresh context to a one-step parity check against FP64, and the first context recovers too."""
+    L = _lib.load()
+    world = ag.World(256, 256, [ag.Kernel(radius=13.0)])
+    rng = np.random.default_rng(7)
+    s = rng.random((256, 256), dtype=np.float32)
+    with Sim(world, path="bf16x3") as sim:
+        sim.write_state(0, s)
+        assert L.lenia_tc_set_wait_limit(sim._ctx, 1) == 0
+        assert L.lenia_step(sim._ctx, 1) == 0
+        rc = L.lenia_sync(sim._ctx)
+        assert rc == _lib.ECUDA, rc
+        msg = L.lenia_last_error(sim._ctx).decode()
+        assert "gave up waiting" in msg, msg
+        # the flag is cleared once reported; with the default limit the context steps correctly again
+        assert L.lenia_tc_set_wait_limit(sim._ctx, 0) == 0
+        sim.write_state(0, s)
+        sim.step(1)
+        assert L.lenia_sync(sim._ctx) == 0
+        err_same = float(np.abs(sim.read_state(0) - fp64_step(world, s[None])).max())
+    with Sim(world, path="bf16x3") as fresh:
+        fresh.write_state(0, s)
+        fresh.step(1)
+        assert L.lenia_sync(fresh._ctx) == 0
+        err_fresh = float(np.abs(fresh.read_state(0) - fp64_step(world, s[None])).max())
+    print("after a forced wait timeout: same context %.3e, fresh context %.3e vs FP64" % (err_same, err_fresh))
+    assert err_same < 1e-4 and err_fresh < 1e-4, (err_same, err_fresh)
+
+
+def test_wait_limit_hook_rejected_without_tensor_cores():
+    L = _lib.load()
+    with Sim(ag.World(64, 64, [ag.Kernel(radius=8.0)]), path="fp32") as sim:
+        assert L.lenia_tc_set_wait_limit(sim._ctx, 1) == _lib.ESTATE

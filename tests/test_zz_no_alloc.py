@@ -19,17 +19,19 @@ from auto_gb300 import Sim, _lib
 pytestmark = pytest.mark.gpu
 
 
-def test_noalloc_matches_context_step_on_two_calls():
+# 1024 x 1024 fills the half-spectrum region exactly; 4096 x 256 fills the column-item region and
+# 256 x 4096 the row-item region.
+@pytest.mark.parametrize("w,h", [(512, 256), (1024, 1024), (4096, 256), (256, 4096)])
+def test_noalloc_matches_context_step_on_two_calls(w, h):
     torch = pytest.importorskip("torch")
     from auto_gb300 import native
     native.build()
     L = _lib.load()
-    w, h = 512, 256
     k = ag.Kernel(radius=20.0, beta=[1.0, 0.5], mu=0.2, sigma=0.03)
     world = ag.World(w, h, [k], dt=0.1)
-    rng = np.random.default_rng(3)
+    rng = np.random.default_rng(3 + w + h)
     s0 = np.zeros((h, w), np.float32)
-    s0[64:192, 128:384] = rng.random((128, 256), dtype=np.float32)
+    s0[h // 4:3 * h // 4, w // 4:3 * w // 4] = rng.random((h // 2, w // 2), dtype=np.float32)
 
     kd = world.to_desc().kernels[0]
     khat = np.zeros((w // 2 + 1) * (h // 2 + 1), np.float32)
