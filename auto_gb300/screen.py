@@ -245,9 +245,13 @@ def run(cfg: ScreenConfig, path: str = "fp32", log=print) -> Dict:
     nu = judged_u["labels"]
     good_l = int(nl[:, 1].sum())
     good_u = int(nu[:, 1].sum())
-    # per GPU-hour: the learned screen pays for its ranking on top of the simulations it judges
+    # per GPU-hour, two ways.  Amortised: the learned screen pays for its ranking on top of the
+    # simulations it judges (the cost once a trained model is reused).  All-in: it also pays for the
+    # simulations that labelled its training set and for its training.
     hours_l = (judged_l["gpu_ms"] * 1e-3 + t_rank) / 3600.0
     hours_u = judged_u["gpu_ms"] * 1e-3 / 3600.0
+    fixed_s = data["gpu_ms"] * 1e-3 + t_train
+    hours_l_all = hours_l + fixed_s / 3600.0
     rep = {
         "train_worlds": cfg.train_worlds, "side": cfg.side, "steps": cfg.steps, "candidates": cfg.candidates,
         "top": cfg.top, "train_loss_first_last": [hist[0], hist[-1]], "train_seconds": t_train,
@@ -260,8 +264,33 @@ def run(cfg: ScreenConfig, path: str = "fp32", log=print) -> Dict:
     rep["gain_nontrivial_per_gpu_hour"] = (rep["learned"]["nontrivial_per_gpu_hour"] /
                                            rep["uniform"]["nontrivial_per_gpu_hour"]
                                            if good_u else None)
+    rep["all_in"] = all_in_accounting(good_l, good_u, cfg.top, hours_l * 3600.0, hours_u * 3600.0, fixed_s,
+                                      data["gpu_ms"] * 1e-3, t_train)
+    rep["label_positives_train"] = {"survive": int(Y[:, 0].sum()), "move": int(Y[:, 1].sum()),
+                                    "explode": int(Y[:, 2].sum())}
+    if int(Y[:, 2].sum()) == 0:
+        rep["explode_head"] = ("untrained: no world in the training ranges exploded (mass above 0.9 of the area), "
+                               "so the head only learns to predict 0; the ranking score's (1 - p_explode) is then ~1")
     mlp.close()
     return rep
+
+
+def all_in_accounting(good_l, good_u, judged, judge_s_l, judge_s_u, fixed_s, data_s, train_s):
+    """The learned screen charged in full: labelling its training set (simulator GPU time) and training
+    it, on top of ranking and judging.  With n worlds judged per trained model, its yield per GPU-hour
+    is (good_l / judged) n / (fixed + (judge_s_l / judged) n); the uniform screen's is good_u / judge_s_u.
+    Returns the all-in ratio at this run's n and the n at which the learned screen breaks even (1x) and
+    reaches 3x (None if it never does: its per-world rate times the uniform cost is below 3x)."""
+    rate_l, cost_l = good_l / judged, judge_s_l / judged
+    yield_u = good_u / judge_s_u if judge_s_u and good_u else None
+    total_l = fixed_s + judge_s_l
+    out = {"fixed_seconds": fixed_s, "training_data_gpu_seconds": data_s, "training_seconds": train_s,
+           "learned_seconds_all_in": total_l, "nontrivial_per_gpu_hour_all_in": good_l / (total_l / 3600.0),
+           "gain_all_in": (good_l / total_l) / yield_u if yield_u else None}
+    for name, f in (("break_even_judged_worlds", 1.0), ("judged_worlds_for_3x", 3.0)):
+        den = rate_l - f * yield_u * cost_l if yield_u else 0.0
+        out[name] = f * yield_u * fixed_s / den if den > 0 else None
+    return out
 
 
 if __name__ == "__main__":

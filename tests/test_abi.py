@@ -90,3 +90,18 @@ def test_configs_are_deterministic():
     m = ag.configs.multichannel()
     for d in range(3):
         assert abs(sum(k.weight for k in m.kernels if k.dst == d) - 1.0) < 1e-6
+
+
+def test_rust_crate_binds_only_declared_entry_points():
+    """crates/auto-cuda (not compiled here: no Rust toolchain) binds the C ABI by name: every
+    function in its extern block is one the header declares, with the same number of arguments."""
+    src = open(os.path.join(ROOT, "crates", "auto-cuda", "src", "lib.rs")).read()
+    block = src[src.index('unsafe extern "C" {'):]
+    block = block[:block.index("\n}\n")]
+    rust = dict(re.findall(r"fn (lenia_\w+)\(([^)]*)\)", block.replace("\n", " ")))
+    hdr = open(os.path.join(ROOT, "include", "lenia_gb300.h")).read().replace("\n", " ")
+    c = dict(re.findall(r"LENIA_API\s+[\w\s\*]*?\b(lenia_\w+)\s*\(([^)]*)\)", hdr))
+    assert len(rust) >= 15
+    for name, args in rust.items():
+        assert name in c, name
+        assert len([a for a in args.split(",") if a.strip()]) == len([a for a in c[name].split(",") if a.strip()]), name
