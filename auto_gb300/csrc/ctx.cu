@@ -28,6 +28,15 @@ namespace {
 
 thread_local std::string g_create_error;
 
+// A run of consecutive worlds of one size class (their items are consecutive in the class lists).
+// The step graph advances a chunk through all of its steps before the next chunk starts, so a chunk
+// small enough for L2 keeps its states, spectra and kernel spectra there across generations instead
+// of streaming them from HBM twice per generation.
+struct Chunk {
+    int col0 = 0, ncol = 0, tcg0 = 0, ntcg = 0, row0 = 0, nrow = 0;
+    size_t bytes = 0;
+};
+
 struct SizeClass {
     int W = 0, H = 0;
     std::vector<int> worlds;
@@ -39,7 +48,14 @@ struct SizeClass {
     int nrow = 0;
     int var_col = 0, var_row = 0;  // launch variants (see launch_col_fp32)
     int general = 0, planes = 0;
+    size_t bytes = 0;          // device bytes the class's worlds touch in a step
+    size_t chunk_budget = 0;   // largest chunk in bytes (0: the whole class is one chunk)
+    std::vector<Chunk> chunks;
 };
+
+// Default chunk budget: worlds are grouped so that each chunk touches at most this many bytes per
+// step, well inside the 129 MB L2 (the autotuner also tries larger and smaller budgets).
+constexpr size_t DEFAULT_CHUNK_BUDGET = 64ull << 20;
 
 struct WorldBuffers {
     ColItem* d_col = nullptr;  // this world's column items (inspection, U fields)
@@ -359,6 +375,60 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
     return ok && cudaStreamWaitEvent(s, ctx->ev_join, 0) == cudaSuccess;
 }
 
+// `steps` steps of one size class, chunk after chunk, with the given launch variants.
+int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const std::vector<Chunk>& chunks, int var_col, int var_row,
+                  int steps, cudaStream_t s) {
+    for (const Chunk& ch : chunks) {
+        for (int st = 0; st < steps; st++) {
+            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, var_col, s);
+            if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
+            ok = launch_row_fp32(cl.W, var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0, ch.nrow,
+                                 cl.planes, ctx->d_tw, s);
+            if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
+        }
+    }
+    return 0;
+}
+
+// Device bytes world w touches in one step: state, half-spectra, convolved spectra, kernel spectra.
+size_t world_step_bytes(const LeniaWorldDesc& d) {
+    const size_t cells = (size_t)d.width * d.height;
+    const size_t spec = cells * 4;  // W/2 x H complex f32
+    const size_t conv = (d.channels == 1 && d.nkernels == 1) ? 0 : spec * d.nkernels;
+    const size_t khat = (size_t)(d.width / 2 + 1) * khat_stride(d.height) * 4 * d.nkernels;
+    return cells * 4 * d.channels + spec * d.channels + conv + khat;
+}
+
+// Split a class into runs of consecutive worlds of at most `budget` bytes each, as even in world
+// count as the budget allows (budget 0: one chunk).
+std::vector<Chunk> make_chunks(const LeniaCtx* ctx, const SizeClass& cl, size_t budget) {
+    const int n = (int)cl.worlds.size();
+    int nchunks = 1;
+    if (budget > 0 && cl.bytes > budget) nchunks = (int)std::min<size_t>((size_t)n, (cl.bytes + budget - 1) / budget);
+    std::vector<Chunk> out;
+    int col = 0, tcg = 0, row = 0, w = 0;
+    for (int c = 0; c < nchunks; c++) {
+        const int wend = (int)(((long long)(c + 1) * n) / nchunks);
+        Chunk ch;
+        ch.col0 = col;
+        ch.tcg0 = tcg;
+        ch.row0 = row;
+        for (; w < wend; w++) {
+            const int wi = cl.worlds[w];
+            const WorldBuffers& b = ctx->wb[wi];
+            ch.ncol += b.ncol;
+            ch.ntcg += b.ntcg;
+            ch.nrow += b.nrow;
+            ch.bytes += world_step_bytes(ctx->desc[wi]);
+        }
+        col += ch.ncol;
+        tcg += ch.ntcg;
+        row += ch.nrow;
+        if (ch.ncol + ch.ntcg + ch.nrow > 0) out.push_back(ch);
+    }
+    return out;
+}
+
 // Enqueue `steps` steps of every world on the context's streams (captured into graphs).
 int enqueue_steps(LeniaCtx* ctx, int steps) {
     if (ctx->path == LENIA_PATH_RADIX2) {
@@ -367,18 +437,14 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
         CK(cudaGetLastError());
         return 0;
     }
-    // Size classes one after another, each for all its steps: a class's half-spectrum then stays in
-    // L2 between its column and row passes.  Measured on the 384-world batched workload, this order
-    // is 6% faster than running the classes as concurrent graph branches.
+    // Size classes one after another, and within a class its chunks one after another, each chunk for
+    // all its steps: a chunk's states and spectra then stay in L2 across its generations.  Measured on
+    // the 384-world batched workload, running the classes one after another was 6% faster than
+    // running them as concurrent graph branches.
     cudaStream_t s = ctx->stream;
     for (auto& cl : ctx->classes) {
-        for (int st = 0; st < steps; st++) {
-            bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, cl.var_col, s);
-            if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
-            ok = launch_row_fp32(cl.W, cl.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
-                                 ctx->d_tw, s);
-            if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
-        }
+        int rc = enqueue_class(ctx, cl, cl.chunks, cl.var_col, cl.var_row, steps, s);
+        if (rc) return rc;
     }
     CK(cudaGetLastError());
     return 0;
@@ -599,6 +665,7 @@ int setup_fused(LeniaCtx* ctx) {
         }
         // per-world slices of the class lists
         size_t co = 0, ro = 0, go = 0;
+        cl.bytes = 0;
         for (int wi : cl.worlds) {
             WorldBuffers& b = ctx->wb[wi];
             b.d_col = cl.d_col + co;
@@ -607,7 +674,10 @@ int setup_fused(LeniaCtx* ctx) {
             co += b.ncol;
             ro += b.nrow;
             go += b.ntcg;
+            cl.bytes += world_step_bytes(ctx->desc[wi]);
         }
+        cl.chunk_budget = DEFAULT_CHUNK_BUDGET;
+        cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
             if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
@@ -672,6 +742,55 @@ int setup_radix2(LeniaCtx* ctx) {
 }
 
 float* state_ptr(LeniaCtx* ctx, int w) { return ctx->path == LENIA_PATH_RADIX2 ? ctx->r2[w].state : ctx->hw[w].state; }
+
+// Device time of `steps` steps of one size class in the graph's order (chunk after chunk, each for
+// all its steps), split into its column and row launches: events around every launch, one
+// synchronisation at the end.  var_col / var_row / chunks as given (the autotuner's candidates).
+struct EventList {
+    std::vector<cudaEvent_t> e;
+    ~EventList() {
+        for (cudaEvent_t x : e) cudaEventDestroy(x);
+    }
+};
+int time_class(LeniaCtx* ctx, const SizeClass& cl, const std::vector<Chunk>& chunks, int var_col, int var_row, int steps,
+               double* col_ms, double* row_ms) {
+    EventList ev;
+    const size_t n = 1 + 2 * chunks.size() * (size_t)steps;
+    ev.e.reserve(n);
+    for (size_t i = 0; i < n; i++) {
+        cudaEvent_t x;
+        CK(cudaEventCreate(&x));
+        ev.e.push_back(x);
+    }
+    size_t k = 0;
+    CK(cudaEventRecord(ev.e[k++], ctx->stream));
+    for (const Chunk& ch : chunks) {
+        for (int st = 0; st < steps; st++) {
+            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, var_col, ctx->stream);
+            CK(cudaEventRecord(ev.e[k++], ctx->stream));
+            ok = ok && launch_row_fp32(cl.W, var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0, ch.nrow,
+                                       cl.planes, ctx->d_tw, ctx->stream);
+            CK(cudaEventRecord(ev.e[k++], ctx->stream));
+            if (!ok) {
+                cudaStreamSynchronize(ctx->stream);
+                cudaGetLastError();
+                return fail(ctx, LENIA_ECUDA, "launch failed for %dx%d", cl.W, cl.H);
+            }
+        }
+    }
+    CK(cudaEventSynchronize(ev.e[k - 1]));
+    double c = 0, r = 0;
+    for (size_t i = 1; i < k; i += 2) {
+        float a = 0, b = 0;
+        CK(cudaEventElapsedTime(&a, ev.e[i - 1], ev.e[i]));
+        CK(cudaEventElapsedTime(&b, ev.e[i], ev.e[i + 1]));
+        c += a;
+        r += b;
+    }
+    *col_ms = c;
+    *row_ms = r;
+    return 0;
+}
 
 }  // namespace
 
@@ -1129,33 +1248,42 @@ int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
         ctx->tick += steps;
         return 0;
     }
-    // time every class's column and row launches on the context stream, serially
-    Events evs;
-    cudaEvent_t* ev = evs.e;
-    for (int i = 0; i < 3; i++) CK(cudaEventCreate(&ev[i]));
+    // every class's column and row launches on the context stream, in the graph's order
     double col_ms = 0, row_ms = 0;
-    for (uint32_t s = 0; s < steps; s++) {
-        for (auto& cl : ctx->classes) {
-            CK(cudaEventRecord(ev[0], ctx->stream));
-            bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, cl.var_col, ctx->stream);
-            CK(cudaEventRecord(ev[1], ctx->stream));
-            ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow, cl.planes,
-                                       ctx->d_tw, ctx->stream);
-            CK(cudaEventRecord(ev[2], ctx->stream));
-            if (!ok) return fail(ctx, LENIA_ECUDA, "profile launch failed");
-            CK(cudaEventSynchronize(ev[2]));
-            float a = 0, b = 0;
-            cudaEventElapsedTime(&a, ev[0], ev[1]);
-            cudaEventElapsedTime(&b, ev[1], ev[2]);
-            col_ms += a;
-            row_ms += b;
-        }
+    for (auto& cl : ctx->classes) {
+        double c = 0, r = 0;
+        int rc = time_class(ctx, cl, cl.chunks, cl.var_col, cl.var_row, (int)steps, &c, &r);
+        if (rc) return rc;
+        col_ms += c;
+        row_ms += r;
     }
     out3[0] = (float)(col_ms / steps);
     out3[1] = (float)(row_ms / steps);
     out3[2] = (float)((col_ms + row_ms) / steps);
     ctx->tick += steps;
     return 0;
+}
+
+int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t count, size_t* nclasses) {
+    if (!ctx || !nclasses) return LENIA_EINVAL;
+    *nclasses = ctx->classes.size();
+    if (!out) return 0;
+    if (steps == 0 || count < 4 * ctx->classes.size()) return fail(ctx, LENIA_EINVAL, "need steps > 0 and 4 floats per class");
+    if (ctx->path == LENIA_PATH_RADIX2) return fail(ctx, LENIA_ESTATE, "the radix-2 path has no size classes");
+    int frc = flush_spectra(ctx);
+    if (frc) return frc;
+    for (size_t c = 0; c < ctx->classes.size(); c++) {
+        const SizeClass& cl = ctx->classes[c];
+        double col_ms = 0, row_ms = 0;
+        int rc = time_class(ctx, cl, cl.chunks, cl.var_col, cl.var_row, (int)steps, &col_ms, &row_ms);
+        if (rc) return rc;
+        out[4 * c] = (float)cl.W;
+        out[4 * c + 1] = (float)cl.H;
+        out[4 * c + 2] = (float)(col_ms / steps);
+        out[4 * c + 3] = (float)(row_ms / steps);
+    }
+    ctx->tick += steps;
+    return tc_check_error(ctx->tc, &ctx->err);
 }
 
 int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, uint32_t height, float* out, size_t count) {
@@ -1214,6 +1342,41 @@ int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t
     return 0;
 }
 
+int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib) {
+    if (!ctx) return LENIA_EINVAL;
+    if (mib > (1u << 20)) return fail(ctx, LENIA_EINVAL, "chunk budget above 1 TiB");
+    if (ctx->path == LENIA_PATH_RADIX2) return 0;  // no size classes
+    for (auto& cl : ctx->classes) {
+        cl.chunk_budget = (size_t)mib << 20;
+        cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses) {
+    if (!ctx || !nclasses) return LENIA_EINVAL;
+    *nclasses = ctx->classes.size();
+    if (!out) return 0;
+    if (count < 8 * ctx->classes.size()) return LENIA_EINVAL;
+    for (size_t i = 0; i < ctx->classes.size(); i++) {
+        const auto& cl = ctx->classes[i];
+        int32_t* o = out + 8 * i;
+        o[0] = cl.W;
+        o[1] = cl.H;
+        o[2] = cl.var_col;
+        o[3] = cl.var_row;
+        o[4] = (int32_t)cl.chunks.size();
+        o[5] = (int32_t)cl.worlds.size();
+        o[6] = (int32_t)(cl.chunk_budget >> 20);
+        o[7] = row_item_rows(cl.W, cl.general);
+    }
+    return 0;
+}
+
 int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) {
     if (!ctx) return LENIA_EINVAL;
     if (col_variant < -1 || col_variant > 2 || row_variant < -1 || row_variant > 1)
@@ -1231,6 +1394,46 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
     return 0;
 }
 
+// The autotuner's search, on states it may advance: for every size class, every chunk budget that
+// gives a different number of chunks, and every pair of column and row launch variants, the time of
+// a few steps in the graph's order.  A class keeps its current choice unless another is at least 3%
+// faster, so that timing noise does not flip it.
+static int autotune_search(LeniaCtx* ctx) {
+    const size_t budgets[] = {0, 96ull << 20, 64ull << 20, 40ull << 20, 24ull << 20, 12ull << 20};
+    constexpr int NVC = 3, NVR = 2, WARM = 2, REPS = 8;
+    for (auto& cl : ctx->classes) {
+        std::vector<std::pair<size_t, std::vector<Chunk>>> cands;
+        for (size_t b : budgets) {
+            std::vector<Chunk> ch = make_chunks(ctx, cl, b);
+            bool seen = false;
+            for (auto& c : cands) seen = seen || c.second.size() == ch.size();
+            if (!seen) cands.push_back({b, ch});
+        }
+        double cur = 0, best = 1e300;
+        size_t best_budget = cl.chunk_budget;
+        int best_vc = cl.var_col, best_vr = cl.var_row;
+        for (auto& cand : cands) {
+            for (int vc = 0; vc < NVC; vc++)
+                for (int vr = 0; vr < NVR; vr++) {
+                    double c = 0, r = 0;
+                    int rc = time_class(ctx, cl, cand.second, vc, vr, WARM, &c, &r);
+                    if (!rc) rc = time_class(ctx, cl, cand.second, vc, vr, REPS, &c, &r);
+                    if (rc) return rc;
+                    const double t = c + r;
+                    if (cand.second.size() == cl.chunks.size() && vc == cl.var_col && vr == cl.var_row) cur = t;
+                    if (t < best) best = t, best_budget = cand.first, best_vc = vc, best_vr = vr;
+                }
+        }
+        if (cur == 0 || best < 0.97 * cur) {
+            cl.chunk_budget = best_budget;
+            cl.var_col = best_vc;
+            cl.var_row = best_vr;
+            cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
+        }
+    }
+    return 0;
+}
+
 int lenia_autotune(LeniaCtx* ctx) {
     if (!ctx) return LENIA_EINVAL;
     if (ctx->path == LENIA_PATH_RADIX2) return 0;
@@ -1238,86 +1441,37 @@ int lenia_autotune(LeniaCtx* ctx) {
         int frc = flush_spectra(ctx);
         if (frc) return frc;
     }
-    // Time every built variant of each class's column and row launches; keep the fastest.
-    // The trial steps advance the worlds, so every state is saved to a device buffer and restored.
+    // The trial steps advance the worlds, so every state is saved to a device buffer first and
+    // restored afterwards, also when the search fails.
     size_t total = 0;
     for (const auto& d : ctx->desc) total += state_count(d);
     DeviceBuffer save_buf;
     CK(cudaMalloc(&save_buf.p, total * sizeof(float)));
     float* saved = static_cast<float*>(save_buf.p);
-    {
+    auto copy_states = [&](bool restore) -> cudaError_t {
         size_t off = 0;
         for (size_t w = 0; w < ctx->desc.size(); w++) {
             const size_t n = state_count(ctx->desc[w]);
-            if (!ctx->states || w == 0)
-                CK(cudaMemcpyAsync(saved + off, state_ptr(ctx, (int)w), (ctx->states ? total : n) * sizeof(float),
-                                   cudaMemcpyDeviceToDevice, ctx->stream));
-            off += n;
-        }
-    }
-    Events ev;
-    CK(cudaEventCreate(&ev.e[0]));
-    CK(cudaEventCreate(&ev.e[1]));
-    cudaEvent_t a = ev.e[0], b = ev.e[1];
-    const int reps = 5;
-    // column variants: scalar at 64 and 128 registers, paired; row variants: 64 and 128 registers
-    constexpr int NVC = 3, NVR = 2;
-    for (auto& cl : ctx->classes) {
-        float tcol[NVC], trow[NVR];
-        for (int which = 0; which < NVC; which++) {
-            const bool row = which < NVR;
-            float t_col = 0, t_row = 0;
-            for (int r = 0; r < reps + 1; r++) {
-                CK(cudaEventRecord(a, ctx->stream));
-                bool ok = launch_columns(ctx, cl, cl.d_col, cl.ncol, cl.d_tcg, cl.ntcg, which, ctx->stream);
-                CK(cudaEventRecord(b, ctx->stream));
-                CK(cudaEventSynchronize(b));
-                float ms = 0;
-                cudaEventElapsedTime(&ms, a, b);
-                if (r) t_col += ms;
-                if (row) {
-                    CK(cudaEventRecord(a, ctx->stream));
-                    ok = ok && launch_row_fp32(cl.W, which, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, cl.nrow,
-                                               cl.planes, ctx->d_tw, ctx->stream);
-                    CK(cudaEventRecord(b, ctx->stream));
-                    CK(cudaEventSynchronize(b));
-                    cudaEventElapsedTime(&ms, a, b);
-                    if (r) t_row += ms;
-                }
-                if (!ok) {
-                    cudaGetLastError();
-                    t_col = t_row = 1e30f;
-                    break;
-                }
+            if (!ctx->states || w == 0) {
+                float* dev = state_ptr(ctx, (int)w);
+                const size_t cnt = (ctx->states ? total : n) * sizeof(float);
+                cudaError_t e = restore ? cudaMemcpyAsync(dev, saved + off, cnt, cudaMemcpyDeviceToDevice, ctx->stream)
+                                        : cudaMemcpyAsync(saved + off, dev, cnt, cudaMemcpyDeviceToDevice, ctx->stream);
+                if (e != cudaSuccess) return e;
             }
-            tcol[which] = t_col;
-            if (row) trow[which] = t_row;
-        }
-        // the default variant stays unless another is at least 3% faster, so that timing noise does
-        // not flip the choice
-        auto choose = [](const float* t, int n, int cur) {
-            int best = cur;
-            for (int i = 0; i < n; i++)
-                if (t[i] < t[best]) best = i;
-            return t[best] < 0.97f * t[cur] ? best : cur;
-        };
-        cl.var_col = choose(tcol, NVC, cl.var_col);
-        cl.var_row = choose(trow, NVR, cl.var_row);
-    }
-    {
-        size_t off = 0;
-        for (size_t w = 0; w < ctx->desc.size(); w++) {
-            const size_t n = state_count(ctx->desc[w]);
-            if (!ctx->states || w == 0)
-                CK(cudaMemcpyAsync(state_ptr(ctx, (int)w), saved + off, (ctx->states ? total : n) * sizeof(float),
-                                   cudaMemcpyDeviceToDevice, ctx->stream));
-            refresh_spectrum(ctx, (int)w);
             off += n;
         }
-    }
-    CK(cudaStreamSynchronize(ctx->stream));
-    int rc = rebuild_graphs(ctx);
+        return cudaSuccess;
+    };
+    CK(copy_states(false));
+    const int rc = autotune_search(ctx);
+    const cudaError_t e = copy_states(true);
+    for (size_t w = 0; w < ctx->desc.size(); w++) refresh_spectrum(ctx, (int)w);
     if (rc) return rc;
+    CK(e);
+    CK(cudaStreamSynchronize(ctx->stream));
+    int grc = rebuild_graphs(ctx);
+    if (grc) return grc;
     CK(cudaStreamSynchronize(ctx->stream));
     return 0;
 }

@@ -198,6 +198,20 @@ class Sim:
         self._check(self._L.lenia_class_variants(self._ctx, out, 4 * n.value, ctypes.byref(n)))
         return {(out[4 * i], out[4 * i + 1]): (out[4 * i + 2], out[4 * i + 3]) for i in range(n.value)}
 
+    def shapes(self):
+        """{(width, height): {...}} for every size class: launch variants, chunks (L2-resident runs of
+        worlds), worlds, chunk budget (MiB, 0 = one chunk) and rows per row-pass item."""
+        n = ctypes.c_size_t(0)
+        self._check(self._L.lenia_class_shapes(self._ctx, None, 0, ctypes.byref(n)))
+        out = (ctypes.c_int32 * (8 * n.value))()
+        self._check(self._L.lenia_class_shapes(self._ctx, out, 8 * n.value, ctypes.byref(n)))
+        keys = ("column_variant", "row_variant", "chunks", "worlds", "chunk_budget_mib", "rows_per_row_item")
+        return {(out[8 * i], out[8 * i + 1]): dict(zip(keys, out[8 * i + 2:8 * i + 8])) for i in range(n.value)}
+
+    def set_chunk_budget(self, mib: int):
+        """Pin every size class's chunk budget in MiB (see lenia_set_chunk_budget); 0 = one chunk."""
+        self._check(self._L.lenia_set_chunk_budget(self._ctx, int(mib)))
+
     def set_variants(self, column: int = -1, row: int = -1):
         """Pin every size class's launch variants (see lenia_set_variants); -1 keeps one."""
         self._check(self._L.lenia_set_variants(self._ctx, int(column), int(row)))
@@ -207,3 +221,12 @@ class Sim:
         out = np.zeros(3, np.float32)
         self._check(self._L.lenia_profile_step(self._ctx, int(steps), fptr(out)))
         return out
+
+    def profile_classes(self, steps: int = 5):
+        """Per size class: {(width, height): (column ms, row ms)} per step, each class timed alone."""
+        n = ctypes.c_size_t()
+        self._check(self._L.lenia_profile_classes(self._ctx, int(steps), None, 0, ctypes.byref(n)))
+        out = np.zeros(4 * n.value, np.float32)
+        self._check(self._L.lenia_profile_classes(self._ctx, int(steps), fptr(out), out.size, ctypes.byref(n)))
+        return {(int(out[4 * i]), int(out[4 * i + 1])): (float(out[4 * i + 2]), float(out[4 * i + 3]))
+                for i in range(n.value)}

@@ -435,8 +435,12 @@ def run_ours(args, dist):
     seed_all(sim, worlds, seeds)
     if not args.no_autotune:
         sim.autotune()  # the engine's autotuner: times every launch variant per size class
-    # launch variant per size class (column: 0/1 scalar at 64/128 registers, 2 paired; row: 0/1)
-    variants = {"%dx%d" % wh: {"column": v[0], "row": v[1]} for wh, v in sim.variants().items()}
+    # launch shape per size class after autotuning: variants (column: 0/1 scalar at 64/128 registers,
+    # 2 paired; row: 0/1), chunks of worlds run back to back through L2, rows per row item
+    variants = {"%dx%d" % wh: {"column": v["column_variant"], "row": v["row_variant"], "chunks": v["chunks"],
+                               "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
+                               "rows_per_row_item": v["rows_per_row_item"]}
+                for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step
     for _ in range(args.warmup):
@@ -460,6 +464,19 @@ def run_ours(args, dist):
     # per-kernel breakdown (event-timed launches on the engine stream, right after the timed region)
     prof = sim.profile(5)
     col_ms, row_ms, step_ms = [float(x) for x in prof]
+    # per size class: its launches timed alone, and its cell-updates/s at that time
+    class_cells = {}
+    for w in worlds:
+        class_cells[(w.width, w.height)] = class_cells.get((w.width, w.height), 0) + w.channels * w.width * w.height
+    classes = {}
+    if len(class_cells) > 1 and args.path != "radix2":
+        for (cw, ch), (cms, rms) in sorted(sim.profile_classes(3).items()):
+            n = class_cells[(cw, ch)]
+            v = variants.get("%dx%d" % (cw, ch), {})
+            classes["%dx%d" % (cw, ch)] = {"worlds": sum(1 for w in worlds if (w.width, w.height) == (cw, ch)),
+                                           "column_ms": cms, "row_ms": rms,
+                                           "cell_updates_per_s": n / ((cms + rms) * 1e-3) if cms + rms > 0 else None,
+                                           "launch_variant": v}
     nclasses = len({(w.width, w.height) for w in worlds})
     # per size class and generation: one column and one row launch; the tensor-core paths add the
     # FP32 column launch for each channel's first tile group (sizes 256..4096)
@@ -596,7 +613,7 @@ def run_ours(args, dist):
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches_per_gen * G * args.steps,
-               "launch_variants": variants,
+               "launch_variants": variants, "classes": classes,
                "paths": paths,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
         print(json.dumps(out))

@@ -176,7 +176,10 @@ LENIA_API int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel,
 LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
 
 /* Autotuner: times the candidate launch shapes of every size class on this context's worlds
- * and keeps the fastest.  Rebuilds the step graphs.  Optional; defaults are reasonable. */
+ * and keeps the fastest: every pair of column and row launch variants, under every chunk budget
+ * (worlds per L2-resident run, see lenia_class_shapes) that changes the class's number of chunks.
+ * The states are saved first and restored afterwards, also when it fails.  Rebuilds the step
+ * graphs.  Optional; defaults are reasonable. */
 LENIA_API int lenia_autotune(LeniaCtx* ctx);
 
 /* Pins the launch variant of every size class, in place of the defaults or the autotuner's
@@ -188,6 +191,17 @@ LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row
 /* The size classes and their current launch variants: *nclasses = the number of classes; with
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
 LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
+/* The launch shape of every size class, as the autotuner left it: *nclasses = the number of classes;
+ * with `out` (count >= 8 * classes) eight int32 per class: width, height, column variant, row
+ * variant, chunks, worlds, chunk budget in MiB (0: the class is one chunk), rows per row-pass item.
+ * A chunk is a run of the class's worlds that the step graph advances through all of its steps
+ * before the next run starts, sized so that its states and spectra stay in L2. */
+LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
+/* Pins the chunk budget of every size class, in place of the default (64 MiB) or the autotuner's
+ * choice: a class is split into runs of consecutive worlds of at most `mib` MiB of per-step data each
+ * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
+ * Rebuilds the step graphs.  No reference counterpart. */
+LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
 
 /* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
  * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.
@@ -262,6 +276,11 @@ LENIA_API int lenia_mlp_predict(LeniaMlp* mlp, const float* x, uint32_t count, f
 /* Event-timed average device time of the dominant launches of one step, in milliseconds:
  * out[0] = column passes, out[1] = row passes, out[2] = whole step.  Runs `steps` steps. */
 LENIA_API int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3);
+/* The same per size class: *nclasses = the number of classes; with `out` (count >= 4 * classes)
+ * four floats per class: width, height, column-pass ms and row-pass ms, each the event-timed
+ * average over `steps` steps of that class alone (its launches one after another, every other
+ * class idle).  Advances every class by `steps`. */
+LENIA_API int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t count, size_t* nclasses);
 
 #ifdef __cplusplus
 }

@@ -427,3 +427,31 @@ def test_headless_view_matches_oracle(ref, palette, samples, scale, origin):
     want = ref.render(s, 200, 150, origin=origin, scale=scale, samples=samples, palette=palette)
     diff = np.abs(img.astype(int) - want.astype(int))
     assert diff.max() <= 1 and (diff > 0).mean() < 1e-3
+
+
+def test_chunked_classes_give_the_same_bits():
+    """Splitting size classes into L2-sized runs of worlds only regroups the launches: every world's
+    state after 6 steps is bit-identical with one run per class, with runs of a few worlds, and after
+    the autotuner's choice; the shapes report the chunking."""
+    worlds = configs.batched(64)
+    outs = []
+    for budget in (0, 8, 1):
+        with Sim(worlds, seed=0) as sim:
+            for i, w in enumerate(worlds):
+                sim.seed_patches(i, i, w.seed.patches)
+            sim.set_chunk_budget(budget)
+            shapes = sim.shapes()
+            if budget == 0:
+                assert all(v["chunks"] == 1 for v in shapes.values())
+            if budget == 1:  # every world of 512 and up is a chunk of its own
+                assert all(v["chunks"] == v["worlds"] for (w, h), v in shapes.items() if w >= 512)
+            sim.step(6)
+            outs.append(sim.read_states().copy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    with Sim(worlds, seed=0) as sim:
+        for i, w in enumerate(worlds):
+            sim.seed_patches(i, i, w.seed.patches)
+        sim.autotune()
+        sim.step(6)
+        got = sim.read_states()
+    assert np.abs(got - outs[0]).max() < 1e-5  # launch variants may differ in rounding
