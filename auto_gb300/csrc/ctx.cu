@@ -53,9 +53,12 @@ struct SizeClass {
     std::vector<Chunk> chunks;
 };
 
-// Default chunk budget: worlds are grouped so that each chunk touches at most this many bytes per
-// step, well inside the 129 MB L2 (the autotuner also tries larger and smaller budgets).
-constexpr size_t DEFAULT_CHUNK_BUDGET = 64ull << 20;
+// Default chunk budget: 0, every class is one chunk.  Chunks of up to 32 MiB do keep their worlds in
+// L2 (measured with ncu on the 55 worlds of 1024 x 1024: DRAM traffic 1.4 GB -> 23 MB per
+// generation), but the passes are not bound by HBM there, and launches over a few worlds fill the GPU
+// less: every budget measured slower (1024 x 1024: 1.91e11 cell-updates/s as one chunk, 1.75e11 in 8
+// chunks, 1.50e11 in 16).  The autotuner still tries budgets per class.
+constexpr size_t DEFAULT_CHUNK_BUDGET = 0;
 
 struct WorldBuffers {
     ColItem* d_col = nullptr;  // this world's column items (inspection, U fields)
@@ -375,14 +378,20 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
     return ok && cudaStreamWaitEvent(s, ctx->ev_join, 0) == cudaSuccess;
 }
 
-// `steps` steps of one size class, chunk after chunk, with the given launch variants.
-int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const std::vector<Chunk>& chunks, int var_col, int var_row,
-                  int steps, cudaStream_t s) {
-    for (const Chunk& ch : chunks) {
+// A launch shape of one size class: launch variants and chunks.
+struct Shape {
+    int var_col, var_row;
+    const std::vector<Chunk>* chunks;
+};
+Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, &cl.chunks}; }
+
+// `steps` steps of one size class, chunk after chunk, in the given launch shape.
+int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, cudaStream_t s) {
+    for (const Chunk& ch : *sh.chunks) {
         for (int st = 0; st < steps; st++) {
-            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, var_col, s);
+            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
-            ok = launch_row_fp32(cl.W, var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0, ch.nrow,
+            ok = launch_row_fp32(cl.W, sh.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0, ch.nrow,
                                  cl.planes, ctx->d_tw, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
         }
@@ -443,7 +452,7 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
     // running them as concurrent graph branches.
     cudaStream_t s = ctx->stream;
     for (auto& cl : ctx->classes) {
-        int rc = enqueue_class(ctx, cl, cl.chunks, cl.var_col, cl.var_row, steps, s);
+        int rc = enqueue_class(ctx, cl, shape_of(cl), steps, s);
         if (rc) return rc;
     }
     CK(cudaGetLastError());
@@ -752,8 +761,8 @@ struct EventList {
         for (cudaEvent_t x : e) cudaEventDestroy(x);
     }
 };
-int time_class(LeniaCtx* ctx, const SizeClass& cl, const std::vector<Chunk>& chunks, int var_col, int var_row, int steps,
-               double* col_ms, double* row_ms) {
+int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, double* col_ms, double* row_ms) {
+    const std::vector<Chunk>& chunks = *sh.chunks;
     EventList ev;
     const size_t n = 1 + 2 * chunks.size() * (size_t)steps;
     ev.e.reserve(n);
@@ -766,10 +775,11 @@ int time_class(LeniaCtx* ctx, const SizeClass& cl, const std::vector<Chunk>& chu
     CK(cudaEventRecord(ev.e[k++], ctx->stream));
     for (const Chunk& ch : chunks) {
         for (int st = 0; st < steps; st++) {
-            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, var_col, ctx->stream);
+            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col,
+                                     ctx->stream);
             CK(cudaEventRecord(ev.e[k++], ctx->stream));
-            ok = ok && launch_row_fp32(cl.W, var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0, ch.nrow,
-                                       cl.planes, ctx->d_tw, ctx->stream);
+            ok = ok && launch_row_fp32(cl.W, sh.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0,
+                                       ch.nrow, cl.planes, ctx->d_tw, ctx->stream);
             CK(cudaEventRecord(ev.e[k++], ctx->stream));
             if (!ok) {
                 cudaStreamSynchronize(ctx->stream);
@@ -1252,7 +1262,7 @@ int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3) {
     double col_ms = 0, row_ms = 0;
     for (auto& cl : ctx->classes) {
         double c = 0, r = 0;
-        int rc = time_class(ctx, cl, cl.chunks, cl.var_col, cl.var_row, (int)steps, &c, &r);
+        int rc = time_class(ctx, cl, shape_of(cl), (int)steps, &c, &r);
         if (rc) return rc;
         col_ms += c;
         row_ms += r;
@@ -1275,7 +1285,7 @@ int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t coun
     for (size_t c = 0; c < ctx->classes.size(); c++) {
         const SizeClass& cl = ctx->classes[c];
         double col_ms = 0, row_ms = 0;
-        int rc = time_class(ctx, cl, cl.chunks, cl.var_col, cl.var_row, (int)steps, &col_ms, &row_ms);
+        int rc = time_class(ctx, cl, shape_of(cl), (int)steps, &col_ms, &row_ms);
         if (rc) return rc;
         out[4 * c] = (float)cl.W;
         out[4 * c + 1] = (float)cl.H;
@@ -1394,41 +1404,58 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
     return 0;
 }
 
-// The autotuner's search, on states it may advance: for every size class, every chunk budget that
-// gives a different number of chunks, and every pair of column and row launch variants, the time of
-// a few steps in the graph's order.  A class keeps its current choice unless another is at least 3%
-// faster, so that timing noise does not flip it.
+// The autotuner's search, on states it may advance.  For every size class, in turn: every pair of
+// column and row launch variants, then every chunk budget that gives a different number of chunks.
+// Each candidate is timed over a few steps in the graph's order, and a class keeps its current
+// choice of a dimension unless another is at least 3% faster, so that timing noise does not flip it.
 static int autotune_search(LeniaCtx* ctx) {
-    const size_t budgets[] = {0, 96ull << 20, 64ull << 20, 40ull << 20, 24ull << 20, 12ull << 20};
-    constexpr int NVC = 3, NVR = 2, WARM = 2, REPS = 8;
+    const size_t budgets[] = {0, 128ull << 20, 96ull << 20, 64ull << 20, 32ull << 20};
+    constexpr int WARM = 2, REPS = 8;
     for (auto& cl : ctx->classes) {
-        std::vector<std::pair<size_t, std::vector<Chunk>>> cands;
-        for (size_t b : budgets) {
-            std::vector<Chunk> ch = make_chunks(ctx, cl, b);
-            bool seen = false;
-            for (auto& c : cands) seen = seen || c.second.size() == ch.size();
-            if (!seen) cands.push_back({b, ch});
+        auto timed = [&](const Shape& sh, double* t) {
+            double c = 0, r = 0;
+            int rc = time_class(ctx, cl, sh, WARM, &c, &r);
+            if (!rc) rc = time_class(ctx, cl, sh, REPS, &c, &r);
+            *t = c + r;
+            return rc;
+        };
+        // pick among candidate shapes; the first candidate is the current shape
+        auto pick = [&](std::vector<Shape>& cands, int* best_i) {
+            std::vector<double> t(cands.size());
+            for (size_t i = 0; i < cands.size(); i++) {
+                int rc = timed(cands[i], &t[i]);
+                if (rc) return rc;
+            }
+            int b = 0;
+            for (size_t i = 1; i < cands.size(); i++)
+                if (t[i] < t[b]) b = (int)i;
+            *best_i = t[b] < 0.97 * t[0] ? b : 0;
+            return 0;
+        };
+        int bi = 0, rc = 0;
+        {
+            std::vector<Shape> c{shape_of(cl)};
+            for (int vc = 0; vc < 3; vc++)
+                for (int vr = 0; vr < 2; vr++)
+                    if (vc != cl.var_col || vr != cl.var_row) c.push_back(Shape{vc, vr, &cl.chunks});
+            if ((rc = pick(c, &bi))) return rc;
+            cl.var_col = c[bi].var_col;
+            cl.var_row = c[bi].var_row;
         }
-        double cur = 0, best = 1e300;
-        size_t best_budget = cl.chunk_budget;
-        int best_vc = cl.var_col, best_vr = cl.var_row;
-        for (auto& cand : cands) {
-            for (int vc = 0; vc < NVC; vc++)
-                for (int vr = 0; vr < NVR; vr++) {
-                    double c = 0, r = 0;
-                    int rc = time_class(ctx, cl, cand.second, vc, vr, WARM, &c, &r);
-                    if (!rc) rc = time_class(ctx, cl, cand.second, vc, vr, REPS, &c, &r);
-                    if (rc) return rc;
-                    const double t = c + r;
-                    if (cand.second.size() == cl.chunks.size() && vc == cl.var_col && vr == cl.var_row) cur = t;
-                    if (t < best) best = t, best_budget = cand.first, best_vc = vc, best_vr = vr;
-                }
-        }
-        if (cur == 0 || best < 0.97 * cur) {
-            cl.chunk_budget = best_budget;
-            cl.var_col = best_vc;
-            cl.var_row = best_vr;
-            cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
+        {
+            std::vector<std::vector<Chunk>> lists{cl.chunks};
+            std::vector<size_t> bud{cl.chunk_budget};
+            for (size_t b : budgets) {
+                std::vector<Chunk> ch = make_chunks(ctx, cl, b);
+                bool seen = false;
+                for (auto& l : lists) seen = seen || l.size() == ch.size();
+                if (!seen) lists.push_back(ch), bud.push_back(b);
+            }
+            std::vector<Shape> c;
+            for (auto& l : lists) c.push_back(Shape{cl.var_col, cl.var_row, &l});
+            if ((rc = pick(c, &bi))) return rc;
+            cl.chunk_budget = bud[bi];
+            cl.chunks = lists[bi];
         }
     }
     return 0;

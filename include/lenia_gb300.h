@@ -176,8 +176,9 @@ LENIA_API int lenia_read_spectrum(LeniaCtx* ctx, int32_t world, int32_t channel,
 LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
 
 /* Autotuner: times the candidate launch shapes of every size class on this context's worlds
- * and keeps the fastest: every pair of column and row launch variants, under every chunk budget
- * (worlds per L2-resident run, see lenia_class_shapes) that changes the class's number of chunks.
+ * and keeps the fastest, one dimension after another: the pair of column and row launch variants,
+ * then every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that changes the
+ * class's number of chunks.
  * The states are saved first and restored afterwards, also when it fails.  Rebuilds the step
  * graphs.  Optional; defaults are reasonable. */
 LENIA_API int lenia_autotune(LeniaCtx* ctx);
@@ -197,7 +198,7 @@ LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t cou
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
-/* Pins the chunk budget of every size class, in place of the default (64 MiB) or the autotuner's
+/* Pins the chunk budget of every size class, in place of the default (0) or the autotuner's
  * choice: a class is split into runs of consecutive worlds of at most `mib` MiB of per-step data each
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */

@@ -431,8 +431,8 @@ def test_headless_view_matches_oracle(ref, palette, samples, scale, origin):
 
 def test_chunked_classes_give_the_same_bits():
     """Splitting size classes into L2-sized runs of worlds only regroups the launches: every world's
-    state after 6 steps is bit-identical with one run per class, with runs of a few worlds, and after
-    the autotuner's choice; the shapes report the chunking."""
+    state after 6 steps is bit-identical with one run per class and with runs of a few worlds, and
+    within rounding after the autotuner's choice; the shapes report the chunking."""
     worlds = configs.batched(64)
     outs = []
     for budget in (0, 8, 1):
