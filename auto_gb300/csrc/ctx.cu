@@ -51,6 +51,10 @@ struct SizeClass {
     size_t bytes = 0;          // device bytes the class's worlds touch in a step
     size_t chunk_budget = 0;   // largest chunk in bytes (0: the whole class is one chunk)
     std::vector<Chunk> chunks;
+    // cluster-resident step (resident.cu): possible for square one-channel, one-kernel Lenia classes
+    // of 128..512 on the FP32 path; `resident` selects it over the two launches per generation
+    int resident_ok = 0, resident = 0;
+    int* d_world_ids = nullptr;
 };
 
 // Default chunk budget: 0, every class is one chunk.  Chunks of up to 32 MiB do keep their worlds in
@@ -116,6 +120,8 @@ struct LeniaCtx {
     // all states back to back in world order (fused paths): one copy for every world
     float* states = nullptr;
     size_t states_count = 0;
+    // device error flag of the cluster-resident step (1: a cluster sync gave up)
+    int* d_flags = nullptr;
 };
 
 namespace {
@@ -385,8 +391,14 @@ struct Shape {
 };
 Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, &cl.chunks}; }
 
-// `steps` steps of one size class, chunk after chunk, in the given launch shape.
+// `steps` steps of one size class, chunk after chunk, in the given launch shape; a resident class is
+// one launch for all its worlds and steps.
 int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, cudaStream_t s) {
+    if (cl.resident) {
+        if (!launch_resident(cl.W, ctx->d_worlds, cl.d_world_ids, (int)cl.worlds.size(), steps, ctx->d_tw, ctx->d_flags, s))
+            return fail(ctx, LENIA_ECUDA, "resident launch failed (%dx%d)", cl.W, cl.H);
+        return 0;
+    }
     for (const Chunk& ch : *sh.chunks) {
         for (int st = 0; st < steps; st++) {
             bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col, s);
@@ -687,6 +699,16 @@ int setup_fused(LeniaCtx* ctx) {
         }
         cl.chunk_budget = DEFAULT_CHUNK_BUDGET;
         cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
+        // the cluster-resident step: square one-channel, one-kernel Lenia worlds of 128..512 on the
+        // FP32 path, where the GPU can hold at least one of its clusters
+        if (ctx->path == LENIA_PATH_FP32 && !general && cl.W == cl.H && resident_supported(cl.W) &&
+            resident_clusters_that_fit(cl.W) > 0) {
+            if ((rc = dalloc(ctx, &cl.d_world_ids, cl.worlds.size()))) return rc;
+            CK(cudaMemcpy(cl.d_world_ids, cl.worlds.data(), cl.worlds.size() * sizeof(int), cudaMemcpyHostToDevice));
+            cl.resident_ok = 1;
+            cl.resident = 1;
+        }
+        cudaGetLastError();
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
             if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
@@ -762,6 +784,22 @@ struct EventList {
     }
 };
 int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, double* col_ms, double* row_ms) {
+    if (cl.resident) {
+        // one launch: its whole time is reported as the column share
+        Events ev;
+        CK(cudaEventCreate(&ev.e[0]));
+        CK(cudaEventCreate(&ev.e[1]));
+        CK(cudaEventRecord(ev.e[0], ctx->stream));
+        int rc = enqueue_class(ctx, cl, sh, steps, ctx->stream);
+        CK(cudaEventRecord(ev.e[1], ctx->stream));
+        if (rc) return rc;
+        CK(cudaEventSynchronize(ev.e[1]));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, ev.e[0], ev.e[1]));
+        *col_ms = ms;
+        *row_ms = 0;
+        return 0;
+    }
     const std::vector<Chunk>& chunks = *sh.chunks;
     EventList ev;
     const size_t n = 1 + 2 * chunks.size() * (size_t)steps;
@@ -799,6 +837,20 @@ int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, d
     }
     *col_ms = c;
     *row_ms = r;
+    return 0;
+}
+
+// The device-side error flags of the context's kernels: the tensor-core passes' and the resident
+// step's (set when a bounded barrier wait gave up).  Reading them synchronises with the device.
+int check_device_errors(LeniaCtx* ctx) {
+    int rc = tc_check_error(ctx->tc, &ctx->err);
+    if (rc || !ctx->d_flags) return rc;
+    int h = 0;
+    CK(cudaMemcpy(&h, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+    if (h) {
+        CK(cudaMemset(ctx->d_flags, 0, sizeof(int)));
+        return fail(ctx, LENIA_ECUDA, "a cluster-resident step gave up waiting on a cluster sync; results of that step are invalid");
+    }
     return 0;
 }
 
@@ -887,6 +939,11 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         if (packed) ctx->states = ctx->hw[0].state, ctx->states_count = off;
     }
     if ((rc = dalloc(ctx, &ctx->d_stats, 3 * (size_t)nworlds))) return bail(rc);
+    if ((rc = dalloc(ctx, &ctx->d_flags, 1))) return bail(rc);
+    if (cudaMemset(ctx->d_flags, 0, sizeof(int)) != cudaSuccess) {
+        fail(ctx, LENIA_ECUDA, "flag initialisation failed");
+        return bail(LENIA_ECUDA);
+    }
     if ((rc = rebuild_graphs(ctx))) return bail(rc);
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
         fail(ctx, LENIA_ECUDA, "initialisation failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -941,7 +998,7 @@ int lenia_read_state(LeniaCtx* ctx, int32_t world, float* host, size_t count) {
     if (!host || count != state_count(ctx->desc[world])) return fail(ctx, LENIA_EINVAL, "bad count for world %d", world);
     CK(cudaMemcpyAsync(host, state_ptr(ctx, world), count * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
-    return tc_check_error(ctx->tc, &ctx->err);
+    return check_device_errors(ctx);
 }
 
 int lenia_read_state_device(LeniaCtx* ctx, int32_t world, float* dev, size_t count) {
@@ -987,7 +1044,7 @@ int lenia_read_states(LeniaCtx* ctx, float* host, size_t count) {
         }
     }
     CK(cudaStreamSynchronize(ctx->stream));
-    return tc_check_error(ctx->tc, &ctx->err);
+    return check_device_errors(ctx);
 }
 
 // Asynchronous whole-context state copies.  The host copy runs on the upload (download) stream
@@ -1056,7 +1113,7 @@ int lenia_step_timed(LeniaCtx* ctx, uint32_t steps, float* ms) {
     CK(cudaEventRecord(ev.e[1], ctx->stream));
     CK(cudaEventSynchronize(ev.e[1]));
     CK(cudaEventElapsedTime(ms, ev.e[0], ev.e[1]));
-    if (!rc) rc = tc_check_error(ctx->tc, &ctx->err);
+    if (!rc) rc = check_device_errors(ctx);
     return rc;
 }
 
@@ -1065,7 +1122,7 @@ int lenia_sync(LeniaCtx* ctx) {
     CK(cudaStreamSynchronize(ctx->stream));
     CK(cudaStreamSynchronize(ctx->up));
     CK(cudaStreamSynchronize(ctx->down));
-    int rc = tc_check_error(ctx->tc, &ctx->err);
+    int rc = check_device_errors(ctx);
     return rc;
 }
 
@@ -1293,7 +1350,7 @@ int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t coun
         out[4 * c + 3] = (float)(row_ms / steps);
     }
     ctx->tick += steps;
-    return tc_check_error(ctx->tc, &ctx->err);
+    return check_device_errors(ctx);
 }
 
 int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, uint32_t height, float* out, size_t count) {
@@ -1367,14 +1424,25 @@ int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib) {
     return 0;
 }
 
+int lenia_set_resident(LeniaCtx* ctx, int32_t on) {
+    if (!ctx) return LENIA_EINVAL;
+    if (on != 0 && on != 1) return fail(ctx, LENIA_EINVAL, "on must be 0 or 1");
+    for (auto& cl : ctx->classes) cl.resident = on && cl.resident_ok;
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
 int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses) {
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (count < 8 * ctx->classes.size()) return LENIA_EINVAL;
+    if (count < 9 * ctx->classes.size()) return LENIA_EINVAL;
     for (size_t i = 0; i < ctx->classes.size(); i++) {
         const auto& cl = ctx->classes[i];
-        int32_t* o = out + 8 * i;
+        int32_t* o = out + 9 * i;
         o[0] = cl.W;
         o[1] = cl.H;
         o[2] = cl.var_col;
@@ -1383,6 +1451,7 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
         o[5] = (int32_t)cl.worlds.size();
         o[6] = (int32_t)(cl.chunk_budget >> 20);
         o[7] = row_item_rows(cl.W, cl.general);
+        o[8] = cl.resident;
     }
     return 0;
 }
@@ -1433,6 +1502,20 @@ static int autotune_search(LeniaCtx* ctx) {
             return 0;
         };
         int bi = 0, rc = 0;
+        if (cl.resident_ok) {
+            // the cluster-resident step against the two-pass step in its current shape
+            double t_res = 0, t_two = 0;
+            const int was = cl.resident;
+            cl.resident = 1;
+            rc = timed(shape_of(cl), &t_res);
+            cl.resident = 0;
+            if (!rc) rc = timed(shape_of(cl), &t_two);
+            cl.resident = was;
+            if (rc) return rc;
+            const double t_cur = was ? t_res : t_two, t_other = was ? t_two : t_res;
+            if (t_other < 0.97 * t_cur) cl.resident = !was;
+            if (cl.resident) continue;  // launch variants and chunks do not apply to it
+        }
         {
             std::vector<Shape> c{shape_of(cl)};
             for (int vc = 0; vc < 3; vc++)

@@ -66,6 +66,16 @@ int row_item_rows(int W, int general);  // rows per row-pass item: 4, or 2 (gene
 int fp32_local_bytes(int row, int n, int variant);  // spill/stack bytes per thread of a pass instantiation
 int max_smem_optin();
 
+// Cluster-resident step (resident.cu): one launch advances every world of a square size class of
+// side N (128, 192, 256, 384 or 512; one channel, one Lenia kernel) `gens` generations, one
+// thread-block cluster of N/32 CTAs per world.  world_ids: the class's world indices (device).
+// err: a device int set to 1 if a cluster sync gave up.  A zero-world call only configures the
+// kernel (outside any stream capture).
+bool resident_supported(int N);
+int resident_clusters_that_fit(int N);  // co-resident clusters on this GPU (0: the launch cannot run)
+bool launch_resident(int N, const DevWorld* worlds, const int* world_ids, int nworlds, int gens, const float2* tw,
+                     int* err, cudaStream_t s);
+
 // Seeding and statistics (seed.cu).
 void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* patches, int npatch,
                          cudaStream_t s);

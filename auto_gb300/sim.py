@@ -200,13 +200,19 @@ class Sim:
 
     def shapes(self):
         """{(width, height): {...}} for every size class: launch variants, chunks (L2-resident runs of
-        worlds), worlds, chunk budget (MiB, 0 = one chunk) and rows per row-pass item."""
+        worlds), worlds, chunk budget (MiB, 0 = one chunk), rows per row-pass item and whether the class runs
+        the cluster-resident step."""
         n = ctypes.c_size_t(0)
         self._check(self._L.lenia_class_shapes(self._ctx, None, 0, ctypes.byref(n)))
-        out = (ctypes.c_int32 * (8 * n.value))()
-        self._check(self._L.lenia_class_shapes(self._ctx, out, 8 * n.value, ctypes.byref(n)))
-        keys = ("column_variant", "row_variant", "chunks", "worlds", "chunk_budget_mib", "rows_per_row_item")
-        return {(out[8 * i], out[8 * i + 1]): dict(zip(keys, out[8 * i + 2:8 * i + 8])) for i in range(n.value)}
+        out = (ctypes.c_int32 * (9 * n.value))()
+        self._check(self._L.lenia_class_shapes(self._ctx, out, 9 * n.value, ctypes.byref(n)))
+        keys = ("column_variant", "row_variant", "chunks", "worlds", "chunk_budget_mib", "rows_per_row_item",
+                "resident")
+        return {(out[9 * i], out[9 * i + 1]): dict(zip(keys, out[9 * i + 2:9 * i + 9])) for i in range(n.value)}
+
+    def set_resident(self, on: bool):
+        """Cluster-resident step on or off where it applies (see lenia_set_resident)."""
+        self._check(self._L.lenia_set_resident(self._ctx, 1 if on else 0))
 
     def set_chunk_budget(self, mib: int):
         """Pin every size class's chunk budget in MiB (see lenia_set_chunk_budget); 0 = one chunk."""

@@ -439,7 +439,7 @@ def run_ours(args, dist):
     # 2 paired; row: 0/1), chunks of worlds run back to back through L2, rows per row item
     variants = {"%dx%d" % wh: {"column": v["column_variant"], "row": v["row_variant"], "chunks": v["chunks"],
                                "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
-                               "rows_per_row_item": v["rows_per_row_item"]}
+                               "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"]}
                 for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step
@@ -481,8 +481,12 @@ def run_ours(args, dist):
     # per size class and generation: one column and one row launch; the tensor-core paths add the
     # FP32 column launch for each channel's first tile group (sizes 256..4096)
     tc_sizes = (256, 512, 1024, 2048, 4096)
+    shapes = sim.shapes()
     launches_per_gen = sum(3 if args.path in ("tf32", "bf16x3") and h in tc_sizes else 2
-                           for (_, h) in {(w.width, w.height) for w in worlds})
+                           for (wd, h) in {(w.width, w.height) for w in worlds}
+                           if not shapes.get((wd, h), {}).get("resident"))
+    # a cluster-resident class is one launch per bench step (all G generations)
+    launches_per_step_resident = sum(1 for v in shapes.values() if v.get("resident"))
     if args.path == "radix2":
         n = worlds[0].width
         lg = int(np.log2(n))
@@ -612,7 +616,7 @@ def run_ours(args, dist):
         out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
-               "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches_per_gen * G * args.steps,
+               "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": (launches_per_gen * G + launches_per_step_resident) * args.steps,
                "launch_variants": variants, "classes": classes,
                "paths": paths,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}

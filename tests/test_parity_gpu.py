@@ -455,3 +455,54 @@ def test_chunked_classes_give_the_same_bits():
         sim.step(6)
         got = sim.read_states()
     assert np.abs(got - outs[0]).max() < 1e-5  # launch variants may differ in rounding
+
+
+def test_resident_step_matches_two_pass_and_fp64():
+    """The cluster-resident step (one launch advances a class's worlds through every generation, one
+    thread-block cluster per world with its half-spectrum in distributed shared memory) against the
+    two launches per generation on the same worlds -- every side it serves, 128 to 512 -- after 1, 5
+    and 64 more generations, and one step against FP64.  Its butterflies, packing and growth are the
+    two-pass step's own device code, so the two agree to float rounding of the same operations."""
+    worlds = [w for w in configs.batched(160) if w.width <= 512]
+    assert {w.width for w in worlds} == {128, 192, 256, 384, 512}
+    with Sim(worlds, seed=0) as a, Sim(worlds, seed=0) as b:
+        for sim in (a, b):
+            for i, w in enumerate(worlds):
+                sim.seed_patches(i, i, w.seed.patches)
+        a.set_resident(True)
+        b.set_resident(False)
+        assert all(v["resident"] == 1 for v in a.shapes().values())
+        assert all(v["resident"] == 0 for v in b.shapes().values())
+        worst = 0.0
+        identical = True
+        for steps in (1, 5, 64):
+            a.step(steps)
+            b.step(steps)
+            sa, sb = a.read_states(), b.read_states()
+            identical = identical and np.array_equal(sa, sb)
+            worst = max(worst, float(np.abs(sa - sb).max()))
+        a.wait()  # raises if a cluster sync gave up
+        print("resident vs two-pass after 70 generations: max|diff| %.3e, bit-identical %s" % (worst, identical))
+        assert worst < 1e-5, worst
+        before = [a.read_state(i) for i in range(len(worlds))]
+        a.step(1)
+        for i, w in enumerate(worlds):
+            err = float(np.abs(a.read_state(i) - fp64_step(w, before[i])).max())
+            assert err < 1e-5, (i, w.width, err)
+        # the engine's spectrum is current after a resident launch: a U-field read uses it
+        u = a.u_field(0, 0)
+        assert np.abs(u - fp64_convolve(worlds[0], a.read_state(0))[0]).max() < 2e-6
+
+
+def test_resident_step_applies_only_where_it_can():
+    """Classes the resident step does not serve (wider than 512, several kernels, the tensor-core
+    paths) keep the two launches per generation whatever lenia_set_resident asks."""
+    worlds = [configs.batched_world(i) for i in range(40)]
+    big = [w for w in worlds if w.width > 512][:2]
+    two = ag.World(256, 256, [ag.Kernel(radius=10.0), ag.Kernel(radius=6.0, mu=0.2, sigma=0.03, weight=0.5)])
+    with Sim(big + [two], seed=0) as sim:
+        sim.set_resident(True)
+        assert all(v["resident"] == 0 for v in sim.shapes().values())
+    with Sim([w for w in worlds if w.width == 256][:2], seed=0, path="bf16x3") as sim:
+        sim.set_resident(True)
+        assert all(v["resident"] == 0 for v in sim.shapes().values())
