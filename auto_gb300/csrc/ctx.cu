@@ -54,6 +54,8 @@ struct SizeClass {
     // cluster-resident step (resident.cu): possible for square one-channel, one-kernel Lenia classes
     // of 128..512 on the FP32 path; `resident` selects it over the two launches per generation
     int resident_ok = 0, resident = 0;
+    int var_res = 0;                       // its launch variant (resident.cu)
+    int res_fits[RESIDENT_VARIANTS] = {};  // clusters of each variant the GPU holds at once (0: cannot run)
     int* d_world_ids = nullptr;
 };
 
@@ -63,6 +65,9 @@ struct SizeClass {
 // less: every budget measured slower (1024 x 1024: 1.91e11 cell-updates/s as one chunk, 1.75e11 in 8
 // chunks, 1.50e11 in 16).  The autotuner still tries budgets per class.
 constexpr size_t DEFAULT_CHUNK_BUDGET = 0;
+// Whether a class the cluster-resident step serves starts with it (the autotuner then times it
+// against the two launches per generation and keeps the faster).
+constexpr int RESIDENT_DEFAULT = 0;
 
 struct WorldBuffers {
     ColItem* d_col = nullptr;  // this world's column items (inspection, U fields)
@@ -395,7 +400,8 @@ Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, &cl.c
 // one launch for all its worlds and steps.
 int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, cudaStream_t s) {
     if (cl.resident) {
-        if (!launch_resident(cl.W, ctx->d_worlds, cl.d_world_ids, (int)cl.worlds.size(), steps, ctx->d_tw, ctx->d_flags, s))
+        if (!launch_resident(cl.W, cl.var_res, ctx->d_worlds, cl.d_world_ids, (int)cl.worlds.size(), steps, ctx->d_tw,
+                             ctx->d_flags, s))
             return fail(ctx, LENIA_ECUDA, "resident launch failed (%dx%d)", cl.W, cl.H);
         return 0;
     }
@@ -701,14 +707,22 @@ int setup_fused(LeniaCtx* ctx) {
         cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
         // the cluster-resident step: square one-channel, one-kernel Lenia worlds of 128..512 on the
         // FP32 path, where the GPU can hold at least one of its clusters
-        if (ctx->path == LENIA_PATH_FP32 && !general && cl.W == cl.H && resident_supported(cl.W) &&
-            resident_clusters_that_fit(cl.W) > 0) {
-            if ((rc = dalloc(ctx, &cl.d_world_ids, cl.worlds.size()))) return rc;
-            CK(cudaMemcpy(cl.d_world_ids, cl.worlds.data(), cl.worlds.size() * sizeof(int), cudaMemcpyHostToDevice));
-            cl.resident_ok = 1;
-            cl.resident = 1;
+        if (ctx->path == LENIA_PATH_FP32 && !general && cl.W == cl.H && resident_supported(cl.W)) {
+            cl.var_res = -1;
+            for (int v = 0; v < RESIDENT_VARIANTS; v++) {
+                cl.res_fits[v] = resident_clusters_that_fit(cl.W, v);
+                if (cl.res_fits[v] > 0 && cl.var_res < 0) cl.var_res = v;
+            }
+            cudaGetLastError();
+            if (cl.var_res >= 0) {
+                if ((rc = dalloc(ctx, &cl.d_world_ids, cl.worlds.size()))) return rc;
+                CK(cudaMemcpy(cl.d_world_ids, cl.worlds.data(), cl.worlds.size() * sizeof(int), cudaMemcpyHostToDevice));
+                cl.resident_ok = 1;
+                cl.resident = RESIDENT_DEFAULT;
+            } else {
+                cl.var_res = 0;
+            }
         }
-        cudaGetLastError();
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
             if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
@@ -1424,10 +1438,16 @@ int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib) {
     return 0;
 }
 
-int lenia_set_resident(LeniaCtx* ctx, int32_t on) {
+int lenia_set_resident(LeniaCtx* ctx, int32_t mode) {
     if (!ctx) return LENIA_EINVAL;
-    if (on != 0 && on != 1) return fail(ctx, LENIA_EINVAL, "on must be 0 or 1");
-    for (auto& cl : ctx->classes) cl.resident = on && cl.resident_ok;
+    if (mode < 0 || mode > 1 + RESIDENT_VARIANTS)
+        return fail(ctx, LENIA_EINVAL, "mode must be 0 (off), 1 (on) or 2..%d (on, launch variant mode - 2)",
+                    1 + RESIDENT_VARIANTS);
+    for (auto& cl : ctx->classes) {
+        const int v = mode >= 2 ? mode - 2 : cl.var_res;
+        cl.resident = mode != 0 && cl.resident_ok && cl.res_fits[v] > 0;
+        if (cl.resident) cl.var_res = v;
+    }
     CK(cudaStreamSynchronize(ctx->stream));
     int rc = rebuild_graphs(ctx);
     if (rc) return rc;
@@ -1439,10 +1459,10 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (count < 9 * ctx->classes.size()) return LENIA_EINVAL;
+    if (count < 10 * ctx->classes.size()) return LENIA_EINVAL;
     for (size_t i = 0; i < ctx->classes.size(); i++) {
         const auto& cl = ctx->classes[i];
-        int32_t* o = out + 9 * i;
+        int32_t* o = out + 10 * i;
         o[0] = cl.W;
         o[1] = cl.H;
         o[2] = cl.var_col;
@@ -1452,6 +1472,7 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
         o[6] = (int32_t)(cl.chunk_budget >> 20);
         o[7] = row_item_rows(cl.W, cl.general);
         o[8] = cl.resident;
+        o[9] = cl.var_res;
     }
     return 0;
 }
@@ -1503,17 +1524,29 @@ static int autotune_search(LeniaCtx* ctx) {
         };
         int bi = 0, rc = 0;
         if (cl.resident_ok) {
-            // the cluster-resident step against the two-pass step in its current shape
-            double t_res = 0, t_two = 0;
-            const int was = cl.resident;
-            cl.resident = 1;
-            rc = timed(shape_of(cl), &t_res);
-            cl.resident = 0;
-            if (!rc) rc = timed(shape_of(cl), &t_two);
-            cl.resident = was;
+            // every variant of the cluster-resident step that fits, against the two-pass step in its
+            // current shape; candidate 0 is the current choice
+            const int was_res = cl.resident, was_var = cl.var_res;
+            std::vector<std::pair<int, int>> cands{{was_res, was_var}};  // (resident, variant)
+            if (was_res) cands.push_back({0, was_var});
+            for (int v = 0; v < RESIDENT_VARIANTS; v++)
+                if (cl.res_fits[v] > 0 && !(was_res && v == was_var)) cands.push_back({1, v});
+            std::vector<double> t(cands.size());
+            for (size_t i = 0; i < cands.size() && !rc; i++) {
+                cl.resident = cands[i].first;
+                cl.var_res = cands[i].second;
+                rc = timed(shape_of(cl), &t[i]);
+            }
+            cl.resident = was_res;
+            cl.var_res = was_var;
             if (rc) return rc;
-            const double t_cur = was ? t_res : t_two, t_other = was ? t_two : t_res;
-            if (t_other < 0.97 * t_cur) cl.resident = !was;
+            size_t b = 0;
+            for (size_t i = 1; i < cands.size(); i++)
+                if (t[i] < t[b]) b = i;
+            if (t[b] < 0.97 * t[0]) {
+                cl.resident = cands[b].first;
+                cl.var_res = cands[b].second;
+            }
             if (cl.resident) continue;  // launch variants and chunks do not apply to it
         }
         {

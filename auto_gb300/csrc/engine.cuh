@@ -71,10 +71,13 @@ int max_smem_optin();
 // thread-block cluster of N/32 CTAs per world.  world_ids: the class's world indices (device).
 // err: a device int set to 1 if a cluster sync gave up.  A zero-world call only configures the
 // kernel (outside any stream capture).
+// Each size is built in RESIDENT_VARIANTS launch variants (sequences per batch, register budget).
+constexpr int RESIDENT_VARIANTS = 3;
 bool resident_supported(int N);
-int resident_clusters_that_fit(int N);  // co-resident clusters on this GPU (0: the launch cannot run)
-bool launch_resident(int N, const DevWorld* worlds, const int* world_ids, int nworlds, int gens, const float2* tw,
-                     int* err, cudaStream_t s);
+// co-resident clusters of a variant on this GPU (0: the launch cannot run); configures the kernel
+int resident_clusters_that_fit(int N, int variant);
+bool launch_resident(int N, int variant, const DevWorld* worlds, const int* world_ids, int nworlds, int gens,
+                     const float2* tw, int* err, cudaStream_t s);
 
 // Seeding and statistics (seed.cu).
 void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* patches, int npatch,

@@ -54,9 +54,12 @@ __device__ __forceinline__ uint32_t map_rank(uint32_t saddr, uint32_t rank) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
     return r;
 }
+// No memory clobber: these loads are ordered after the peers' stores by the cluster sync (whose
+// arrive and wait carry the clobber), and leaving them free lets a thread issue all of its remote
+// loads before it uses the first.
 __device__ __forceinline__ float2 ld_dsmem(uint32_t addr) {
     float2 v;
-    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr) : "memory");
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
     return v;
 }
 __device__ __forceinline__ void st_dsmem(uint32_t addr, float2 v) {
@@ -84,17 +87,18 @@ constexpr uint32_t SYNC_POLLS = 1u << 22;      // a cluster sync gives up after 
 constexpr uint32_t SYNC_POLLS_DEAD = 1u << 6;  // after one has given up: keep arriving, barely wait
 
 // -------------------------------------------------------------- shape of one size class
-template <int N>
+// S: sequences a CTA transforms at once, S packed row pairs (2S rows) or S columns (16: all 32 rows
+// and all 16 columns in one batch); MINB: resident CTAs per SM the registers are budgeted for.  Each
+// size is built in a few (S, MINB) launch variants, which the autotuner times.
+template <int N, int S_, int MINB_>
 struct Res {
     static constexpr int G = N / 32;                 // CTAs per cluster (one world)
     static constexpr int ROWS = 32;                  // rows a CTA owns
     static constexpr int COLS = 16;                  // spectrum columns a CTA owns
     static constexpr int R0 = plan_radix(N, 0), NB = N / R0;
-    // sequences a CTA transforms at once: S packed row pairs (2S rows) or S columns
-    static constexpr int S = N <= 192 ? 16 : (N == 512 ? 4 : 8);
+    static constexpr int S = S_, MINB = MINB_;
     static constexpr int NT = S * NB;                // one first-stage butterfly per thread
-    // resident CTAs per SM the registers are budgeted for (shared memory allows at least as many)
-    static constexpr int MINB = N == 256 ? 3 : ((N == 128 || N == 512) ? 2 : 1);
+    static constexpr int GATHER = S * (N / 2) / NT;  // remote elements a thread gathers (and scatters) per batch
     static constexpr int SEQ = seq_stride(N);
     static constexpr int HQC = khat_cols_stride<N>();
     // shared memory: CS [COLS][SEQ] float2 | WK [S][SEQ] float2 | stage tables | KH [COLS][HQC] float | bars
@@ -106,6 +110,7 @@ struct Res {
     static_assert(G * ROWS == N && G * COLS == N / 2, "32 rows and 16 spectrum columns per CTA");
     static_assert(ROWS % (2 * S) == 0 && COLS % S == 0 && S >= TC, "batches of S");
     static_assert(fusable<N>(), "chained transforms");
+    static_assert(GATHER * NT == S * (N / 2), "gather loop without remainder");
 };
 
 // Cluster sync, bounded (see the file comment).  Returns false once a wait has run out, on every
@@ -130,11 +135,11 @@ struct ClusterSync {
 };
 
 // -------------------------------------------------------------- the kernel
-template <int N>
-__global__ void __launch_bounds__(Res<N>::NT, Res<N>::MINB)
+template <int N, int S_, int MINB_>
+__global__ void __launch_bounds__(Res<N, S_, MINB_>::NT, MINB_)
     resident_step(const DevWorld* __restrict__ worlds, const int* __restrict__ world_ids, int gens,
                   const float2* __restrict__ tw, int* __restrict__ err) {
-    using P = Res<N>;
+    using P = Res<N, S_, MINB_>;
     constexpr int S = P::S, NT = P::NT, SEQ = P::SEQ, COLS = P::COLS, HQC = P::HQC;
     extern __shared__ float4 smem_raw[];
     uint8_t* base = reinterpret_cast<uint8_t*>(smem_raw);
@@ -218,15 +223,22 @@ __global__ void __launch_bounds__(Res<N>::NT, Res<N>::MINB)
                 if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, 2 * S * N * (uint32_t)sizeof(float));
                 // gather: Z_p = A + iB (A = row r0 + 2p, B = row r0 + 2p + 1) with Hermitian symmetry
                 // for kx > N/2, the formulas of load_rows_spectrum; consecutive lanes on
-                // consecutive kx
-                for (int e = threadIdx.x; e < S * (N / 2); e += NT) {
-                    const int p = e / (N / 2), kx = e - p * (N / 2);
+                // consecutive kx.  Every remote load of the thread is issued before the first is used.
+                float2 GA[P::GATHER], GB[P::GATHER];
+#pragma unroll
+                for (int i = 0; i < P::GATHER; i++) {
+                    const int e = threadIdx.x + i * NT, p = e / (N / 2), kx = e - p * (N / 2);
                     // rows r0 + 2p and r0 + 2p + 1 of column kx in its owner's slice: r0 + 2p is even, so
                     // the two are neighbours (padding follows odd indices 15 mod 16 only)
                     const uint32_t off = cs_addr + (uint32_t)(((kx % COLS) * SEQ + pad(r0 + 2 * p)) * sizeof(float2));
                     const uint32_t src = map_rank(off, (uint32_t)(kx / COLS));
-                    const float2 A = ld_dsmem(src);
-                    const float2 B = ld_dsmem(src + (uint32_t)sizeof(float2));
+                    GA[i] = ld_dsmem(src);
+                    GB[i] = ld_dsmem(src + (uint32_t)sizeof(float2));
+                }
+#pragma unroll
+                for (int i = 0; i < P::GATHER; i++) {
+                    const int e = threadIdx.x + i * NT, p = e / (N / 2), kx = e - p * (N / 2);
+                    const float2 A = GA[i], B = GB[i];
                     float2* z = WK + p * SEQ;
                     if (kx == 0) {
                         z[pad(0)] = make_float2(A.x, B.x);
@@ -259,8 +271,9 @@ __global__ void __launch_bounds__(Res<N>::NT, Res<N>::MINB)
                     });
                 // scatter: the half-spectra of the 2S new rows into the owners' column slices (the
                 // formulas of store_rows_spectrum)
-                for (int e = threadIdx.x; e < S * (N / 2); e += NT) {
-                    const int p = e / (N / 2), kx = e - p * (N / 2);
+#pragma unroll
+                for (int i = 0; i < P::GATHER; i++) {
+                    const int e = threadIdx.x + i * NT, p = e / (N / 2), kx = e - p * (N / 2);
                     const float2* z = WK + p * SEQ;
                     float2 A, B;
                     if (kx == 0) {
@@ -290,16 +303,16 @@ __global__ void __launch_bounds__(Res<N>::NT, Res<N>::MINB)
     if (cs.dead && threadIdx.x == 0) atomicExch(err, 1);
 }
 
-template <int N>
+template <int N, int S, int MINB>
 bool launch_shape(const DevWorld* worlds, const int* world_ids, int nworlds, int gens, const float2* tw, int* err,
                   cudaStream_t s) {
-    using P = Res<N>;
+    using P = Res<N, S, MINB>;
     static int configured = 0;
     if (!configured) {
-        if (cudaFuncSetAttribute(resident_step<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM) !=
-                cudaSuccess ||
-            (P::G > 8 && cudaFuncSetAttribute(resident_step<N>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-                             cudaSuccess))
+        if (cudaFuncSetAttribute(resident_step<N, S, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)P::SMEM) != cudaSuccess ||
+            (P::G > 8 && cudaFuncSetAttribute(resident_step<N, S, MINB>,
+                                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess))
             return false;
         configured = 1;
     }
@@ -316,12 +329,13 @@ bool launch_shape(const DevWorld* worlds, const int* world_ids, int nworlds, int
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, resident_step<N>, worlds, world_ids, gens, tw, err) == cudaSuccess;
+    return cudaLaunchKernelEx(&cfg, resident_step<N, S, MINB>, worlds, world_ids, gens, tw, err) == cudaSuccess;
 }
 
-template <int N>
+template <int N, int S, int MINB>
 int clusters_that_fit() {
-    using P = Res<N>;
+    using P = Res<N, S, MINB>;
+    if (!launch_shape<N, S, MINB>(nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr)) return 0;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)P::G);
     cfg.blockDim = dim3((unsigned)P::NT);
@@ -334,38 +348,41 @@ int clusters_that_fit() {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, resident_step<N>, &cfg) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveClusters(&n, resident_step<N, S, MINB>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
 }
 
+// The launch variants of each size, (S, MINB): 0 = (16, 1), 1 = (8, 1), 2 = (4, 2).
+#define LENIA_RESIDENT_VARIANT(N, F) (variant == 0 ? F<N, 16, 1> : variant == 1 ? F<N, 8, 1> : F<N, 4, 2>)
+
 }  // namespace
 
 bool resident_supported(int N) { return N == 128 || N == 192 || N == 256 || N == 384 || N == 512; }
 
-int resident_clusters_that_fit(int N) {
-    // configure first (shared-memory limit and non-portable cluster sizes), with a zero-world launch
-    if (!launch_resident(N, nullptr, nullptr, 0, 0, nullptr, nullptr, nullptr)) return 0;
+int resident_clusters_that_fit(int N, int variant) {
+    if (variant < 0 || variant >= RESIDENT_VARIANTS) return 0;
     switch (N) {
-    case 128: return clusters_that_fit<128>();
-    case 192: return clusters_that_fit<192>();
-    case 256: return clusters_that_fit<256>();
-    case 384: return clusters_that_fit<384>();
-    case 512: return clusters_that_fit<512>();
+    case 128: return LENIA_RESIDENT_VARIANT(128, clusters_that_fit)();
+    case 192: return LENIA_RESIDENT_VARIANT(192, clusters_that_fit)();
+    case 256: return LENIA_RESIDENT_VARIANT(256, clusters_that_fit)();
+    case 384: return LENIA_RESIDENT_VARIANT(384, clusters_that_fit)();
+    case 512: return LENIA_RESIDENT_VARIANT(512, clusters_that_fit)();
     }
     return 0;
 }
 
-bool launch_resident(int N, const DevWorld* worlds, const int* world_ids, int nworlds, int gens, const float2* tw,
-                     int* err, cudaStream_t s) {
+bool launch_resident(int N, int variant, const DevWorld* worlds, const int* world_ids, int nworlds, int gens,
+                     const float2* tw, int* err, cudaStream_t s) {
+    if (variant < 0 || variant >= RESIDENT_VARIANTS) return false;
     switch (N) {
-    case 128: return launch_shape<128>(worlds, world_ids, nworlds, gens, tw, err, s);
-    case 192: return launch_shape<192>(worlds, world_ids, nworlds, gens, tw, err, s);
-    case 256: return launch_shape<256>(worlds, world_ids, nworlds, gens, tw, err, s);
-    case 384: return launch_shape<384>(worlds, world_ids, nworlds, gens, tw, err, s);
-    case 512: return launch_shape<512>(worlds, world_ids, nworlds, gens, tw, err, s);
+    case 128: return LENIA_RESIDENT_VARIANT(128, launch_shape)(worlds, world_ids, nworlds, gens, tw, err, s);
+    case 192: return LENIA_RESIDENT_VARIANT(192, launch_shape)(worlds, world_ids, nworlds, gens, tw, err, s);
+    case 256: return LENIA_RESIDENT_VARIANT(256, launch_shape)(worlds, world_ids, nworlds, gens, tw, err, s);
+    case 384: return LENIA_RESIDENT_VARIANT(384, launch_shape)(worlds, world_ids, nworlds, gens, tw, err, s);
+    case 512: return LENIA_RESIDENT_VARIANT(512, launch_shape)(worlds, world_ids, nworlds, gens, tw, err, s);
     }
     return false;
 }

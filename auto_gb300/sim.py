@@ -204,15 +204,16 @@ class Sim:
         the cluster-resident step."""
         n = ctypes.c_size_t(0)
         self._check(self._L.lenia_class_shapes(self._ctx, None, 0, ctypes.byref(n)))
-        out = (ctypes.c_int32 * (9 * n.value))()
-        self._check(self._L.lenia_class_shapes(self._ctx, out, 9 * n.value, ctypes.byref(n)))
+        out = (ctypes.c_int32 * (10 * n.value))()
+        self._check(self._L.lenia_class_shapes(self._ctx, out, 10 * n.value, ctypes.byref(n)))
         keys = ("column_variant", "row_variant", "chunks", "worlds", "chunk_budget_mib", "rows_per_row_item",
-                "resident")
-        return {(out[9 * i], out[9 * i + 1]): dict(zip(keys, out[9 * i + 2:9 * i + 9])) for i in range(n.value)}
+                "resident", "resident_variant")
+        return {(out[10 * i], out[10 * i + 1]): dict(zip(keys, out[10 * i + 2:10 * i + 10])) for i in range(n.value)}
 
-    def set_resident(self, on: bool):
-        """Cluster-resident step on or off where it applies (see lenia_set_resident)."""
-        self._check(self._L.lenia_set_resident(self._ctx, 1 if on else 0))
+    def set_resident(self, on: bool, variant: int = -1):
+        """Cluster-resident step on or off where it applies, optionally in launch variant `variant`
+        (see lenia_set_resident)."""
+        self._check(self._L.lenia_set_resident(self._ctx, (2 + variant if variant >= 0 else 1) if on else 0))
 
     def set_chunk_budget(self, mib: int):
         """Pin every size class's chunk budget in MiB (see lenia_set_chunk_budget); 0 = one chunk."""

@@ -439,7 +439,8 @@ def run_ours(args, dist):
     # 2 paired; row: 0/1), chunks of worlds run back to back through L2, rows per row item
     variants = {"%dx%d" % wh: {"column": v["column_variant"], "row": v["row_variant"], "chunks": v["chunks"],
                                "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
-                               "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"]}
+                               "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"],
+                               "resident_variant": v["resident_variant"]}
                 for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step

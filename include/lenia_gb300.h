@@ -194,9 +194,10 @@ LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
 LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
 /* The launch shape of every size class, as the autotuner left it: *nclasses = the number of classes;
- * with `out` (count >= 9 * classes) nine int32 per class: width, height, column variant, row
+ * with `out` (count >= 10 * classes) ten int32 per class: width, height, column variant, row
  * variant, chunks, worlds, chunk budget in MiB (0: the class is one chunk), rows per row-pass item,
- * and 1 if the class runs the cluster-resident step (lenia_set_resident), else 0.
+ * 1 if the class runs the cluster-resident step (lenia_set_resident) else 0, and that step's launch
+ * variant.
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
@@ -205,15 +206,16 @@ LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */
 LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
-/* The cluster-resident step, on (1, the default where it applies) or off (0) for every size class it
- * applies to: square worlds of 128, 192, 256, 384 or 512 with one channel and one Lenia kernel on
+/* The cluster-resident step, on (mode 1; 2 + v: on in launch variant v, which transforms 16, 8 or 4
+ * sequences at a time for v = 0, 1, 2) or off (mode 0, the default until lenia_autotune chooses)
+ * for every size class it applies to: square worlds of 128, 192, 256, 384 or 512 with one channel and one Lenia kernel on
  * the FP32 path.  One launch then advances all of a class's worlds through every generation of a
  * step call, one thread-block cluster (side/32 CTAs) per world with the world's half-spectrum held
  * in the cluster's distributed shared memory, in place of two launches per generation.  The
  * arithmetic is the two-pass step's.  A cluster sync that gives up is reported as LENIA_ECUDA by
  * lenia_sync.  Rebuilds the step graphs.  No reference counterpart (the reference dispatches every
  * pass of every world separately, crates/auto-core/src/sim.rs:297-380). */
-LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t on);
+LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t mode);
 
 /* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
  * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.
