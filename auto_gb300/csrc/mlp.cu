@@ -7,7 +7,10 @@
 // (scripts/life_screen.py:143-179), which is the baseline this proposer is compared with.
 //
 // Parameters: FP32 master weights updated by Adam; BF16 copies feed every GEMM; activations are
-// stored in BF16 for the backward pass; every GEMM accumulates in FP32.
+// stored in BF16 for the backward pass; every GEMM accumulates in FP32.  The GEMMs of the two
+// 256-wide layers -- forward h1 and h2, backward dh1 and the weight gradients dW1 and dW2 -- run on
+// the 5th-generation tensor cores (gemm_tc: tcgen05 MMAs, TMEM accumulators); the 3-wide output
+// layer's (z, dW3, dh2) on the CUDA cores.
 //   layer 1: W1 [256 x 16],  b1 [256]      h1 = relu(x W1^T + b1)
 //   layer 2: W2 [256 x 256], b2 [256]      h2 = relu(h1 W2^T + b2)
 //   layer 3: W3 [3 x 256],   b3 [3]        z  = h2 W3^T + b3,  p = sigmoid(z)
@@ -21,6 +24,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "tc_ptx.cuh"
 
 namespace lenia {
 namespace mlp {
@@ -33,12 +37,14 @@ using bf16 = __nv_bfloat16;
 
 // C[M x N] = A[M x K] * B^T (B is [N x K]) with bf16 operands and FP32 accumulation, when
 // TRANS_B is false; C = A * B (B is [K x N]) when TRANS_B is true.  TRANS_A reads A as [K x M].
-// Epilogue: + bias[n], relu, and output in f32 and/or bf16.  64 x 64 tiles, 256 threads, 4 x 4
-// outputs per thread, K in steps of 16 through shared memory.
+// Epilogue: + bias[n], relu, and output in f32 and/or bf16 (and bf16 transposed, CbT[n * ldt + m]).
+// 64 x 64 tiles, 256 threads, 4 x 4 outputs per thread, K in steps of 16 through shared memory: the
+// CUDA-core GEMM of the 3-wide output layer, where an MMA tile would be almost all padding.
 template <bool TRANS_A, bool TRANS_B>
 __global__ void __launch_bounds__(256) gemm_bf16(const bf16* __restrict__ A, const bf16* __restrict__ B, int M, int N,
                                                  int K, const float* __restrict__ bias, int relu, float* __restrict__ Cf,
-                                                 bf16* __restrict__ Cb, const bf16* __restrict__ mask) {
+                                                 bf16* __restrict__ Cb, const bf16* __restrict__ mask,
+                                                 bf16* __restrict__ CbT = nullptr, int ldt = 0) {
     __shared__ float As[16][64 + 1];
     __shared__ float Bs[16][64 + 1];
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
@@ -82,12 +88,182 @@ __global__ void __launch_bounds__(256) gemm_bf16(const bf16* __restrict__ A, con
             if (mask && __bfloat162float(mask[(size_t)m * N + n]) <= 0.f) v = 0.f;
             if (Cf) Cf[(size_t)m * N + n] = v;
             if (Cb) Cb[(size_t)m * N + n] = __float2bfloat16_rn(v);
+            if (CbT) CbT[(size_t)n * ldt + m] = __float2bfloat16_rn(v);
         }
+}
+
+// ------------------------------------------------------------------ tensor-core GEMM (tcgen05)
+// C[M x N] = A[M x K] * B[N x K]^T with A and B bf16, K-major (rows lda / ldb elements apart), and
+// FP32 accumulation in TMEM: the GEMMs of the 256-wide layers.  A CTA of 128 threads owns 128 rows
+// of C and all N columns (N a multiple of 16, at most 256) and loops over K in chunks of 64:
+// every thread stages 16-byte pieces of both operands into shared memory with cp.async, in the
+// canonical K-major layout without swizzle (8-row x 16-byte core matrices, K-adjacent ones 128 bytes
+// apart, 8-row groups 1024 bytes apart), double-buffered, and one elected thread issues the
+// M = 128, N, K = 16 MMAs of a chunk and commits them to that buffer's mbarrier.  Elements past M or
+// K are zero-filled.  With ksplit > 1, CTA column kz of the grid takes every ksplit-th chunk and adds
+// its partial sums into Cf (zeroed by the caller) with atomics; the bias, ReLU, mask and bf16 outputs
+// need ksplit = 1.  Epilogue per row (a thread per TMEM lane): + bias[n], ReLU, zero where mask <= 0,
+// then FP32 (Cf), bf16 (Cb) and transposed bf16 (CbT[n * ldt + m]) outputs, each optional.  Every
+// barrier wait is bounded; a CTA that gives up waits (bounded) for its own MMAs, raises *err, frees
+// its TMEM and writes nothing.
+constexpr int TCK = 64;  // K elements per staged chunk: 128 bytes of bf16 per operand row
+template <int N>
+struct TcGemm {
+    static constexpr int ABYTES = 128 * TCK * 2, BBYTES = N * TCK * 2, STAGE = ABYTES + BBYTES;
+    static constexpr int SMEM = 2 * STAGE + 64;
+    static constexpr uint32_t TCOLS = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));
+    static_assert(N % 16 == 0 && N >= 16 && N <= 256, "MMA N");
+};
+
+__device__ __forceinline__ void cp_async16_zfill(void* dst, const void* src, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(tc::smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+
+template <int N>
+__global__ void __launch_bounds__(128, 1)
+    gemm_tc(const bf16* __restrict__ A, int lda, const bf16* __restrict__ B, int ldb, int M, int K, int ksplit,
+            const float* __restrict__ bias, int relu, const bf16* __restrict__ mask, float* __restrict__ Cf,
+            bf16* __restrict__ Cb, bf16* __restrict__ CbT, int ldt, int* __restrict__ err) {
+    using P = TcGemm<N>;
+    extern __shared__ __align__(128) uint8_t smem[];
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * P::STAGE);  // MMA done, per buffer
+    uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 2);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int m0 = blockIdx.x * 128, kz = blockIdx.y;
+    const int nchunks_all = (K + TCK - 1) / TCK;
+    const int nchunks = nchunks_all > kz ? (nchunks_all - kz + ksplit - 1) / ksplit : 0;  // this CTA's chunks
+    if (tid == 0) {
+        tc::mbar_init(bars, 1);
+        tc::mbar_init(bars + 1, 1);
+        tc::fence_barrier_init();
+    }
+    if (warp == 0) tc::tmem_alloc(slot, P::TCOLS);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *slot;
+
+    // stage chunk `ci` (the ci-th of this CTA) into buffer b
+    auto load = [&](int ci, int b) {
+        uint8_t* sa = smem + b * P::STAGE;
+        uint8_t* sb = sa + P::ABYTES;
+        const int k0 = (kz + ci * ksplit) * TCK;
+        constexpr int PIECES = (128 + N) * (TCK / 8);
+        for (int idx = tid; idx < PIECES; idx += 128) {
+            const int row = idx / (TCK / 8), kg = idx % (TCK / 8), k = k0 + 8 * kg;
+            const bool is_a = row < 128;
+            const int r = is_a ? row : row - 128;
+            const int grow = is_a ? m0 + r : r;
+            const bool valid = (!is_a || grow < M) && k < K;
+            uint8_t* dst = (is_a ? sa : sb) + tc::kmajor_offset(r, 8 * kg, TCK, 2);
+            if (valid && k + 8 <= K) {
+                cp_async16_zfill(dst, (is_a ? A + (size_t)grow * lda : B + (size_t)grow * ldb) + k, 16);
+            } else if (valid) {
+                // the last piece of a row whose K is not a multiple of 8: element by element
+                const uint16_t* src = reinterpret_cast<const uint16_t*>((is_a ? A + (size_t)grow * lda : B + (size_t)grow * ldb) + k);
+                uint16_t h[8];
+                for (int i = 0; i < 8; i++) h[i] = k + i < K ? src[i] : (uint16_t)0;
+                *reinterpret_cast<uint4*>(dst) = make_uint4(h[0] | (uint32_t)h[1] << 16, h[2] | (uint32_t)h[3] << 16,
+                                                            h[4] | (uint32_t)h[5] << 16, h[6] | (uint32_t)h[7] << 16);
+            } else {
+                *reinterpret_cast<uint4*>(dst) = make_uint4(0, 0, 0, 0);
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    };
+    constexpr uint32_t IDESC = tc::instr_desc(1, 128, N);
+    constexpr uint32_t SBO = TCK * 2 * 8;
+    bool ok = true;
+    int issued = 0;  // chunks whose MMAs were issued
+    if (nchunks > 0) load(0, 0);
+    for (int ci = 0; ci < nchunks && ok; ci++) {
+        if (ci + 1 < nchunks) {
+            // the buffer of chunk ci + 1 was read by the MMAs of chunk ci - 1
+            if (ci >= 1 && __syncthreads_or(!tc::mbar_wait(bars + ((ci + 1) & 1), ((ci - 1) >> 1) & 1))) {
+                ok = false;
+                break;
+            }
+            load(ci + 1, (ci + 1) & 1);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        tc::fence_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc::tc_fence_after();
+            const uint32_t sa = tc::smem_u32(smem + (ci & 1) * P::STAGE), sb = sa + P::ABYTES;
+            const int k0 = (kz + ci * ksplit) * TCK;
+            const int ksteps = (min(TCK, K - k0) + 15) / 16;
+            for (int s = 0; s < ksteps; s++)
+                tc::mma<false>(tmem, tc::smem_desc(sa + 256u * s, 128, SBO), tc::smem_desc(sb + 256u * s, 128, SBO),
+                               IDESC, (ci > 0 || s > 0) ? 1u : 0u);
+            tc::mma_commit(bars + (ci & 1));
+        }
+        issued = ci + 1;
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+    // the last issued chunk's commit covers every earlier MMA
+    if (ok && issued > 0 && __syncthreads_or(!tc::mbar_wait(bars + ((issued - 1) & 1), ((issued - 1) >> 1) & 1)))
+        ok = false;
+    tc::tc_fence_after();
+    if (ok && issued > 0) {
+        const int row = m0 + tid;
+        for (int n0 = 0; n0 < N; n0 += 32) {
+            float v[32];
+            tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)n0, v);
+            if (row >= M) continue;
+            const int nn = N - n0 < 32 ? N - n0 : 32;
+            for (int i = 0; i < nn; i++) {
+                const int n = n0 + i;
+                float x = v[i];
+                if (ksplit > 1) {
+                    atomicAdd(Cf + (size_t)row * N + n, x);
+                    continue;
+                }
+                if (bias) x += bias[n];
+                if (relu) x = fmaxf(x, 0.f);
+                if (mask && __bfloat162float(mask[(size_t)row * N + n]) <= 0.f) x = 0.f;
+                if (Cf) Cf[(size_t)row * N + n] = x;
+                const bf16 xb = __float2bfloat16_rn(x);
+                if (Cb) Cb[(size_t)row * N + n] = xb;
+                if (CbT) CbT[(size_t)n * ldt + row] = xb;
+            }
+        }
+    }
+    if (!ok && tid == 0) {
+        if (issued > 0) tc::mbar_wait(bars + ((issued - 1) & 1), ((issued - 1) >> 1) & 1);  // drain, bounded
+        atomicExch(err, 1);
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, P::TCOLS);
+    }
 }
 
 __global__ void to_bf16(const float* __restrict__ x, bf16* __restrict__ y, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] = __float2bfloat16_rn(x[i]);
+}
+
+// The batch's inputs (B x IN, f32) as bf16, row-major and transposed (IN x ldt).
+__global__ void inputs_bf16(const float* __restrict__ x, bf16* __restrict__ xb, bf16* __restrict__ xt, int B, int ldt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= B * IN) return;
+    const bf16 v = __float2bfloat16_rn(x[i]);
+    xb[i] = v;
+    xt[(size_t)(i % IN) * ldt + i / IN] = v;
+}
+
+// W2 (FP32 master, [out][in]) as bf16 transposed, [in][out]: the B operand of dh1 = dh2 W2.
+__global__ void w2_transposed(const float* __restrict__ w2, bf16* __restrict__ w2t) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= HID * HID) return;
+    const int o = i / HID, in = i % HID;
+    w2t[(size_t)in * HID + o] = __float2bfloat16_rn(w2[i]);
 }
 
 // BCE with logits: dz = (sigmoid(z) - y) / (B * OUT); per-row losses for the host to average.
@@ -149,6 +325,11 @@ struct LeniaMlp {
     bf16* wb = nullptr;                                             // BF16 copy of the parameters
     float *x = nullptr, *y = nullptr, *z = nullptr, *dz = nullptr, *dh = nullptr, *loss = nullptr, *p = nullptr;
     bf16 *xb = nullptr, *h1 = nullptr, *h2 = nullptr, *dzb = nullptr, *dh2b = nullptr, *dh1b = nullptr;
+    // transposed copies (feature-major, batch contiguous, ldt apart): the K-major operands of the
+    // weight-gradient GEMMs, whose K is the batch; and W2 transposed for dh1 = dh2 W2
+    int ldt = 0;
+    bf16 *xt = nullptr, *h1t = nullptr, *dh2t = nullptr, *dh1t = nullptr, *w2t = nullptr;
+    int* err = nullptr;  // set by a tensor-core GEMM that gave up waiting on a barrier
     std::vector<void*> allocs;
 };
 
@@ -170,14 +351,33 @@ int err(const char* msg) {
 
 dim3 grid_for(int M, int N) { return dim3((N + 63) / 64, (M + 63) / 64); }
 
-// forward pass of `B` rows already in n->x; logits into n->z
+// One tensor-core GEMM launch (see gemm_tc): C [M x N] = A [M x K] B[N x K]^T.
+template <int N>
+void tc_gemm(LeniaMlp* n, const bf16* A, int lda, const bf16* B, int ldb, int M, int K, int ksplit, const float* bias,
+             int relu, const bf16* mask, float* Cf, bf16* Cb, bf16* CbT) {
+    static int configured = 0;
+    if (!configured) {
+        cudaFuncSetAttribute(gemm_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcGemm<N>::SMEM);
+        configured = 1;
+    }
+    const dim3 grid((M + 127) / 128, ksplit);
+    gemm_tc<N><<<grid, 128, TcGemm<N>::SMEM, n->stream>>>(A, lda, B, ldb, M, K, ksplit, bias, relu, mask, Cf, Cb, CbT,
+                                                          n->ldt, n->err);
+}
+
+// K-splits of a weight-gradient GEMM whose K is the batch: enough CTAs to spread the batch over SMs
+int ksplit_for(int B) {
+    const int chunks = (B + TCK - 1) / TCK;
+    return chunks < 32 ? chunks : 32;
+}
+
+// forward pass of `B` rows already in n->x; logits into n->z.  The 16 -> 256 and 256 -> 256 layers
+// run on the tensor cores; the 256 -> 3 layer on the CUDA cores.
 void forward(LeniaMlp* n, int B) {
     cudaStream_t s = n->stream;
-    to_bf16<<<(B * IN + 255) / 256, 256, 0, s>>>(n->x, n->xb, B * IN);
-    gemm_bf16<false, false><<<grid_for(B, HID), 256, 0, s>>>(n->xb, n->wb + P_W1, B, HID, IN, n->w + P_B1, 1, nullptr,
-                                                              n->h1, nullptr);
-    gemm_bf16<false, false><<<grid_for(B, HID), 256, 0, s>>>(n->h1, n->wb + P_W2, B, HID, HID, n->w + P_B2, 1, nullptr,
-                                                              n->h2, nullptr);
+    inputs_bf16<<<(B * IN + 255) / 256, 256, 0, s>>>(n->x, n->xb, n->xt, B, n->ldt);
+    tc_gemm<HID>(n, n->xb, IN, n->wb + P_W1, IN, B, IN, 1, n->w + P_B1, 1, nullptr, nullptr, n->h1, n->h1t);
+    tc_gemm<HID>(n, n->h1, HID, n->wb + P_W2, HID, B, HID, 1, n->w + P_B2, 1, nullptr, nullptr, n->h2, nullptr);
     gemm_bf16<false, false><<<grid_for(B, OUT), 256, 0, s>>>(n->h2, n->wb + P_W3, B, OUT, HID, n->w + P_B3, 0, n->z,
                                                               nullptr, nullptr);
 }
@@ -191,17 +391,29 @@ void backward(LeniaMlp* n, int B) {
                                                              nullptr, nullptr);
     col_sum<<<1, 32, 0, s>>>(n->dz, B, OUT, n->g + P_B3);
     gemm_bf16<false, true><<<grid_for(B, HID), 256, 0, s>>>(n->dzb, n->wb + P_W3, B, HID, OUT, nullptr, 0, n->dh,
-                                                            n->dh2b, n->h2);
-    // layer 2: dW2 = dh2^T h1, db2 = sum dh2, dh1 = (dh2 W2) * (h1 > 0)
-    gemm_bf16<true, true><<<grid_for(HID, HID), 256, 0, s>>>(n->dh2b, n->h1, HID, HID, B, nullptr, 0, n->g + P_W2,
-                                                             nullptr, nullptr);
+                                                            n->dh2b, n->h2, n->dh2t, n->ldt);
+    // layer 2 (tensor cores): dW2 = dh2^T h1 (K = the batch, split over CTAs), db2 = sum dh2,
+    // dh1 = (dh2 W2) * (h1 > 0)
+    cudaMemsetAsync(n->g + P_W2, 0, (size_t)HID * HID * sizeof(float), s);
+    tc_gemm<HID>(n, n->dh2t, n->ldt, n->h1t, n->ldt, HID, B, ksplit_for(B), nullptr, 0, nullptr, n->g + P_W2, nullptr,
+                 nullptr);
     col_sum<<<(HID + 127) / 128, 128, 0, s>>>(n->dh, B, HID, n->g + P_B2);
-    gemm_bf16<false, true><<<grid_for(B, HID), 256, 0, s>>>(n->dh2b, n->wb + P_W2, B, HID, HID, nullptr, 0, n->dh,
-                                                            n->dh1b, n->h1);
-    // layer 1: dW1 = dh1^T x, db1 = sum dh1
-    gemm_bf16<true, true><<<grid_for(HID, IN), 256, 0, s>>>(n->dh1b, n->xb, HID, IN, B, nullptr, 0, n->g + P_W1,
-                                                            nullptr, nullptr);
+    tc_gemm<HID>(n, n->dh2b, HID, n->w2t, HID, B, HID, 1, nullptr, 0, n->h1, n->dh, n->dh1b, n->dh1t);
+    // layer 1 (tensor cores): dW1 = dh1^T x, db1 = sum dh1
+    cudaMemsetAsync(n->g + P_W1, 0, (size_t)HID * IN * sizeof(float), s);
+    tc_gemm<IN>(n, n->dh1t, n->ldt, n->xt, n->ldt, HID, B, ksplit_for(B), nullptr, 0, nullptr, n->g + P_W1, nullptr,
+                nullptr);
     col_sum<<<(HID + 127) / 128, 128, 0, s>>>(n->dh, B, HID, n->g + P_B1);
+}
+
+int check_err(LeniaMlp* n) {
+    int h = 0;
+    if (cudaMemcpy(&h, n->err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return err("mlp: error flag read failed");
+    if (h) {
+        cudaMemset(n->err, 0, sizeof(int));
+        return err("mlp: a tensor-core GEMM gave up waiting on a barrier; results are invalid");
+    }
+    return 0;
 }
 
 int upload_batch(LeniaMlp* n, const float* x, const float* y, uint32_t B) {
@@ -238,6 +450,10 @@ LENIA_API int lenia_mlp_create(uint32_t seed, uint32_t max_batch, LeniaMlp** out
               mal(n, &n->dh, B * HID) && mal(n, &n->loss, B) && mal(n, &n->p, B * OUT) && mal(n, &n->xb, B * IN) &&
               mal(n, &n->h1, B * HID) && mal(n, &n->h2, B * HID) && mal(n, &n->dzb, B * OUT) &&
               mal(n, &n->dh2b, B * HID) && mal(n, &n->dh1b, B * HID);
+    n->ldt = (int)((B + 15) / 16 * 16);
+    const size_t T = (size_t)n->ldt;
+    ok = ok && mal(n, &n->xt, T * IN) && mal(n, &n->h1t, T * HID) && mal(n, &n->dh2t, T * HID) &&
+         mal(n, &n->dh1t, T * HID) && mal(n, &n->w2t, (size_t)HID * HID) && mal(n, &n->err, 1);
     if (!ok) {
         lenia_mlp_destroy(n);
         set_thread_error("mlp: device allocation failed");
@@ -267,6 +483,7 @@ LENIA_API int lenia_mlp_create(uint32_t seed, uint32_t max_batch, LeniaMlp** out
     }
     cudaMemsetAsync(n->m, 0, NPARAM * 4, n->stream);
     cudaMemsetAsync(n->v, 0, NPARAM * 4, n->stream);
+    cudaMemsetAsync(n->err, 0, sizeof(int), n->stream);
     if (cudaStreamSynchronize(n->stream) != cudaSuccess) {
         lenia_mlp_destroy(n);
         return err("mlp: initialisation failed");
@@ -298,6 +515,7 @@ LENIA_API int lenia_mlp_set_params(LeniaMlp* n, const float* host, size_t count)
     if (cudaMemcpyAsync(n->w, host, NPARAM * 4, cudaMemcpyHostToDevice, n->stream) != cudaSuccess)
         return err("mlp: upload failed");
     to_bf16<<<(NPARAM + 255) / 256, 256, 0, n->stream>>>(n->w, n->wb, NPARAM);
+    w2_transposed<<<(HID * HID + 255) / 256, 256, 0, n->stream>>>(n->w + P_W2, n->w2t);
     n->t = 0;
     return cudaStreamSynchronize(n->stream) == cudaSuccess ? 0 : err("mlp: set_params failed");
 }
@@ -326,7 +544,8 @@ LENIA_API int lenia_mlp_gradients(LeniaMlp* n, const float* x, const float* y, u
     cudaMemcpyAsync(grads, n->g, NPARAM * 4, cudaMemcpyDeviceToHost, n->stream);
     const float l = mean_loss(n, batch);
     if (loss) *loss = l;
-    return cudaGetLastError() == cudaSuccess ? 0 : err("mlp: gradients failed");
+    if (cudaGetLastError() != cudaSuccess) return err("mlp: gradients failed");
+    return check_err(n);
 }
 
 LENIA_API int lenia_mlp_train_step(LeniaMlp* n, const float* x, const float* y, uint32_t batch, float lr, float* loss) {
@@ -341,10 +560,11 @@ LENIA_API int lenia_mlp_train_step(LeniaMlp* n, const float* x, const float* y, 
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.f - std::pow(b1, (float)n->t), c2 = 1.f - std::pow(b2, (float)n->t);
     adam<<<(NPARAM + 255) / 256, 256, 0, n->stream>>>(n->w, n->g, n->m, n->v, n->wb, NPARAM, lr, b1, b2, 1e-8f, c1, c2);
+    w2_transposed<<<(HID * HID + 255) / 256, 256, 0, n->stream>>>(n->w + P_W2, n->w2t);
     if (cudaGetLastError() != cudaSuccess) return err("mlp: launch failed");
     const float l = mean_loss(n, batch);
     if (loss) *loss = l;
-    return 0;
+    return check_err(n);
 }
 
 LENIA_API int lenia_mlp_predict(LeniaMlp* n, const float* x, uint32_t count, float* probs) {
@@ -360,7 +580,7 @@ LENIA_API int lenia_mlp_predict(LeniaMlp* n, const float* x, uint32_t count, flo
         cudaMemcpyAsync(probs + (size_t)off * OUT, n->p, (size_t)B * OUT * 4, cudaMemcpyDeviceToHost, n->stream);
     }
     if (cudaStreamSynchronize(n->stream) != cudaSuccess) return err("mlp: predict failed");
-    return 0;
+    return check_err(n);
 }
 
 }  // extern "C"
