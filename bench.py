@@ -72,6 +72,9 @@ def parse(argv=None):
     p.add_argument("--no-paths", action="store_true", help="skip timing the other step paths side by side")
     p.add_argument("--grids", action="store_true",
                    help="the reference's own published programs and grids, measured its way: one line per grid")
+    p.add_argument("--only-side", type=int, default=0,
+                   help="keep only the workload's worlds of this side (a size class alone, e.g. for a profile)")
+    p.add_argument("--max-worlds", type=int, default=0, help="keep at most this many of the workload's worlds")
     p.add_argument("--profile-window", action="store_true",
                    help="set up, autotune and warm up the workload, then run exactly one bench step (one graph "
                         "replay) between cudaProfilerStart and cudaProfilerStop and exit: for ncu "
@@ -206,7 +209,20 @@ class Clocks:
 
 # ----------------------------------------------------------------------------- workloads
 
-def workload(name):
+def workload(name, only_side=0, max_worlds=0):
+    """(worlds, seeds, config) of a named workload, optionally cut to one size class and / or its first
+    max_worlds worlds (the config then says so)."""
+    worlds, seeds, cfg = _workload(name)
+    if only_side or max_worlds:
+        keep = [i for i, w in enumerate(worlds) if not only_side or w.width == only_side]
+        keep = keep[:max_worlds] if max_worlds else keep
+        worlds, seeds = [worlds[i] for i in keep], [seeds[i] for i in keep]
+        cfg = dict(cfg, workload=cfg["workload"] + " -- subset: %d world(s)%s" % (
+            len(worlds), " of side %d" % only_side if only_side else ""))
+    return worlds, seeds, cfg
+
+
+def _workload(name):
     import auto_gb300 as ag
     from auto_gb300 import configs
     if name == "single_4096":
@@ -276,7 +292,7 @@ def cpu_leg(worlds, seeds, min_seconds=10.0):
 
 
 def run_reference(args, dist):
-    worlds, seeds, cfg = workload(args.config)
+    worlds, seeds, cfg = workload(args.config, args.only_side, args.max_worlds)
     if dist.rank != 0:
         return
     from oracle.oracle import RefF32
@@ -403,7 +419,7 @@ def profile_window(args, dist):
     autotuning and warm-up as the timed run, for ``ncu --profile-from-start off``."""
     import torch
     from auto_gb300 import Sim
-    worlds, seeds, cfg = workload(args.config)
+    worlds, seeds, cfg = workload(args.config, args.only_side, args.max_worlds)
     sim = Sim(worlds, seed=0, path=args.path)
     seed_all(sim, worlds, seeds)
     if not args.no_autotune:
@@ -424,7 +440,7 @@ def run_ours(args, dist):
     import auto_gb300 as ag
     from auto_gb300 import Sim
 
-    worlds, seeds, cfg = workload(args.config)
+    worlds, seeds, cfg = workload(args.config, args.only_side, args.max_worlds)
     scaling = "weak"
     if dist.world > 1 and len(worlds) > 1:
         # several worlds: split them across ranks (total work fixed); one world: every rank a replica
