@@ -854,6 +854,40 @@ int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, d
     return 0;
 }
 
+// Device time of `steps` steps of one size class as the step graph runs them: the class's launches in
+// `sh` captured into a graph, replayed once to warm up and once under events.  (Events around every
+// launch, as in time_class, leave the GPU idle between small launches that a graph replays back to
+// back, which would favour the one-launch resident step.)
+int time_class_graph(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, double* ms) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue_class(ctx, cl, sh, steps, ctx->stream);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    if (rc || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc ? rc : fail(ctx, LENIA_ECUDA, "autotune capture failed: %s", cudaGetErrorString(e));
+    }
+    cudaGraphExec_t ge = nullptr;
+    e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(ctx, LENIA_ECUDA, "autotune instantiate failed: %s", cudaGetErrorString(e));
+    Events ev;
+    float t = 0;
+    e = cudaEventCreate(&ev.e[0]);
+    if (e == cudaSuccess) e = cudaEventCreate(&ev.e[1]);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ge, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev.e[0], ctx->stream);
+    if (e == cudaSuccess) e = cudaGraphLaunch(ge, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(ev.e[1], ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev.e[1]);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, ev.e[0], ev.e[1]);
+    cudaGraphExecDestroy(ge);
+    if (e != cudaSuccess) return fail(ctx, LENIA_ECUDA, "autotune timing failed: %s", cudaGetErrorString(e));
+    *ms = t;
+    return 0;
+}
+
 // The device-side error flags of the context's kernels: the tensor-core passes' and the resident
 // step's (set when a bounded barrier wait gave up).  Reading them synchronises with the device.
 int check_device_errors(LeniaCtx* ctx) {
@@ -1496,19 +1530,14 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
 
 // The autotuner's search, on states it may advance.  For every size class, in turn: every pair of
 // column and row launch variants, then every chunk budget that gives a different number of chunks.
-// Each candidate is timed over a few steps in the graph's order, and a class keeps its current
-// choice of a dimension unless another is at least 3% faster, so that timing noise does not flip it.
+// Each candidate is timed as a captured graph of a few steps (time_class_graph), and a class keeps
+// its current choice of a dimension unless another is at least 3% faster, so that timing noise does
+// not flip it.
 static int autotune_search(LeniaCtx* ctx) {
     const size_t budgets[] = {0, 128ull << 20, 96ull << 20, 64ull << 20, 32ull << 20};
-    constexpr int WARM = 2, REPS = 8;
+    constexpr int REPS = 8;
     for (auto& cl : ctx->classes) {
-        auto timed = [&](const Shape& sh, double* t) {
-            double c = 0, r = 0;
-            int rc = time_class(ctx, cl, sh, WARM, &c, &r);
-            if (!rc) rc = time_class(ctx, cl, sh, REPS, &c, &r);
-            *t = c + r;
-            return rc;
-        };
+        auto timed = [&](const Shape& sh, double* t) { return time_class_graph(ctx, cl, sh, REPS, t); };
         // pick among candidate shapes; the first candidate is the current shape
         auto pick = [&](std::vector<Shape>& cands, int* best_i) {
             std::vector<double> t(cands.size());
