@@ -89,6 +89,11 @@ struct LeniaCtx {
     cudaStream_t stream = nullptr;
     // the tensor-core paths run a class's few FP32 column items beside the tensor-core launch
     cudaStream_t side = nullptr;
+    // two-branch step graph (FP32 path): the size classes of at most `branch_cells` cells a world run
+    // one after another on `branch`, beside the larger classes on `stream` (0: one branch)
+    cudaStream_t branch = nullptr;
+    cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;
+    int64_t branch_cells = 0;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // asynchronous state copies (lenia_write_states_async / lenia_read_states_async): uploads on
     // `up`, downloads on `down`, through device staging buffers, so that they overlap the
@@ -466,12 +471,24 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
     }
     // Size classes one after another, and within a class its chunks one after another, each chunk for
     // all its steps: a chunk's states and spectra then stay in L2 across its generations.  Measured on
-    // the 384-world batched workload, running the classes one after another was 6% faster than
-    // running them as concurrent graph branches.
+    // the 384-world batched workload, running every class as its own concurrent graph branch was 6%
+    // slower than one after another.  With branch_cells set, the small classes (latency-bound: little
+    // work a launch) run one after another on a second branch beside the large ones, whose launches
+    // fill the GPU; lenia_autotune decides whether that pays.
     cudaStream_t s = ctx->stream;
+    const bool two = ctx->branch_cells > 0 && ctx->path == LENIA_PATH_FP32;
+    if (two) {
+        CK(cudaEventRecord(ctx->ev_bfork, s));
+        CK(cudaStreamWaitEvent(ctx->branch, ctx->ev_bfork, 0));
+    }
     for (auto& cl : ctx->classes) {
-        int rc = enqueue_class(ctx, cl, shape_of(cl), steps, s);
+        const bool small = two && (int64_t)cl.W * cl.H <= ctx->branch_cells;
+        int rc = enqueue_class(ctx, cl, shape_of(cl), steps, small ? ctx->branch : s);
         if (rc) return rc;
+    }
+    if (two) {
+        CK(cudaEventRecord(ctx->ev_bjoin, ctx->branch));
+        CK(cudaStreamWaitEvent(s, ctx->ev_bjoin, 0));
     }
     CK(cudaGetLastError());
     return 0;
@@ -858,10 +875,11 @@ int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, d
 // `sh` captured into a graph, replayed once to warm up and once under events.  (Events around every
 // launch, as in time_class, leave the GPU idle between small launches that a graph replays back to
 // back, which would favour the one-launch resident step.)
-int time_class_graph(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, double* ms) {
+template <class Enqueue>
+int time_graph(LeniaCtx* ctx, Enqueue enqueue, double* ms) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = enqueue_class(ctx, cl, sh, steps, ctx->stream);
+    int rc = enqueue();
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
     if (rc || e != cudaSuccess) {
         if (g) cudaGraphDestroy(g);
@@ -886,6 +904,10 @@ int time_class_graph(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int st
     if (e != cudaSuccess) return fail(ctx, LENIA_ECUDA, "autotune timing failed: %s", cudaGetErrorString(e));
     *ms = t;
     return 0;
+}
+
+int time_class_graph(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, double* ms) {
+    return time_graph(ctx, [&]() { return enqueue_class(ctx, cl, sh, steps, ctx->stream); }, ms);
 }
 
 // The device-side error flags of the context's kernels: the tensor-core passes' and the resident
@@ -944,6 +966,9 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
     };
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&ctx->branch, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_bfork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_bjoin, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1017,6 +1042,9 @@ int lenia_destroy(LeniaCtx* ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->side) cudaStreamDestroy(ctx->side);
+    if (ctx->branch) cudaStreamSynchronize(ctx->branch), cudaStreamDestroy(ctx->branch);
+    if (ctx->ev_bfork) cudaEventDestroy(ctx->ev_bfork);
+    if (ctx->ev_bjoin) cudaEventDestroy(ctx->ev_bjoin);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return 0;
@@ -1489,6 +1517,24 @@ int lenia_set_resident(LeniaCtx* ctx, int32_t mode) {
     return 0;
 }
 
+int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells) {
+    if (!ctx) return LENIA_EINVAL;
+    if (cells < 0) return fail(ctx, LENIA_EINVAL, "cells must be >= 0");
+    if (ctx->path != LENIA_PATH_FP32) return 0;  // one branch on the other paths
+    ctx->branch_cells = cells;
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells) {
+    if (!ctx || !cells) return LENIA_EINVAL;
+    *cells = ctx->branch_cells;
+    return 0;
+}
+
 int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses) {
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
@@ -1602,6 +1648,31 @@ static int autotune_search(LeniaCtx* ctx) {
             cl.chunk_budget = bud[bi];
             cl.chunks = lists[bi];
         }
+    }
+    // The whole step: the small classes on a second graph branch beside the large ones, for every
+    // split point between class sizes, against one branch (kept unless another is 3% faster).
+    if (ctx->path == LENIA_PATH_FP32 && ctx->classes.size() > 1) {
+        std::vector<int64_t> sizes;
+        for (auto& cl : ctx->classes) sizes.push_back((int64_t)cl.W * cl.H);
+        std::sort(sizes.begin(), sizes.end());
+        sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+        std::vector<int64_t> cands{ctx->branch_cells};
+        if (ctx->branch_cells) cands.push_back(0);
+        for (size_t i = 0; i + 1 < sizes.size(); i++)
+            if (sizes[i] != ctx->branch_cells) cands.push_back(sizes[i]);
+        const int64_t was = ctx->branch_cells;
+        std::vector<double> t(cands.size());
+        int rc = 0;
+        for (size_t i = 0; i < cands.size() && !rc; i++) {
+            ctx->branch_cells = cands[i];
+            rc = time_graph(ctx, [&]() { return enqueue_steps(ctx, REPS); }, &t[i]);
+        }
+        ctx->branch_cells = was;
+        if (rc) return rc;
+        size_t b = 0;
+        for (size_t i = 1; i < cands.size(); i++)
+            if (t[i] < t[b]) b = i;
+        if (t[b] < 0.97 * t[0]) ctx->branch_cells = cands[b];
     }
     return 0;
 }

@@ -390,7 +390,8 @@ def summarise_traffic(csv_path, config, path, gens):
     for name, m in rows:
         b = m.get("dram__bytes_read.sum", 0.0) + m.get("dram__bytes_write.sum", 0.0)
         t = m.get("gpu__time_duration.sum", 0.0)
-        key = name.split("<")[0].split("(")[0].strip()
+        # the kernel's own name: no return type, namespaces or template arguments
+        key = name.split("(")[0].split("<")[0].replace("void ", "").split("::")[-1].strip()
         f = fam.setdefault(key, {"launches": 0, "dram_bytes": 0.0, "time_s": 0.0})
         f["launches"] += 1
         f["dram_bytes"] += b
@@ -634,7 +635,7 @@ def run_ours(args, dist):
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": (launches_per_gen * G + launches_per_step_resident) * args.steps,
-               "launch_variants": variants, "classes": classes,
+               "launch_variants": variants, "classes": classes, "branch_split_cells": sim.branch_split,
                "paths": paths,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
         print(json.dumps(out))

@@ -179,7 +179,8 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
  * and keeps the fastest, one dimension after another: the cluster-resident step against the two
  * launches per generation (where it applies), then for two-pass classes the pair of column and row
  * launch variants and every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that
- * changes the class's number of chunks.
+ * changes the class's number of chunks; then, for the whole step, the split of small classes onto a
+ * second graph branch (lenia_set_branch_split).
  * The states are saved first and restored afterwards, also when it fails.  Rebuilds the step
  * graphs.  Optional; defaults are reasonable. */
 LENIA_API int lenia_autotune(LeniaCtx* ctx);
@@ -206,6 +207,13 @@ LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */
 LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
+/* Two-branch step graph (FP32 path): size classes of at most `cells` cells a world run one after
+ * another on a second graph branch, beside the larger classes, so that the small classes' latency-bound
+ * launches share the GPU with the large classes' (0: one branch, every class in turn, the default).
+ * lenia_autotune tries every split between class sizes.  Results do not depend on it (bit for bit).
+ * Rebuilds the step graphs.  lenia_branch_split reports the current split.  No reference counterpart. */
+LENIA_API int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells);
+LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells);
 /* The cluster-resident step, on (mode 1; 2 + v: on in launch variant v, which transforms 16, 8 or 4
  * sequences at a time for v = 0, 1, 2) or off (mode 0, the default until lenia_autotune chooses)
  * for every size class it applies to: square worlds of 128, 192, 256, 384 or 512 with one channel and one Lenia kernel on

@@ -506,3 +506,19 @@ def test_resident_step_applies_only_where_it_can():
     with Sim([w for w in worlds if w.width == 256][:2], seed=0, path="bf16x3") as sim:
         sim.set_resident(True)
         assert all(v["resident"] == 0 for v in sim.shapes().values())
+
+
+def test_two_branch_graph_gives_the_same_bits():
+    """Running the small size classes on a second graph branch beside the large ones only reorders
+    independent launches: every state after 5 steps is bit-identical to one branch."""
+    worlds = configs.batched(64)
+    outs = []
+    for split in (0, 256 * 256, 512 * 512):
+        with Sim(worlds, seed=0) as sim:
+            for i, w in enumerate(worlds):
+                sim.seed_patches(i, i, w.seed.patches)
+            sim.set_branch_split(split)
+            assert sim.branch_split == split
+            sim.step(5)
+            outs.append(sim.read_states().copy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
