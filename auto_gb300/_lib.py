@@ -91,8 +91,8 @@ def _declare(L):
         "lenia_class_shapes": [vp, ctypes.POINTER(ctypes.c_int32), sz, ctypes.POINTER(ctypes.c_size_t)],
         "lenia_set_chunk_budget": [vp, u32],
         "lenia_set_resident": [vp, i32],
-        "lenia_set_branch_split": [vp, ctypes.c_int64],
-        "lenia_branch_split": [vp, ctypes.POINTER(ctypes.c_int64)],
+        "lenia_set_branch_split": [vp, ctypes.c_int64, i32],
+        "lenia_branch_split": [vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int32)],
         "lenia_profile_step": [vp, u32, _c_float_p],
         "lenia_profile_classes": [vp, u32, _c_float_p, sz, ctypes.POINTER(ctypes.c_size_t)],
         "lenia_kernel_spectrum": [ctypes.POINTER(LeniaKernel), u32, u32, _c_float_p, sz],

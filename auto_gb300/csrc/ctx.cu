@@ -91,9 +91,12 @@ struct LeniaCtx {
     cudaStream_t side = nullptr;
     // two-branch step graph (FP32 path): the size classes of at most `branch_cells` cells a world run
     // one after another on `branch`, beside the larger classes on `stream` (0: one branch)
-    cudaStream_t branch = nullptr;
-    cudaEvent_t ev_bfork = nullptr, ev_bjoin = nullptr;
+    // with branch_each, every such class gets a branch of its own
+    static constexpr int MAX_BRANCHES = 8;
+    cudaStream_t branch[MAX_BRANCHES] = {};
+    cudaEvent_t ev_bfork = nullptr, ev_bjoin[MAX_BRANCHES] = {};
     int64_t branch_cells = 0;
+    int branch_each = 0;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // asynchronous state copies (lenia_write_states_async / lenia_read_states_async): uploads on
     // `up`, downloads on `down`, through device staging buffers, so that they overlap the
@@ -476,19 +479,25 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
     // work a launch) run one after another on a second branch beside the large ones, whose launches
     // fill the GPU; lenia_autotune decides whether that pays.
     cudaStream_t s = ctx->stream;
-    const bool two = ctx->branch_cells > 0 && ctx->path == LENIA_PATH_FP32;
-    if (two) {
-        CK(cudaEventRecord(ctx->ev_bfork, s));
-        CK(cudaStreamWaitEvent(ctx->branch, ctx->ev_bfork, 0));
-    }
+    const bool split = ctx->branch_cells > 0 && ctx->path == LENIA_PATH_FP32;
+    int used = 0;  // side branches in use
+    if (split) CK(cudaEventRecord(ctx->ev_bfork, s));
     for (auto& cl : ctx->classes) {
-        const bool small = two && (int64_t)cl.W * cl.H <= ctx->branch_cells;
-        int rc = enqueue_class(ctx, cl, shape_of(cl), steps, small ? ctx->branch : s);
+        cudaStream_t on = s;
+        if (split && (int64_t)cl.W * cl.H <= ctx->branch_cells) {
+            const int b = ctx->branch_each ? std::min(used, LeniaCtx::MAX_BRANCHES - 1) : 0;
+            if (b >= used) {
+                CK(cudaStreamWaitEvent(ctx->branch[b], ctx->ev_bfork, 0));
+                used = b + 1;
+            }
+            on = ctx->branch[b];
+        }
+        int rc = enqueue_class(ctx, cl, shape_of(cl), steps, on);
         if (rc) return rc;
     }
-    if (two) {
-        CK(cudaEventRecord(ctx->ev_bjoin, ctx->branch));
-        CK(cudaStreamWaitEvent(s, ctx->ev_bjoin, 0));
+    for (int b = 0; b < used; b++) {
+        CK(cudaEventRecord(ctx->ev_bjoin[b], ctx->branch[b]));
+        CK(cudaStreamWaitEvent(s, ctx->ev_bjoin[b], 0));
     }
     CK(cudaGetLastError());
     return 0;
@@ -966,9 +975,7 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
     };
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&ctx->branch, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_bfork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_bjoin, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
         cudaStreamCreateWithFlags(&ctx->up, cudaStreamNonBlocking) != cudaSuccess ||
@@ -981,6 +988,12 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         fail(ctx, LENIA_ECUDA, "stream creation failed");
         return bail(LENIA_ECUDA);
     }
+    for (int b = 0; b < LeniaCtx::MAX_BRANCHES; b++)
+        if (cudaStreamCreateWithFlags(&ctx->branch[b], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_bjoin[b], cudaEventDisableTiming) != cudaSuccess) {
+            fail(ctx, LENIA_ECUDA, "stream creation failed");
+            return bail(LENIA_ECUDA);
+        }
     // twiddles exp(-2 pi i t / TWN) from FP64
     {
         std::vector<float2> tw(lfft::TWN);
@@ -1042,9 +1055,11 @@ int lenia_destroy(LeniaCtx* ctx) {
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
     if (ctx->side) cudaStreamDestroy(ctx->side);
-    if (ctx->branch) cudaStreamSynchronize(ctx->branch), cudaStreamDestroy(ctx->branch);
+    for (int b = 0; b < LeniaCtx::MAX_BRANCHES; b++) {
+        if (ctx->branch[b]) cudaStreamSynchronize(ctx->branch[b]), cudaStreamDestroy(ctx->branch[b]);
+        if (ctx->ev_bjoin[b]) cudaEventDestroy(ctx->ev_bjoin[b]);
+    }
     if (ctx->ev_bfork) cudaEventDestroy(ctx->ev_bfork);
-    if (ctx->ev_bjoin) cudaEventDestroy(ctx->ev_bjoin);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return 0;
@@ -1517,11 +1532,12 @@ int lenia_set_resident(LeniaCtx* ctx, int32_t mode) {
     return 0;
 }
 
-int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells) {
+int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells, int32_t each) {
     if (!ctx) return LENIA_EINVAL;
-    if (cells < 0) return fail(ctx, LENIA_EINVAL, "cells must be >= 0");
+    if (cells < 0 || (each != 0 && each != 1)) return fail(ctx, LENIA_EINVAL, "cells must be >= 0, each 0 or 1");
     if (ctx->path != LENIA_PATH_FP32) return 0;  // one branch on the other paths
     ctx->branch_cells = cells;
+    ctx->branch_each = each;
     CK(cudaStreamSynchronize(ctx->stream));
     int rc = rebuild_graphs(ctx);
     if (rc) return rc;
@@ -1529,9 +1545,10 @@ int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells) {
     return 0;
 }
 
-int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells) {
-    if (!ctx || !cells) return LENIA_EINVAL;
+int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells, int32_t* each) {
+    if (!ctx || !cells || !each) return LENIA_EINVAL;
     *cells = ctx->branch_cells;
+    *each = ctx->branch_each;
     return 0;
 }
 
@@ -1656,23 +1673,28 @@ static int autotune_search(LeniaCtx* ctx) {
         for (auto& cl : ctx->classes) sizes.push_back((int64_t)cl.W * cl.H);
         std::sort(sizes.begin(), sizes.end());
         sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
-        std::vector<int64_t> cands{ctx->branch_cells};
-        if (ctx->branch_cells) cands.push_back(0);
+        // (split, each): candidate 0 is the current choice
+        std::vector<std::pair<int64_t, int>> cands{{ctx->branch_cells, ctx->branch_each}};
+        if (ctx->branch_cells) cands.push_back({0, 0});
         for (size_t i = 0; i + 1 < sizes.size(); i++)
-            if (sizes[i] != ctx->branch_cells) cands.push_back(sizes[i]);
-        const int64_t was = ctx->branch_cells;
+            for (int each = 0; each < 2; each++)
+                if (!(sizes[i] == ctx->branch_cells && each == ctx->branch_each) && !(each && i == 0))
+                    cands.push_back({sizes[i], each});
+        const auto was = cands[0];
         std::vector<double> t(cands.size());
         int rc = 0;
         for (size_t i = 0; i < cands.size() && !rc; i++) {
-            ctx->branch_cells = cands[i];
+            ctx->branch_cells = cands[i].first;
+            ctx->branch_each = cands[i].second;
             rc = time_graph(ctx, [&]() { return enqueue_steps(ctx, REPS); }, &t[i]);
         }
-        ctx->branch_cells = was;
+        ctx->branch_cells = was.first;
+        ctx->branch_each = was.second;
         if (rc) return rc;
         size_t b = 0;
         for (size_t i = 1; i < cands.size(); i++)
             if (t[i] < t[b]) b = i;
-        if (t[b] < 0.97 * t[0]) ctx->branch_cells = cands[b];
+        if (t[b] < 0.97 * t[0]) ctx->branch_cells = cands[b].first, ctx->branch_each = cands[b].second;
     }
     return 0;
 }

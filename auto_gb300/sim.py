@@ -215,15 +215,17 @@ class Sim:
         (see lenia_set_resident)."""
         self._check(self._L.lenia_set_resident(self._ctx, (2 + variant if variant >= 0 else 1) if on else 0))
 
-    def set_branch_split(self, cells: int):
-        """Classes of at most `cells` cells a world on a second graph branch (see lenia_set_branch_split)."""
-        self._check(self._L.lenia_set_branch_split(self._ctx, int(cells)))
+    def set_branch_split(self, cells: int, each: bool = False):
+        """Classes of at most `cells` cells a world on side graph branches, one after another or each
+        on its own (see lenia_set_branch_split)."""
+        self._check(self._L.lenia_set_branch_split(self._ctx, int(cells), 1 if each else 0))
 
     @property
-    def branch_split(self) -> int:
-        c = ctypes.c_int64()
-        self._check(self._L.lenia_branch_split(self._ctx, ctypes.byref(c)))
-        return int(c.value)
+    def branch_split(self):
+        """(cells, each) of the step graph's branch split."""
+        c, e = ctypes.c_int64(), ctypes.c_int32()
+        self._check(self._L.lenia_branch_split(self._ctx, ctypes.byref(c), ctypes.byref(e)))
+        return int(c.value), bool(e.value)
 
     def set_chunk_budget(self, mib: int):
         """Pin every size class's chunk budget in MiB (see lenia_set_chunk_budget); 0 = one chunk."""

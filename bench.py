@@ -635,7 +635,7 @@ def run_ours(args, dist):
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": scaling,
                "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg, "roofline": roofline,
                "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": (launches_per_gen * G + launches_per_step_resident) * args.steps,
-               "launch_variants": variants, "classes": classes, "branch_split_cells": sim.branch_split,
+               "launch_variants": variants, "classes": classes, "branch_split": {"cells": sim.branch_split[0], "each_own_branch": sim.branch_split[1]},
                "paths": paths,
                "ms_per_generation": ms_per_gen, "reference_published": PUBLISHED_REF}
         print(json.dumps(out))

@@ -207,13 +207,15 @@ LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */
 LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
-/* Two-branch step graph (FP32 path): size classes of at most `cells` cells a world run one after
- * another on a second graph branch, beside the larger classes, so that the small classes' latency-bound
- * launches share the GPU with the large classes' (0: one branch, every class in turn, the default).
- * lenia_autotune tries every split between class sizes.  Results do not depend on it (bit for bit).
- * Rebuilds the step graphs.  lenia_branch_split reports the current split.  No reference counterpart. */
-LENIA_API int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells);
-LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells);
+/* Branches of the step graph (FP32 path): size classes of at most `cells` cells a world run on graph
+ * branches beside the larger classes -- one after another on one side branch (each = 0), or each on
+ * a branch of its own (each = 1) -- so that the small classes' latency-bound launches share the GPU
+ * with the large classes' (cells = 0: one branch, every class in turn, the default).  lenia_autotune
+ * tries every split between class sizes, both ways.  Results do not depend on it (bit for bit).
+ * Rebuilds the step graphs.  lenia_branch_split reports the current choice.  No reference
+ * counterpart. */
+LENIA_API int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells, int32_t each);
+LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells, int32_t* each);
 /* The cluster-resident step, on (mode 1; 2 + v: on in launch variant v, which transforms 16, 8 or 4
  * sequences at a time for v = 0, 1, 2) or off (mode 0, the default until lenia_autotune chooses)
  * for every size class it applies to: square worlds of 128, 192, 256, 384 or 512 with one channel and one Lenia kernel on

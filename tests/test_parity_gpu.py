@@ -509,16 +509,18 @@ def test_resident_step_applies_only_where_it_can():
 
 
 def test_two_branch_graph_gives_the_same_bits():
-    """Running the small size classes on a second graph branch beside the large ones only reorders
-    independent launches: every state after 5 steps is bit-identical to one branch."""
+    """Running the small size classes on side graph branches beside the large ones (one side branch,
+    or one each) only reorders independent launches: every state after 5 steps is bit-identical to
+    one branch."""
     worlds = configs.batched(64)
     outs = []
-    for split in (0, 256 * 256, 512 * 512):
+    for split, each in ((0, False), (256 * 256, False), (512 * 512, False), (384 * 384, True)):
         with Sim(worlds, seed=0) as sim:
             for i, w in enumerate(worlds):
                 sim.seed_patches(i, i, w.seed.patches)
-            sim.set_branch_split(split)
-            assert sim.branch_split == split
+            sim.set_branch_split(split, each)
+            assert sim.branch_split == (split, each)
             sim.step(5)
             outs.append(sim.read_states().copy())
-    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)
