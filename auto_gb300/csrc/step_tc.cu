@@ -166,6 +166,26 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t t_x = tbase + S::REGION;     // D of GEMMs A, C, D
     const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
 
+    // The twiddles of the two hand-overs from per-thread tables.  A thread's rows are r = b*128 + tid,
+    // and 128 is a multiple of H1 and of H2, so its y1 (A -> B) and its k2 (C -> D) are the same in
+    // every row block: exp(-2 pi i y1 k2 / H) with k2 = 16 q + u is A_q[q] * A_u[u], and with
+    // y1 = 16 q + u it is C_q[q] * C_u[u] -- two exactly rounded table values and one product,
+    // instead of a load from the 24576-entry table per element.
+    constexpr int QA = S::H2 / 16, QC = S::H1 / 16;
+    float2 Aq[QA], Au[16], Cq[QC], Cu[16];
+    {
+        const int y1 = tid % S::H1, k2 = tid % S::H2;
+#pragma unroll
+        for (int q = 0; q < QA; q++) Aq[q] = twid<S::H>(tw, y1, 16 * q);
+#pragma unroll
+        for (int q = 0; q < QC; q++) Cq[q] = twid<S::H>(tw, k2, 16 * q);
+#pragma unroll
+        for (int u = 0; u < 16; u++) {
+            Au[u] = twid<S::H>(tw, y1, u);
+            Cu[u] = twid<S::H>(tw, k2, u);
+        }
+    }
+
     // DFT matrices (hi, lo) once per CTA; first tile group
     if (tid == 0) {
         const uint32_t fbytes = (S::FA + (S::SAME ? 0 : S::FB)) * S::NOP;
@@ -249,13 +269,14 @@ __global__ void __launch_bounds__(128, 1)
         // ---- A -> B: twiddle exp(-2 pi i y1 k2 / H), rows (c, k2), K (re/im, y1)
         for (int b = 0; b < S::MA / 128; b++) {
             const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
+#pragma unroll
             for (int q = 0; q < S::NA / 32; q++) {
                 float v[32];
                 tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NA + 32 * q), v);
 #pragma unroll
                 for (int u = 0; u < 16; u++) {
                     const int k2 = 16 * q + u;
-                    const float2 w = twid<S::H>(tw, y1, k2);
+                    const float2 w = lfft::cmul(Aq[q], Au[u]);
                     const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
                     const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
                     const int rr = c * S::H2 + k2;
@@ -311,13 +332,14 @@ __global__ void __launch_bounds__(128, 1)
             // ---- C -> D: twiddle exp(-2 pi i k2 y1 / H); rows (c, y1), K (re/im, k2)
             for (int b = 0; b < S::MB / 128; b++) {
                 const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
+#pragma unroll
                 for (int q = 0; q < S::NB / 32; q++) {
                     float v[32];
                     tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
 #pragma unroll
                     for (int u = 0; u < 16; u++) {
                         const int y1 = 16 * q + u;
-                        const float2 w = twid<S::H>(tw, k2, y1);
+                        const float2 w = lfft::cmul(Cq[q], Cu[u]);
                         const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
                         const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
                         const int rr = c * S::H1 + y1;
@@ -427,7 +449,11 @@ bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups,
                   int* err, cudaStream_t st, int reserve_sms) {
     static int attr = 0;
     if (!attr) {
-        if (cudaFuncSetAttribute(col_pass_tc<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess)
+        // the whole shared-memory carveout: two CTAs of these shapes fit an SM, and with the default
+        // carveout the occupancy query answered one (measured at 1024: 4 warps per SM)
+        if (cudaFuncSetAttribute(col_pass_tc<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess ||
+            cudaFuncSetAttribute(col_pass_tc<S>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                 cudaSharedmemCarveoutMaxShared) != cudaSuccess)
             return false;
         attr = 1;
     }
