@@ -39,8 +39,9 @@ struct TcShape {
     static constexpr int NOP = X3 ? 2 : 1;            // hi/lo copies
     static constexpr int MA = CT * H1, KA = 2 * H2, NA = 2 * H2;
     static constexpr int MB = CT * H2, KB = 2 * H1, NB = 2 * H1;
-    static constexpr int OPND = 2 * CT * H * E;       // one operand copy (MA*KA*E == MB*KB*E)
-    static constexpr int FA = NA * KA * E, FB = NB * KB * E;
+    static constexpr int LBO = 144;                   // padded K-major layout (kmajor_offset)
+    static constexpr int OPND = kmajor_bytes(MA, KA, E, LBO);  // one operand copy (== MB x KB)
+    static constexpr int FA = kmajor_bytes(NA, KA, E, LBO), FB = kmajor_bytes(NB, KB, E, LBO);
     static constexpr bool SAME = H1 == H2;
     static constexpr int STG = CT * H * 8;            // fp32 complex tile group
     static constexpr int OFF_F2 = OPND * NOP;
@@ -51,7 +52,8 @@ struct TcShape {
     static constexpr int COLS_A = (MA / 128) * NA, COLS_B = (MB / 128) * NB;
     static constexpr int REGION = COLS_A > COLS_B ? COLS_A : COLS_B;
     static constexpr int TCOLS = 2 * REGION <= 32 ? 32 : (2 * REGION <= 64 ? 64 : (2 * REGION <= 128 ? 128 : (2 * REGION <= 256 ? 256 : 512)));
-    static_assert(OPND * NOP == STG, "the output staging reuses the operand area");
+    static_assert(kmajor_bytes(MB, KB, E, LBO) == OPND, "both GEMM shapes fill one operand area");
+    static_assert(OPND * NOP >= STG, "the output staging reuses the operand area");
     static_assert(MA % 128 == 0 && MB % 128 == 0, "row blocks of 128");
     static_assert(NA % 32 == 0 && NB % 32 == 0, "TMEM loads of 32 columns");
     static_assert(2 * REGION <= 512, "TMEM");
@@ -70,52 +72,55 @@ __device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uin
     lo = *reinterpret_cast<const uint32_t*>(&l);
 }
 
-template <bool X3>
+template <bool X3, int LBO>
 __device__ __forceinline__ void store_elem(uint8_t* op, int opnd_bytes, int r, int k, int K, float v) {
     if (X3) {
-        const uint32_t off = kmajor_offset(r, k, K, 2);
+        const uint32_t off = kmajor_offset(r, k, K, 2, LBO);
         const __nv_bfloat16 hi = __float2bfloat16_rn(v);
         const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
         *reinterpret_cast<__nv_bfloat16*>(op + off) = hi;
         *reinterpret_cast<__nv_bfloat16*>(op + opnd_bytes + off) = lo;
     } else {
-        *reinterpret_cast<uint32_t*>(op + kmajor_offset(r, k, K, 4)) = to_tf32(v);
+        *reinterpret_cast<uint32_t*>(op + kmajor_offset(r, k, K, 4, LBO)) = to_tf32(v);
     }
 }
 
 // 16 bytes of consecutive K: 8 values (bf16 hi and lo) or 4 (tf32), starting at k0.
-template <bool X3>
+template <bool X3, int LBO>
 __device__ __forceinline__ void store_chunk(uint8_t* op, int opnd_bytes, int r, int k0, int K, const float* v) {
     if (X3) {
         uint32_t hi[4], lo[4];
 #pragma unroll
         for (int i = 0; i < 4; i++) split_bf16x2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
-        const uint32_t off = kmajor_offset(r, k0, K, 2);
+        const uint32_t off = kmajor_offset(r, k0, K, 2, LBO);
         *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
         *reinterpret_cast<uint4*>(op + opnd_bytes + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
     } else {
-        *reinterpret_cast<uint4*>(op + kmajor_offset(r, k0, K, 4)) =
+        *reinterpret_cast<uint4*>(op + kmajor_offset(r, k0, K, 4, LBO)) =
             make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
     }
 }
 
 // One GEMM: D[rows of M in blocks of 128] (+)= A (M x K, K-major) * F^T (F: N x K, K-major).
-template <bool X3>
+// Both operands in the K-major layout with K-adjacent core matrices LBO bytes apart (kmajor_offset).
+// An MMA consumes 32 bytes of K (two core matrices), so consecutive MMAs start 2 LBO apart.
+template <bool X3, int LBO = 128>
 __device__ __forceinline__ void issue_gemm(uint32_t d_tmem, uint32_t a_saddr, uint32_t a_lo_off, int M, int K,
                                            uint32_t f_saddr, uint32_t f_lo_off, int N, uint32_t idesc) {
     constexpr int E = X3 ? 2 : 4;
-    const uint32_t sbo = (uint32_t)(K * E * 8);
+    const uint32_t sbo = (uint32_t)(K * E / 16 * LBO);
     const int ksteps = K * E / 32;
     for (int b = 0; b < M / 128; b++) {
         const uint32_t d = d_tmem + (uint32_t)(b * N);
         const uint32_t a0 = a_saddr + (uint32_t)b * 16u * sbo;
         for (int s = 0; s < ksteps; s++) {
-            const uint64_t ad = smem_desc(a0 + 256u * s, 128, sbo);
-            const uint64_t bd = smem_desc(f_saddr + 256u * s, 128, sbo);
+            const uint32_t ko = 2u * LBO * s;
+            const uint64_t ad = smem_desc(a0 + ko, LBO, sbo);
+            const uint64_t bd = smem_desc(f_saddr + ko, LBO, sbo);
             mma<!X3>(d, ad, bd, idesc, s > 0 ? 1u : 0u);
             if (X3) {
-                mma<false>(d, ad, smem_desc(f_saddr + f_lo_off + 256u * s, 128, sbo), idesc, 1u);
-                mma<false>(d, smem_desc(a0 + a_lo_off + 256u * s, 128, sbo), bd, idesc, 1u);
+                mma<false>(d, ad, smem_desc(f_saddr + f_lo_off + ko, LBO, sbo), idesc, 1u);
+                mma<false>(d, smem_desc(a0 + a_lo_off + ko, LBO, sbo), bd, idesc, 1u);
             }
         }
     }
@@ -209,7 +214,7 @@ __global__ void __launch_bounds__(128, 1)
     auto gemm = [&](uint32_t d, uint32_t a_off, int M, int K, uint32_t f_addr, uint32_t f_lo, int N, uint32_t idesc) {
         if (tid == 0) {
             tc_fence_after();
-            issue_gemm<S::X3>(d, smem_u32(op), a_off, M, K, f_addr, f_lo, N, idesc);
+            issue_gemm<S::X3, S::LBO>(d, smem_u32(op), a_off, M, K, f_addr, f_lo, N, idesc);
             mma_commit(bar_mma);
         }
         if (__syncthreads_or(!mbar_wait(bar_mma, ph_mma))) {
@@ -248,8 +253,8 @@ __global__ void __launch_bounds__(128, 1)
                     re[u] = v.x;
                     im[u] = v.y;
                 }
-                store_chunk<S::X3>(op, S::OPND, r, y2, S::KA, re);
-                store_chunk<S::X3>(op, S::OPND, r, S::H2 + y2, S::KA, im);
+                store_chunk<S::X3, S::LBO>(op, S::OPND, r, y2, S::KA, re);
+                store_chunk<S::X3, S::LBO>(op, S::OPND, r, S::H2 + y2, S::KA, im);
             }
         }
         fence_async_smem();
@@ -280,8 +285,8 @@ __global__ void __launch_bounds__(128, 1)
                     const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
                     const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
                     const int rr = c * S::H2 + k2;
-                    store_elem<S::X3>(op, S::OPND, rr, y1, S::KB, re);
-                    store_elem<S::X3>(op, S::OPND, rr, S::H1 + y1, S::KB, im);
+                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, y1, S::KB, re);
+                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H1 + y1, S::KB, im);
                 }
             }
         }
@@ -316,8 +321,8 @@ __global__ void __launch_bounds__(128, 1)
                     constexpr int CH = S::X3 ? 8 : 4;
 #pragma unroll
                     for (int u = 0; u < 16; u += CH) {
-                        store_chunk<S::X3>(op, S::OPND, r, 16 * q + u, S::KB, re + u);
-                        store_chunk<S::X3>(op, S::OPND, r, S::H1 + 16 * q + u, S::KB, im + u);
+                        store_chunk<S::X3, S::LBO>(op, S::OPND, r, 16 * q + u, S::KB, re + u);
+                        store_chunk<S::X3, S::LBO>(op, S::OPND, r, S::H1 + 16 * q + u, S::KB, im + u);
                     }
                 }
             }
@@ -343,8 +348,8 @@ __global__ void __launch_bounds__(128, 1)
                         const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
                         const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
                         const int rr = c * S::H1 + y1;
-                        store_elem<S::X3>(op, S::OPND, rr, k2, S::KA, re);
-                        store_elem<S::X3>(op, S::OPND, rr, S::H2 + k2, S::KA, im);
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, k2, S::KA, re);
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H2 + k2, S::KA, im);
                     }
                 }
             }
@@ -406,9 +411,9 @@ namespace {
 
 // DFT matrix of length n as the B operand: rows (k, re/im out), K (re/im in, y), exp(-2 pi i y k / n),
 // in the K-major layout, as bf16 hi then lo, or tf32 -- rounded from FP64.
-void build_dft_operand(int n, bool x3, std::vector<uint8_t>& out) {
+void build_dft_operand(int n, bool x3, std::vector<uint8_t>& out, int lbo) {
     const int N = 2 * n, K = 2 * n, E = x3 ? 2 : 4;
-    const size_t bytes = (size_t)N * K * E;
+    const size_t bytes = (size_t)kmajor_bytes(N, K, E, lbo);
     const size_t base = out.size();
     out.resize(base + bytes * (x3 ? 2 : 1), 0);
     for (int row = 0; row < N; row++)
@@ -416,7 +421,7 @@ void build_dft_operand(int n, bool x3, std::vector<uint8_t>& out) {
             const int k = row / 2, ro = row % 2, ri = kk / n, y = kk % n;
             const double th = 2.0 * M_PI * (double)((long)y * k % n) / n, c = std::cos(th), s = std::sin(th);
             const double v = ro == 0 ? (ri == 0 ? c : s) : (ri == 0 ? -s : c);
-            const uint32_t off = kmajor_offset(row, kk, K, E);
+            const uint32_t off = kmajor_offset(row, kk, K, E, lbo);
             if (x3) {
                 const __nv_bfloat16 hi = __float2bfloat16_rn((float)v);
                 const __nv_bfloat16 lo = __float2bfloat16_rn((float)(v - (double)__bfloat162float(hi)));
@@ -507,8 +512,10 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
     }
     const bool x3 = path == LENIA_PATH_BF16X3;
     std::vector<uint8_t> host;
-    build_dft_operand(s->H2, x3, host);                  // F_H2 (hi, lo)
-    if (s->H1 != s->H2) build_dft_operand(s->H1, x3, host);  // F_H1 (hi, lo)
+    // the 4096-point kernel (step_tc64.cu) packs its operands (LBO 128); the others pad them (144)
+    const int lbo = H == 4096 ? 128 : 144;
+    build_dft_operand(s->H2, x3, host, lbo);                  // F_H2 (hi, lo)
+    if (s->H1 != s->H2) build_dft_operand(s->H1, x3, host, lbo);  // F_H1 (hi, lo)
     void* d = nullptr;
     if (cudaMalloc(&d, host.size()) != cudaSuccess ||
         cudaMemcpy(d, host.data(), host.size(), cudaMemcpyHostToDevice) != cudaSuccess) {

@@ -16,9 +16,18 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)_
 
 // ----------------------------------------------------------------- operand layout
 // Byte offset of element (row r, k) in a K-major, no-swizzle operand with K elements per row.
-__host__ __device__ __forceinline__ uint32_t kmajor_offset(int r, int k, int K, int elem_bytes) {
+// `lbo` is the distance between core matrices adjacent along K (the descriptor's LBO): 128 packs
+// them; 144 leaves 16 bytes between them, so that the 16-byte rows of K-adjacent core matrices fall
+// 4 banks apart instead of on the same banks (a warp writing one operand row with 2-byte stores then
+// touches every core matrix of the row in one wavefront).  8-row groups are (K * elem_bytes / 16) * lbo
+// bytes apart (the descriptor's SBO).
+__host__ __device__ __forceinline__ uint32_t kmajor_offset(int r, int k, int K, int elem_bytes, int lbo = 128) {
     const int kb = k * elem_bytes;
-    return (uint32_t)(((r >> 3) * (K * elem_bytes / 16) + (kb >> 4)) * 128 + (r & 7) * 16 + (kb & 15));
+    return (uint32_t)(((r >> 3) * (K * elem_bytes / 16) + (kb >> 4)) * lbo + (r & 7) * 16 + (kb & 15));
+}
+// Bytes of an M x K operand in that layout.
+__host__ __device__ constexpr int kmajor_bytes(int M, int K, int elem_bytes, int lbo = 128) {
+    return (M / 8) * (K * elem_bytes / 16) * lbo;
 }
 
 // tcgen05 shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), version 1 in
