@@ -31,7 +31,7 @@
 namespace lenia {
 using namespace tc;
 
-template <int H1_, int H2_, int CT_, bool X3_>
+template <int H1_, int H2_, int CT_, bool X3_, int LBO_>
 struct TcShape {
     static constexpr int H1 = H1_, H2 = H2_, CT = CT_, H = H1 * H2;
     static constexpr bool X3 = X3_;
@@ -39,7 +39,7 @@ struct TcShape {
     static constexpr int NOP = X3 ? 2 : 1;            // hi/lo copies
     static constexpr int MA = CT * H1, KA = 2 * H2, NA = 2 * H2;
     static constexpr int MB = CT * H2, KB = 2 * H1, NB = 2 * H1;
-    static constexpr int LBO = 144;                   // padded K-major layout (kmajor_offset)
+    static constexpr int LBO = LBO_;                  // K-major layout, packed (128) or padded (144): kmajor_offset
     static constexpr int OPND = kmajor_bytes(MA, KA, E, LBO);  // one operand copy (== MB x KB)
     static constexpr int FA = kmajor_bytes(NA, KA, E, LBO), FB = kmajor_bytes(NB, KB, E, LBO);
     static constexpr bool SAME = H1 == H2;
@@ -47,7 +47,10 @@ struct TcShape {
     static constexpr int OFF_F2 = OPND * NOP;
     static constexpr int OFF_F1 = OFF_F2 + FA * NOP;
     static constexpr int OFF_STG = OFF_F1 + (SAME ? 0 : FB * NOP);
-    static constexpr int OFF_BAR = OFF_STG + STG;
+    static constexpr int HQ = (H / 2 + 1 + 3) / 4 * 4;  // kernel-spectrum row stride (floats)
+    static constexpr int OFF_KH = OFF_STG + STG;      // the group's CT kernel-spectrum rows
+    static constexpr int KHB = CT * HQ * 4;
+    static constexpr int OFF_BAR = OFF_KH + KHB;
     static constexpr int SMEM = OFF_BAR + 64;
     static constexpr int COLS_A = (MA / 128) * NA, COLS_B = (MB / 128) * NB;
     static constexpr int REGION = COLS_A > COLS_B ? COLS_A : COLS_B;
@@ -57,6 +60,7 @@ struct TcShape {
     static_assert(MA % 128 == 0 && MB % 128 == 0, "row blocks of 128");
     static_assert(NA % 32 == 0 && NB % 32 == 0, "TMEM loads of 32 columns");
     static_assert(2 * REGION <= 512, "TMEM");
+    static_assert(SMEM <= 232448, "shared memory of one CTA");
 };
 
 // ------------------------------------------------------------------ operand stores
@@ -151,7 +155,9 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t* bar_ld = reinterpret_cast<uint64_t*>(smem + S::OFF_BAR);
     uint64_t* bar_mma = bar_ld + 1;
     uint64_t* bar_f = bar_ld + 2;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_ld + 3);
+    uint64_t* bar_kh = bar_ld + 3;  // the group's kernel-spectrum rows arrived
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_ld + 4);
+    float* khs = reinterpret_cast<float*>(smem + S::OFF_KH);
     const int tid = threadIdx.x, warp = tid >> 5;
     constexpr uint32_t IDESC_A = instr_desc(S::X3 ? 1 : 2, 128, S::NA);
     constexpr uint32_t IDESC_B = instr_desc(S::X3 ? 1 : 2, 128, S::NB);
@@ -160,6 +166,7 @@ __global__ void __launch_bounds__(128, 1)
         mbar_init(bar_ld, 1);
         mbar_init(bar_mma, 1);
         mbar_init(bar_f, 1);
+        mbar_init(bar_kh, 1);
         fence_barrier_init();
     }
     if (warp == 0) tmem_alloc(tmem_slot, S::TCOLS);
@@ -206,7 +213,8 @@ __global__ void __launch_bounds__(128, 1)
     };
     if (tid == 0 && blockIdx.x < ngroups) load_group(blockIdx.x);
     // asynchronous work in flight that an early exit has to wait for (uniform across the CTA)
-    bool ld_pending = blockIdx.x < ngroups, mma_pending = false;
+    bool ld_pending = blockIdx.x < ngroups, mma_pending = false, kh_pending = false;
+    uint32_t ph_kh = 0;
     const bool f_failed = __syncthreads_or(!mbar_wait_n(bar_f, 0, f_wait_polls(ctl)));
     bool abort = f_failed;
     uint32_t ph_ld = 0, ph_mma = 0;
@@ -302,11 +310,23 @@ __global__ void __launch_bounds__(128, 1)
 
         for (int k = 0; k < K && !abort; k++) {
             if (wd.kern[k].src != it.chan) continue;
-            const float* kh = wd.khat + (size_t)k * (W / 2 + 1) * HQ;
+            // the group's CT kernel-spectrum rows (kx0 .. kx0 + CT - 1, HQ floats each, contiguous) by
+            // one bulk copy into shared memory, instead of a global load per element of the hand-over
+            if (tid == 0) {
+                mbar_arrive_expect_tx(bar_kh, S::KHB);
+                bulk_g2s(khs, wd.khat + ((size_t)k * (W / 2 + 1) + kx0) * HQ, S::KHB, bar_kh);
+            }
+            kh_pending = true;
+            if (__syncthreads_or(!mbar_wait(bar_kh, ph_kh))) {
+                abort = true;
+                break;
+            }
+            kh_pending = false;
+            ph_kh ^= 1;
             // ---- B -> C: x khat (real, even), conjugate; rows (c, k2), K (re/im, k1)
             for (int b = 0; b < S::MB / 128; b++) {
                 const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
-                const float* khrow = kh + (size_t)(kx0 + c) * HQ;
+                const float* khrow = khs + c * S::HQ;
                 for (int q = 0; q < S::NB / 32; q++) {
                     float v[32];
                     tmem_ld32(t_b + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
@@ -393,6 +413,7 @@ __global__ void __launch_bounds__(128, 1)
             if (f_failed) mbar_wait(bar_f, 0);
             if (ld_pending) mbar_wait(bar_ld, ph_ld);
             if (mma_pending) mbar_wait(bar_mma, ph_mma);
+            if (kh_pending) mbar_wait(bar_kh, ph_kh);
             atomicExch(ctl + CTL_ERR, 1);
         }
         bulk_wait0();
@@ -438,10 +459,14 @@ void build_dft_operand(int n, bool x3, std::vector<uint8_t>& out, int lbo) {
         }
 }
 
+// Column length, its factors H1 x H2, columns per group, and the operand layout's LBO: padded (144,
+// bank-conflict-free hand-over stores) where it fits in shared memory beside the kernel-spectrum
+// rows, packed (128) at 2048 and in the 4096-point kernel (step_tc64.cu).
 struct ShapeInfo {
-    int H, H1, H2, CT;
+    int H, H1, H2, CT, LBO;
 };
-constexpr ShapeInfo SHAPES[] = {{4096, 64, 64, 2}, {2048, 64, 32, 4}, {1024, 32, 32, 4}, {512, 32, 16, 8}, {256, 16, 16, 8}};
+constexpr ShapeInfo SHAPES[] = {{4096, 64, 64, 2, 128}, {2048, 64, 32, 4, 128}, {1024, 32, 32, 4, 144},
+                                {512, 32, 16, 8, 144}, {256, 16, 16, 8, 144}};
 
 const ShapeInfo* shape_for(int H) {
     for (const auto& s : SHAPES)
@@ -463,13 +488,26 @@ bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups,
         attr = 1;
     }
     if (ngroups <= 0) return true;
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, col_pass_tc<S>, 128, S::SMEM) != cudaSuccess || per_sm < 1)
-        return false;
-    // TMEM: co-resident CTAs must fit in 512 columns
-    if (per_sm * S::TCOLS > 512) per_sm = 512 / S::TCOLS;
+    // CTAs per SM from the SM's shared memory and registers (the occupancy query answered one where
+    // two fit, and so left half the SMs' slots empty), and TMEM: co-resident CTAs share 512 columns.
+    // The grid is persistent over the groups, so a CTA that does not find room simply starts later.
+    static int per_sm = 0, sms = 0;
+    if (!per_sm) {
+        int dev = 0, smem_sm = 0, regs_sm = 0, reserved = 0;
+        cudaFuncAttributes fa;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+            cudaFuncGetAttributes(&fa, col_pass_tc<S>) != cudaSuccess)
+            return false;
+        int n = smem_sm / (S::SMEM + reserved);
+        const int by_regs = regs_sm / (128 * (fa.numRegs > 0 ? fa.numRegs : 255));
+        if (by_regs < n) n = by_regs;
+        if (n * S::TCOLS > 512) n = 512 / S::TCOLS;
+        per_sm = n < 1 ? 1 : n;
+    }
     int grid = (sms - reserve_sms) * per_sm;
     if (grid > ngroups) grid = ngroups;
     if (grid < 1) grid = 1;
@@ -512,8 +550,7 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
     }
     const bool x3 = path == LENIA_PATH_BF16X3;
     std::vector<uint8_t> host;
-    // the 4096-point kernel (step_tc64.cu) packs its operands (LBO 128); the others pad them (144)
-    const int lbo = H == 4096 ? 128 : 144;
+    const int lbo = s->LBO;
     build_dft_operand(s->H2, x3, host, lbo);                  // F_H2 (hi, lo)
     if (s->H1 != s->H2) build_dft_operand(s->H1, x3, host, lbo);  // F_H1 (hi, lo)
     void* d = nullptr;
@@ -541,14 +578,14 @@ bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, 
     int* e = (int*)plan.d_err;
     switch (H) {
     case 4096: return launch_col_tc64(x3, fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                         : launch_shape<TcShape<64, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                         : launch_shape<TcShape<32, 32, 4, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 512: return x3 ? launch_shape<TcShape<32, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                        : launch_shape<TcShape<32, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 256: return x3 ? launch_shape<TcShape<16, 16, 8, true>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                        : launch_shape<TcShape<16, 16, 8, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true, 128>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                         : launch_shape<TcShape<64, 32, 4, false, 128>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                         : launch_shape<TcShape<32, 32, 4, false, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 512: return x3 ? launch_shape<TcShape<32, 16, 8, true, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                        : launch_shape<TcShape<32, 16, 8, false, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 256: return x3 ? launch_shape<TcShape<16, 16, 8, true, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                        : launch_shape<TcShape<16, 16, 8, false, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
     }
     return false;
 }
