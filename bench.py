@@ -260,9 +260,11 @@ def seed_all(sim, worlds, seeds):
 
 def cpu_leg(worlds, seeds, min_seconds=10.0):
     """The reference's f32 step restated in C (oracle/lenia_oracle.c) on all host cores: a bounded
-    sample of the workload, at least `min_seconds` of timed CPU work, one generation of one world at
-    a time, cycling through the workload's one-channel power-of-two worlds.  Returns (cell-updates/s,
-    cores, sample description)."""
+    sample of the workload, at least `min_seconds` of timed CPU work, cycling through the workload's
+    one-channel power-of-two worlds one generation at a time.  With several worlds every core steps
+    whole worlds of its own (one thread each); one world runs its rows and columns over all cores.
+    Returns (cell-updates/s, cores, sample description)."""
+    from concurrent.futures import ThreadPoolExecutor
     from oracle.oracle import RefF32
     cores = os.cpu_count() or 1
     ref = RefF32(threads=cores)
@@ -270,24 +272,39 @@ def cpu_leg(worlds, seeds, min_seconds=10.0):
             if w.channels == 1 and (w.width & (w.width - 1)) == 0 and (w.height & (w.height - 1)) == 0]
     if not todo:
         return None, cores, "no world the restated reference step supports"
+    per_world = len(todo) > 1
+    batch = cores if per_world else 1
     prepared = {}
     cells = 0
     t_total = 0.0
     steps_done = 0
     i = 0
+    pool = ThreadPoolExecutor(max_workers=cores) if per_world else None
+
+    def step_one(j):
+        w = todo[j][0]
+        st, spectra = prepared[j]
+        prepared[j][0] = ref.step(w, st, steps=1, spectra=spectra, threads=1 if per_world else cores)
+        return w.width * w.height
+
     while t_total < min_seconds:
-        w, s = todo[i % len(todo)]
-        if i not in prepared:  # initial state and kernel spectrum, outside the timed region
-            prepared[i] = [ref.seed_patches(w.width, w.height, s, w.seed.patches), ref.spectra(w)]
-        st, spectra = prepared[i]
+        js = [(i + k) % len(todo) for k in range(min(batch, len(todo)))]
+        for j in js:
+            if j not in prepared:  # initial state and kernel spectrum, outside the timed region
+                w, s = todo[j]
+                prepared[j] = [ref.seed_patches(w.width, w.height, s, w.seed.patches), ref.spectra(w)]
         t0 = time.perf_counter()
-        prepared[i][0] = ref.step(w, st, steps=1, spectra=spectra)
+        done = sum(pool.map(step_one, js)) if pool else step_one(js[0])
         t_total += time.perf_counter() - t0
-        cells += w.width * w.height
-        steps_done += 1
-        i = (i + 1) % len(todo) if len(todo) > 1 else 0
+        cells += done
+        steps_done += len(js)
+        i = (i + len(js)) % len(todo)
+    if pool:
+        pool.shutdown()
     sample = ("%d generation(s) over %d of the workload's world(s) (one-channel, power-of-two sides), %.1f s "
-              "of CPU time, %d threads" % (steps_done, min(len(todo), steps_done), t_total, cores))
+              "of wall time, %d threads (%s)" % (steps_done, min(len(todo), steps_done), t_total, cores,
+                                                 "a world per thread" if per_world else
+                                                 "the world's rows and columns over the threads"))
     return cells / t_total, cores, sample
 
 
@@ -306,12 +323,22 @@ def run_reference(args, dist):
         if sum(x[0].width * x[0].height for x in prepared) >= 4096 * 4096:
             break
 
+    # Several worlds: every host core steps whole worlds of its own, one thread each (the oracle
+    # releases the GIL), which keeps all cores busy on small worlds where threading one world's rows
+    # and columns does not; one world: its rows and columns over all cores.
+    from concurrent.futures import ThreadPoolExecutor
+    per_world = len(prepared) > 1
+    pool = ThreadPoolExecutor(max_workers=cores) if per_world else None
+
+    def step_one(i):
+        w, st, sp = prepared[i]
+        prepared[i] = (w, ref.step(w, st, steps=1, spectra=sp, threads=1 if per_world else cores), sp)
+        return w.width * w.height
+
     def one():
-        cells = 0
-        for i, (w, st, sp) in enumerate(prepared):
-            prepared[i] = (w, ref.step(w, st, steps=1, spectra=sp), sp)
-            cells += w.width * w.height
-        return cells
+        if pool:
+            return sum(pool.map(step_one, range(len(prepared))))
+        return sum(step_one(i) for i in range(len(prepared)))
 
     for _ in range(args.warmup):
         one()
@@ -320,6 +347,8 @@ def run_reference(args, dist):
     for _ in range(args.steps):
         cells += one()
     dt = time.perf_counter() - t0
+    if pool:
+        pool.shutdown()
     value = cells / dt
     cfg.update({"path": "cpu restatement of spectral.rs (radix-2 Stockham, f32)", "gens_per_step": 1})
     out = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
@@ -327,8 +356,10 @@ def run_reference(args, dist):
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": cfg,
            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": "%d world(s) one generation per step, %d threads; the reference (Rust + WGSL "
-                                      "on Vulkan) cannot build or run on this box" % (len(prepared), cores)},
+                            "sample": "%d world(s) one generation per step, %d threads (%s); the reference (Rust + "
+                                      "WGSL on Vulkan) cannot build or run on this box" % (
+                                          len(prepared), cores, "a world per thread" if per_world else
+                                          "the world's rows and columns over the threads")},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
