@@ -57,6 +57,10 @@ struct SizeClass {
     int var_res = 0;                       // its launch variant (resident.cu)
     int res_fits[RESIDENT_VARIANTS] = {};  // clusters of each variant the GPU holds at once (0: cannot run)
     int* d_world_ids = nullptr;
+    // tensor-core row pass (step_tc_row.cu): possible for one-channel, one-kernel Lenia classes on the
+    // TF32 / BF16X3 paths whose row length it serves; `tc_rows` selects it over the FP32 row pass.
+    // Its groups are tc_row_stride consecutive FP32 row items.
+    int tc_rows_ok = 0, tc_rows = 0, tc_row_stride = 1;
 };
 
 // Default chunk budget: 0, every class is one chunk.  Chunks of up to 32 MiB do keep their worlds in
@@ -397,6 +401,15 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
     return ok && cudaStreamWaitEvent(s, ctx->ev_join, 0) == cudaSuccess;
 }
 
+// The row pass of one step over a run of a class's row items: on the tensor cores where the class
+// takes them, else the FP32 pass.
+bool launch_rows_step(LeniaCtx* ctx, const SizeClass& cl, int variant, const RowItem* items, int nrow, cudaStream_t s) {
+    if (cl.tc_rows)
+        return launch_row_tc(ctx->tc, ctx->path, cl.W, ctx->d_worlds, items, cl.tc_row_stride, nrow / cl.tc_row_stride,
+                             ctx->d_tw, s);
+    return launch_row_fp32(cl.W, variant, MODE_STEP, cl.general, ctx->d_worlds, items, nrow, cl.planes, ctx->d_tw, s);
+}
+
 // A launch shape of one size class: launch variants and chunks.
 struct Shape {
     int var_col, var_row;
@@ -417,8 +430,7 @@ int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps
         for (int st = 0; st < steps; st++) {
             bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
-            ok = launch_row_fp32(cl.W, sh.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0, ch.nrow,
-                                 cl.planes, ctx->d_tw, s);
+            ok = launch_rows_step(ctx, cl, sh.var_row, cl.d_row + ch.row0, ch.nrow, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
         }
     }
@@ -716,6 +728,19 @@ int setup_fused(LeniaCtx* ctx) {
             int trc = tc_prepare_size(ctx->tc, ctx->path, cl.H, &ctx->err);
             if (trc) return trc;
         }
+        // the tensor-core row pass, where the class's worlds all take the one-kernel Lenia step and
+        // their heights are whole groups of its rows
+        if (tc_path && !general && tc_row_supports(cl.W)) {
+            const int rg = tc_row_group_rows(cl.W);
+            bool fits = rg % (int)item_rows == 0;
+            for (int wi : cl.worlds) fits = fits && ctx->desc[wi].height % rg == 0;
+            if (fits) {
+                int trc = tc_row_prepare(ctx->tc, ctx->path, cl.W, &ctx->err);
+                if (trc) return trc;
+                cl.tc_row_stride = rg / (int)item_rows;
+                cl.tc_rows_ok = cl.tc_rows = 1;
+            }
+        }
         // per-world slices of the class lists
         size_t co = 0, ro = 0, go = 0;
         cl.bytes = 0;
@@ -758,6 +783,9 @@ int setup_fused(LeniaCtx* ctx) {
         }
         if (cl.ntcg > 0 && !launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_tcg, 0, ctx->d_tw, ctx->stream))
             return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core pass for H=%d", cl.H);
+        if (cl.tc_rows_ok &&
+            !launch_row_tc(ctx->tc, ctx->path, cl.W, ctx->d_worlds, cl.d_row, cl.tc_row_stride, 0, ctx->d_tw, ctx->stream))
+            return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core row pass for W=%d", cl.W);
     }
     return 0;
 }
@@ -856,8 +884,7 @@ int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, d
             bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col,
                                      ctx->stream);
             CK(cudaEventRecord(ev.e[k++], ctx->stream));
-            ok = ok && launch_row_fp32(cl.W, sh.var_row, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row + ch.row0,
-                                       ch.nrow, cl.planes, ctx->d_tw, ctx->stream);
+            ok = ok && launch_rows_step(ctx, cl, sh.var_row, cl.d_row + ch.row0, ch.nrow, ctx->stream);
             CK(cudaEventRecord(ev.e[k++], ctx->stream));
             if (!ok) {
                 cudaStreamSynchronize(ctx->stream);
@@ -1532,6 +1559,17 @@ int lenia_set_resident(LeniaCtx* ctx, int32_t mode) {
     return 0;
 }
 
+int lenia_set_tc_rows(LeniaCtx* ctx, int32_t on) {
+    if (!ctx) return LENIA_EINVAL;
+    if (on != 0 && on != 1) return fail(ctx, LENIA_EINVAL, "on must be 0 or 1");
+    for (auto& cl : ctx->classes) cl.tc_rows = on && cl.tc_rows_ok;
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
 int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells, int32_t each) {
     if (!ctx) return LENIA_EINVAL;
     if (cells < 0 || (each != 0 && each != 1)) return fail(ctx, LENIA_EINVAL, "cells must be >= 0, each 0 or 1");
@@ -1556,10 +1594,10 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (count < 10 * ctx->classes.size()) return LENIA_EINVAL;
+    if (count < 11 * ctx->classes.size()) return LENIA_EINVAL;
     for (size_t i = 0; i < ctx->classes.size(); i++) {
         const auto& cl = ctx->classes[i];
-        int32_t* o = out + 10 * i;
+        int32_t* o = out + 11 * i;
         o[0] = cl.W;
         o[1] = cl.H;
         o[2] = cl.var_col;
@@ -1570,6 +1608,7 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
         o[7] = row_item_rows(cl.W, cl.general);
         o[8] = cl.resident;
         o[9] = cl.var_res;
+        o[10] = cl.tc_rows;
     }
     return 0;
 }

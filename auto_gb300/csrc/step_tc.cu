@@ -26,6 +26,7 @@
 
 #include "fft_core.cuh"
 #include "step_tc.cuh"
+#include "tc_opnd.cuh"
 #include "tc_ptx.cuh"
 
 namespace lenia {
@@ -62,79 +63,6 @@ struct TcShape {
     static_assert(2 * REGION <= 512, "TMEM");
     static_assert(SMEM <= 232448, "shared memory of one CTA");
 };
-
-// ------------------------------------------------------------------ operand stores
-// BF16x3 split of two values at once: hi = bf16(v) and lo = bf16(v - hi) for a and b, packed as
-// bf16x2 (a in the low half).  One paired conversion for both his, one f32x2 subtract for both
-// (exact) residuals, one paired conversion for both los: the same bits as the per-value split.
-__device__ __forceinline__ void split_bf16x2(float a, float b, uint32_t& hi, uint32_t& lo) {
-    const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    const float2 hf = __bfloat1622float2(h);
-    const float2 r = lfft::f2sub(make_float2(a, b), hf);
-    const __nv_bfloat162 l = __floats2bfloat162_rn(r.x, r.y);
-    hi = *reinterpret_cast<const uint32_t*>(&h);
-    lo = *reinterpret_cast<const uint32_t*>(&l);
-}
-
-template <bool X3, int LBO>
-__device__ __forceinline__ void store_elem(uint8_t* op, int opnd_bytes, int r, int k, int K, float v) {
-    if (X3) {
-        const uint32_t off = kmajor_offset(r, k, K, 2, LBO);
-        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
-        const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
-        *reinterpret_cast<__nv_bfloat16*>(op + off) = hi;
-        *reinterpret_cast<__nv_bfloat16*>(op + opnd_bytes + off) = lo;
-    } else {
-        *reinterpret_cast<uint32_t*>(op + kmajor_offset(r, k, K, 4, LBO)) = to_tf32(v);
-    }
-}
-
-// 16 bytes of consecutive K: 8 values (bf16 hi and lo) or 4 (tf32), starting at k0.
-template <bool X3, int LBO>
-__device__ __forceinline__ void store_chunk(uint8_t* op, int opnd_bytes, int r, int k0, int K, const float* v) {
-    if (X3) {
-        uint32_t hi[4], lo[4];
-#pragma unroll
-        for (int i = 0; i < 4; i++) split_bf16x2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
-        const uint32_t off = kmajor_offset(r, k0, K, 2, LBO);
-        *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(op + opnd_bytes + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
-    } else {
-        *reinterpret_cast<uint4*>(op + kmajor_offset(r, k0, K, 4, LBO)) =
-            make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
-    }
-}
-
-// One GEMM: D[rows of M in blocks of 128] (+)= A (M x K, K-major) * F^T (F: N x K, K-major).
-// Both operands in the K-major layout with K-adjacent core matrices LBO bytes apart (kmajor_offset).
-// An MMA consumes 32 bytes of K (two core matrices), so consecutive MMAs start 2 LBO apart.
-template <bool X3, int LBO = 128>
-__device__ __forceinline__ void issue_gemm(uint32_t d_tmem, uint32_t a_saddr, uint32_t a_lo_off, int M, int K,
-                                           uint32_t f_saddr, uint32_t f_lo_off, int N, uint32_t idesc) {
-    constexpr int E = X3 ? 2 : 4;
-    const uint32_t sbo = (uint32_t)(K * E / 16 * LBO);
-    const int ksteps = K * E / 32;
-    for (int b = 0; b < M / 128; b++) {
-        const uint32_t d = d_tmem + (uint32_t)(b * N);
-        const uint32_t a0 = a_saddr + (uint32_t)b * 16u * sbo;
-        for (int s = 0; s < ksteps; s++) {
-            const uint32_t ko = 2u * LBO * s;
-            const uint64_t ad = smem_desc(a0 + ko, LBO, sbo);
-            const uint64_t bd = smem_desc(f_saddr + ko, LBO, sbo);
-            mma<!X3>(d, ad, bd, idesc, s > 0 ? 1u : 0u);
-            if (X3) {
-                mma<false>(d, ad, smem_desc(f_saddr + f_lo_off + ko, LBO, sbo), idesc, 1u);
-                mma<false>(d, smem_desc(a0 + a_lo_off + ko, LBO, sbo), bd, idesc, 1u);
-            }
-        }
-    }
-}
-
-// Twiddle exp(-2 pi i a b / H) from the global table (TWN entries).
-template <int H>
-__device__ __forceinline__ float2 twid(const float2* __restrict__ tw, int a, int b) {
-    return tw[((a * b) % H) * (lfft::TWN / H)];
-}
 
 // A group is (world, channel, first tile); it covers CT columns = CT / TC consecutive tiles.
 //
@@ -617,6 +545,7 @@ int tc_set_wait_limit(TcPlan& plan, int limit_plus_one, std::string* err) {
 void tc_release(TcPlan& plan) {
     for (int i = 0; i < plan.nsizes; i++) cudaFree(plan.mats[i]);
     plan.nsizes = 0;
+    tc_row_release(plan);
     if (plan.d_err) cudaFree(plan.d_err);
     plan.d_err = nullptr;
     plan.ready = 0;

@@ -17,6 +17,9 @@ struct TcPlan {
     void* mats[16] = {};
     int sizes[16] = {};
     int nsizes = 0;
+    void* rmats[16] = {};  // the row pass's DFT matrices per row length
+    int rsizes[16] = {};
+    int nrsizes = 0;
     void* d_err = nullptr;
 };
 
@@ -38,6 +41,16 @@ int tc_set_wait_limit(TcPlan& plan, int limit_plus_one, std::string* err);
 bool launch_col_tc64(bool x3, const void* fmat, const DevWorld* worlds, const ColItem* groups, int ngroups,
                      const float2* tw, int* err, cudaStream_t s, int reserve_sms = 0);
 void tc_release(TcPlan& plan);
+
+// Tensor-core row pass (step_tc_row.cu) of the one-channel, one-kernel Lenia step: inverse row DFT,
+// growth / dt / clamp, forward row DFT, as GEMMs.  Row lengths served: 256, 512, 1024.
+bool tc_row_supports(int W);
+int tc_row_group_rows(int W);  // rows per group (a multiple of the FP32 row item's 4)
+int tc_row_prepare(TcPlan& plan, int path, int W, std::string* err);
+// items: the FP32 row pass's items (4 rows each); group g starts at items[g * item_stride].
+bool launch_row_tc(const TcPlan& plan, int path, int W, const DevWorld* worlds, const RowItem* items, int item_stride,
+                   int ngroups, const float2* tw, cudaStream_t s);
+void tc_row_release(TcPlan& plan);
 // One GEMM through the same operand layouts and descriptors (diagnostic).
 int tc_selftest(int path, int n, int k, const float* a, const float* b, float* d, std::string* err);
 

@@ -626,6 +626,24 @@ def run_ours(args, dist):
                 t_ms = dist.max(t_ms)
                 paths[pth] = {"value": dist.sum(other.cells_per_step) * g * reps / (t_ms * 1e-3),
                               "ms_per_generation": t_ms / (reps * g)}
+        if not any(w.channels != 1 or len(w.kernels) != 1 for w in worlds):
+            # the tensor-core step with its row pass on the FP32 CUDA cores instead (column pass only on
+            # the tensor cores), to show what the tensor-core row pass adds
+            with Sim(worlds, seed=0, path="bf16x3") as other:
+                seed_all(other, worlds, seeds)
+                tc_classes = ["%dx%d" % k for k, v in other.shapes().items() if v["tc_rows"]]
+                other.set_tc_rows(False)
+                if not args.no_autotune:
+                    other.autotune()
+                other.step(G)
+                other.wait()
+                reps = max(2, min(args.steps, 20))
+                t_ms = dist.max(other.step_timed(reps * G))
+                paths["bf16x3_fp32_rows"] = {"value": dist.sum(other.cells_per_step) * G * reps / (t_ms * 1e-3),
+                                             "ms_per_generation": t_ms / (reps * G),
+                                             "what": "BF16x3 column pass with the FP32 row pass; the bf16x3 entry "
+                                                     "runs the row pass on the tensor cores for classes %s" %
+                                                     (", ".join(tc_classes) or "none")}
         if paths.get("fp32", {}).get("value") and paths.get("radix2", {}).get("value"):
             paths["fp32_over_radix2"] = paths["fp32"]["value"] / paths["radix2"]["value"]
         if paths.get("bf16x3", {}).get("value") and paths.get("radix2", {}).get("value"):

@@ -195,10 +195,10 @@ LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
 LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
 /* The launch shape of every size class, as the autotuner left it: *nclasses = the number of classes;
- * with `out` (count >= 10 * classes) ten int32 per class: width, height, column variant, row
+ * with `out` (count >= 11 * classes) eleven int32 per class: width, height, column variant, row
  * variant, chunks, worlds, chunk budget in MiB (0: the class is one chunk), rows per row-pass item,
- * 1 if the class runs the cluster-resident step (lenia_set_resident) else 0, and that step's launch
- * variant.
+ * 1 if the class runs the cluster-resident step (lenia_set_resident) else 0, that step's launch
+ * variant, and 1 if its row pass runs on the tensor cores (lenia_set_tc_rows) else 0.
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
@@ -226,6 +226,12 @@ LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells, int32_t* e
  * lenia_sync.  Rebuilds the step graphs.  No reference counterpart (the reference dispatches every
  * pass of every world separately, crates/auto-core/src/sim.rs:297-380). */
 LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t mode);
+/* The tensor-core row pass on (1, the default) or off (0) on the TF32 and BF16X3 paths: the inverse
+ * row DFT, the growth / dt / clamp update and the forward row DFT of the one-channel, one-kernel
+ * Lenia step as DFT-as-GEMM on tcgen05 (step rows of 256, 512 and 1024 cells; other classes, and
+ * every class when off, take the FP32 row pass).  Rebuilds the step graphs.  No reference
+ * counterpart: the reference's row transforms are radix-2 dispatches (spectral.rs:225-264). */
+LENIA_API int lenia_set_tc_rows(LeniaCtx* ctx, int32_t on);
 
 /* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
  * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.

@@ -118,3 +118,56 @@ def test_wait_limit_hook_rejected_without_tensor_cores():
     L = _lib.load()
     with Sim(ag.World(64, 64, [ag.Kernel(radius=8.0)]), path="fp32") as sim:
         assert L.lenia_tc_set_wait_limit(sim._ctx, 1) == _lib.ESTATE
+
+
+@pytest.mark.parametrize("path,tol", [("bf16x3", 1e-4), ("tf32", 1e-2)])
+@pytest.mark.parametrize("w,h", [(256, 256), (512, 512), (1024, 1024), (1024, 256), (256, 512), (512, 1024)])
+def test_tc_row_pass_vs_fp64(path, tol, w, h):
+    """The tensor-core row pass (inverse row DFT, growth / dt / clamp, forward row DFT as GEMMs) on
+    the rows it serves, square and not: teacher-forced steps against the FP64 oracle with it on and
+    off (the FP32 row pass), after every step of three.  The class reports which row pass it runs."""
+    world = ag.World(w, h, [ag.Kernel(radius=min(13.0, min(w, h) / 4))])
+    rng = np.random.default_rng(w * 7 + h)
+    s0 = np.zeros((h, w), np.float32)
+    s0[h // 4:3 * h // 4, w // 4:3 * w // 4] = rng.random((h // 2, w // 2), dtype=np.float32)
+    errs = {}
+    for on in (True, False):
+        with Sim(world, path=path) as sim:
+            sim.set_tc_rows(on)
+            assert sim.shapes()[(w, h)]["tc_rows"] == (1 if on else 0)
+            sim.write_state(0, s0)
+            s = s0[None]
+            worst = 0.0
+            for _ in range(3):
+                sim.step(1)
+                got = sim.read_state(0)
+                worst = max(worst, float(np.abs(got - fp64_step(world, s)).max()))
+                s = got
+            errs[on] = worst
+            mass = float(s.mean())
+    print("%s %dx%d per-step max|err| vs FP64: tensor-core rows %.3e, FP32 rows %.3e (mean state %.4f)" %
+          (path, w, h, errs[True], errs[False], mass))
+    assert errs[True] < tol and errs[False] < tol, errs
+    assert 0.0 < mass < 1.0
+
+
+def test_tc_row_pass_batched_many_steps():
+    """The batched workload's tensor-core classes (256, 512, 1024) over 64 steps with the row pass on
+    the tensor cores, checked teacher-forced against FP64 at the last step."""
+    worlds = [w for w in configs.batched(96) if w.width in (256, 512, 1024)][:24]
+    with Sim(worlds, seed=0, path="bf16x3") as sim:
+        for i, w in enumerate(worlds):
+            sim.seed_patches(i, i, w.seed.patches)
+        assert all(v["tc_rows"] == 1 for v in sim.shapes().values())
+        sim.step(63)
+        before = [sim.read_state(i) for i in range(len(worlds))]
+        sim.step(1)
+        worst, alive = 0.0, 0
+        for i, w in enumerate(worlds):
+            got = sim.read_state(i)
+            worst = max(worst, float(np.abs(got - fp64_step(w, before[i])).max()))
+            alive += int(got.mean() > 0)
+    print("batched tensor-core classes, step 64: per-step max|err| vs FP64 %.3e, %d of %d worlds alive" %
+          (worst, alive, len(worlds)))
+    assert worst < 1e-4, worst
+    assert alive > len(worlds) // 2
