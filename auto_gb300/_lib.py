@@ -13,6 +13,7 @@ OK, EINVAL, ESIZE, ENOMEM, ECUDA, ENODEV, ESTATE = 0, -1, -2, -3, -4, -5, -6
 SHAPE_LENIA, SHAPE_SL_INNER, SHAPE_SL_OUTER, SHAPE_RING = 0, 1, 2, 3
 RULE_LENIA, RULE_SMOOTHLIFE, RULE_MNCA = 0, 1, 2
 PATH_FP32, PATH_TF32, PATH_BF16X3, PATH_RADIX2 = 0, 1, 2, 3
+SELFTEST_A_MN = 0x100  # lenia_tc_selftest: A in the MN-major layout
 PATHS = {"fp32": PATH_FP32, "tf32": PATH_TF32, "bf16x3": PATH_BF16X3, "radix2": PATH_RADIX2}
 
 LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "liblenia_gb300.so")

@@ -1630,8 +1630,10 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
     return 0;
 }
 
-// The autotuner's search, on states it may advance.  For every size class, in turn: every pair of
-// column and row launch variants, then every chunk budget that gives a different number of chunks.
+// The autotuner's search, on states it may advance.  For every size class, in turn: the cluster-
+// resident step against two launches a generation (FP32 path, where it applies), the tensor-core row
+// pass against the FP32 one (TF32 / BF16X3 paths, where it applies), every pair of column and row
+// launch variants, then every chunk budget that gives a different number of chunks.
 // Each candidate is timed as a captured graph of a few steps (time_class_graph), and a class keeps
 // its current choice of a dimension unless another is at least 3% faster, so that timing noise does
 // not flip it.
@@ -1679,6 +1681,19 @@ static int autotune_search(LeniaCtx* ctx) {
                 cl.var_res = cands[b].second;
             }
             if (cl.resident) continue;  // launch variants and chunks do not apply to it
+        }
+        if (cl.tc_rows_ok) {
+            // the tensor-core row pass against the FP32 row pass (TF32 / BF16X3 paths); candidate 0 is
+            // the current choice
+            const int was = cl.tc_rows;
+            double t[2] = {0, 0};
+            for (int i = 0; i < 2 && !rc; i++) {
+                cl.tc_rows = i == 0 ? was : !was;
+                rc = timed(shape_of(cl), &t[i]);
+            }
+            cl.tc_rows = was;
+            if (rc) return rc;
+            if (t[1] < 0.97 * t[0]) cl.tc_rows = !was;
         }
         {
             std::vector<Shape> c{shape_of(cl)};

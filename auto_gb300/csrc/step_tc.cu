@@ -89,6 +89,10 @@ __global__ void __launch_bounds__(128, 1)
     const int tid = threadIdx.x, warp = tid >> 5;
     constexpr uint32_t IDESC_A = instr_desc(S::X3 ? 1 : 2, 128, S::NA);
     constexpr uint32_t IDESC_B = instr_desc(S::X3 ? 1 : 2, 128, S::NB);
+    // BF16x3: the transposing hand-overs (A -> B, C -> D) store MN-major A operands, 16 bytes a store
+    // (TF32 keeps every operand K-major)
+    constexpr uint32_t IDESC_AM = instr_desc(S::X3 ? 1 : 2, 128, S::NA, S::X3);
+    constexpr uint32_t IDESC_BM = instr_desc(S::X3 ? 1 : 2, 128, S::NB, S::X3);
 
     if (tid == 0) {
         mbar_init(bar_ld, 1);
@@ -147,10 +151,14 @@ __global__ void __launch_bounds__(128, 1)
     bool abort = f_failed;
     uint32_t ph_ld = 0, ph_mma = 0;
     // issue one GEMM from an elected thread and wait for it; false (on every thread) if the wait gave up
-    auto gemm = [&](uint32_t d, uint32_t a_off, int M, int K, uint32_t f_addr, uint32_t f_lo, int N, uint32_t idesc) {
+    auto gemm = [&](uint32_t d, uint32_t a_off, int M, int K, uint32_t f_addr, uint32_t f_lo, int N, uint32_t idesc,
+                    bool amn = false) {
         if (tid == 0) {
             tc_fence_after();
-            issue_gemm<S::X3, S::LBO>(d, smem_u32(op), a_off, M, K, f_addr, f_lo, N, idesc);
+            if (S::X3 && amn)
+                issue_gemm_amn<S::LBO>(d, smem_u32(op), a_off, M, K, f_addr, f_lo, K, N, idesc);
+            else
+                issue_gemm<S::X3, S::LBO>(d, smem_u32(op), a_off, M, K, f_addr, f_lo, N, idesc);
             mma_commit(bar_mma);
         }
         if (__syncthreads_or(!mbar_wait(bar_mma, ph_mma))) {
@@ -214,15 +222,30 @@ __global__ void __launch_bounds__(128, 1)
             for (int q = 0; q < S::NA / 32; q++) {
                 float v[32];
                 tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NA + 32 * q), v);
+                if constexpr (S::X3) {
+                    float vr[16], vi[16];
 #pragma unroll
-                for (int u = 0; u < 16; u++) {
-                    const int k2 = 16 * q + u;
-                    const float2 w = lfft::cmul(Aq[q], Au[u]);
-                    const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
-                    const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
-                    const int rr = c * S::H2 + k2;
-                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, y1, S::KB, re);
-                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H1 + y1, S::KB, im);
+                    for (int u = 0; u < 16; u++) {
+                        const float2 w = lfft::cmul(Aq[q], Au[u]);
+                        vr[u] = v[2 * u] * w.x - v[2 * u + 1] * w.y;
+                        vi[u] = v[2 * u] * w.y + v[2 * u + 1] * w.x;
+                    }
+                    const int m0 = c * S::H2 + 16 * q;
+                    store_mn_chunk(op, S::OPND, m0, y1, S::MB, vr);
+                    store_mn_chunk(op, S::OPND, m0 + 8, y1, S::MB, vr + 8);
+                    store_mn_chunk(op, S::OPND, m0, S::H1 + y1, S::MB, vi);
+                    store_mn_chunk(op, S::OPND, m0 + 8, S::H1 + y1, S::MB, vi + 8);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const int k2 = 16 * q + u;
+                        const float2 w = lfft::cmul(Aq[q], Au[u]);
+                        const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
+                        const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
+                        const int rr = c * S::H2 + k2;
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, y1, S::KB, re);
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H1 + y1, S::KB, im);
+                    }
                 }
             }
         }
@@ -231,7 +254,7 @@ __global__ void __launch_bounds__(128, 1)
         __syncthreads();
 
         // ---- GEMM B -> spectrum of the channel along y, kept in TMEM region t_b
-        if (!gemm(t_b, S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B)) {
+        if (!gemm(t_b, S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_BM, true)) {
             abort = true;
             break;
         }
@@ -289,15 +312,30 @@ __global__ void __launch_bounds__(128, 1)
                 for (int q = 0; q < S::NB / 32; q++) {
                     float v[32];
                     tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
+                    if constexpr (S::X3) {
+                        float vr[16], vi[16];
 #pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        const int y1 = 16 * q + u;
-                        const float2 w = lfft::cmul(Cq[q], Cu[u]);
-                        const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
-                        const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
-                        const int rr = c * S::H1 + y1;
-                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, k2, S::KA, re);
-                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H2 + k2, S::KA, im);
+                        for (int u = 0; u < 16; u++) {
+                            const float2 w = lfft::cmul(Cq[q], Cu[u]);
+                            vr[u] = v[2 * u] * w.x - v[2 * u + 1] * w.y;
+                            vi[u] = v[2 * u] * w.y + v[2 * u + 1] * w.x;
+                        }
+                        const int m0 = c * S::H1 + 16 * q;
+                        store_mn_chunk(op, S::OPND, m0, k2, S::MA, vr);
+                        store_mn_chunk(op, S::OPND, m0 + 8, k2, S::MA, vr + 8);
+                        store_mn_chunk(op, S::OPND, m0, S::H2 + k2, S::MA, vi);
+                        store_mn_chunk(op, S::OPND, m0 + 8, S::H2 + k2, S::MA, vi + 8);
+                    } else {
+#pragma unroll
+                        for (int u = 0; u < 16; u++) {
+                            const int y1 = 16 * q + u;
+                            const float2 w = lfft::cmul(Cq[q], Cu[u]);
+                            const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
+                            const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
+                            const int rr = c * S::H1 + y1;
+                            store_elem<S::X3, S::LBO>(op, S::OPND, rr, k2, S::KA, re);
+                            store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H2 + k2, S::KA, im);
+                        }
                     }
                 }
             }
@@ -305,7 +343,7 @@ __global__ void __launch_bounds__(128, 1)
             fence_async_smem();
             __syncthreads();
             // ---- GEMM D
-            if (!gemm(t_x, S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_A)) {
+            if (!gemm(t_x, S::OPND, S::MA, S::KA, smem_u32(f2), S::FA, S::NA, IDESC_AM, true)) {
                 abort = true;
                 break;
             }
@@ -556,18 +594,22 @@ void tc_release(TcPlan& plan) {
 // ------------------------------------------------------------------ GEMM self-test
 namespace lenia {
 
-template <bool X3>
+// amn: A in the MN-major layout (mnmajor_offset, BF16x3 only), as the transposing hand-overs store it;
+// else K-major.  The A area is followed by `pad` zeroed bytes, so that a misread descriptor stays in
+// the CTA's shared memory.
+template <bool X3, bool AMN>
 __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __restrict__ a, const uint8_t* __restrict__ b,
-                                                             int n, int k, float* d, int* err) {
+                                                             int n, int k, int pad, float* d, int* err) {
     extern __shared__ __align__(128) uint8_t smem[];
     constexpr int E = X3 ? 2 : 4, NOP = X3 ? 2 : 1;
     const int abytes = 128 * k * E, bbytes = n * k * E;
-    uint8_t* sa = smem;
-    uint8_t* sb = smem + abytes * NOP;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(sb + bbytes * NOP);
+    uint8_t* sb = smem;
+    uint8_t* sa = smem + bbytes * NOP;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(sa + abytes * NOP + pad);
     uint32_t* slot = reinterpret_cast<uint32_t*>(bar + 1);
     const int tid = threadIdx.x, warp = tid >> 5;
     for (int i = tid * 16; i < abytes * NOP; i += 128 * 16) *reinterpret_cast<uint4*>(sa + i) = *reinterpret_cast<const uint4*>(a + i);
+    for (int i = tid * 16; i < pad; i += 128 * 16) *reinterpret_cast<uint4*>(sa + abytes * NOP + i) = make_uint4(0, 0, 0, 0);
     for (int i = tid * 16; i < bbytes * NOP; i += 128 * 16) *reinterpret_cast<uint4*>(sb + i) = *reinterpret_cast<const uint4*>(b + i);
     if (tid == 0) {
         mbar_init(bar, 1);
@@ -580,7 +622,10 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
     tc_fence_after();
     const uint32_t t = *slot;
     if (tid == 0) {
-        issue_gemm<X3>(t, smem_u32(sa), abytes, 128, k, smem_u32(sb), bbytes, n, instr_desc(X3 ? 1 : 2, 128, n));
+        if (AMN)
+            issue_gemm_amn<128>(t, smem_u32(sa), abytes, 128, k, smem_u32(sb), bbytes, k, n, instr_desc(1, 128, n, true));
+        else
+            issue_gemm<X3>(t, smem_u32(sa), abytes, 128, k, smem_u32(sb), bbytes, n, instr_desc(X3 ? 1 : 2, 128, n));
         mma_commit(bar);
     }
     const bool ok = !__syncthreads_or(!mbar_wait(bar, 0));
@@ -603,14 +648,14 @@ __global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const uint8_t* __re
 }
 
 namespace {
-void pack_operand(const float* m, int rows, int k, bool x3, std::vector<uint8_t>& out) {
+void pack_operand(const float* m, int rows, int k, bool x3, bool mn, std::vector<uint8_t>& out) {
     const int E = x3 ? 2 : 4;
     const size_t bytes = (size_t)rows * k * E;
     out.assign(bytes * (x3 ? 2 : 1), 0);
     for (int r = 0; r < rows; r++)
         for (int c = 0; c < k; c++) {
             const float v = m[(size_t)r * k + c];
-            const uint32_t off = kmajor_offset(r, c, k, E);
+            const uint32_t off = mn ? mnmajor_offset(r, c, rows) : kmajor_offset(r, c, k, E);
             if (x3) {
                 const __nv_bfloat16 hi = __float2bfloat16_rn(v);
                 const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
@@ -627,19 +672,24 @@ void pack_operand(const float* m, int rows, int k, bool x3, std::vector<uint8_t>
 }  // namespace
 
 int tc_selftest(int path, int n, int k, const float* a, const float* b, float* d, std::string* err) {
+    const bool amn = (path & LENIA_SELFTEST_A_MN) != 0;
+    path &= ~LENIA_SELFTEST_A_MN;
     const bool x3 = path == LENIA_PATH_BF16X3;
-    if ((path != LENIA_PATH_TF32 && !x3) || n < 32 || n > 256 || n % 32 || k < 16 || k > 256 || k % 16) {
-        if (err) *err = "selftest: path must be TF32 or BF16X3, n in 32..256 (multiple of 32), k in 16..256 (multiple of 16)";
+    if ((path != LENIA_PATH_TF32 && !x3) || n < 32 || n > 256 || n % 32 || k < 16 || k > 256 || k % 16 ||
+        (amn && (!x3 || k > 64))) {
+        if (err) *err = "selftest: path must be TF32 or BF16X3, n in 32..256 (multiple of 32), k in 16..256 (multiple "
+                        "of 16); an MN-major A needs BF16X3 and k <= 64";
         return LENIA_EINVAL;
     }
     std::vector<uint8_t> ha, hb;
-    pack_operand(a, 128, k, x3, ha);
-    pack_operand(b, n, k, x3, hb);
+    pack_operand(a, 128, k, x3, amn, ha);
+    pack_operand(b, n, k, x3, false, hb);
     uint8_t *da = nullptr, *db = nullptr;
     float* dd = nullptr;
     int* de = nullptr;
     int rc = 0;
-    const size_t smem = ha.size() + hb.size() + 64;
+    const int pad = amn ? 64 * 1024 : 0;
+    const size_t smem = ha.size() + hb.size() + pad + 64;
     if (cudaMalloc(&da, ha.size()) || cudaMalloc(&db, hb.size()) || cudaMalloc(&dd, (size_t)128 * n * 4) ||
         cudaMalloc(&de, 4)) {
         rc = LENIA_ENOMEM;
@@ -649,12 +699,15 @@ int tc_selftest(int path, int n, int k, const float* a, const float* b, float* d
         cudaMemset(de, 0, 4);
         cudaMemset(dd, 0, (size_t)128 * n * 4);
         cudaError_t e;
-        if (x3) {
-            cudaFuncSetAttribute(tc_selftest_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            tc_selftest_kernel<true><<<1, 128, smem>>>(da, db, n, k, dd, de);
+        if (amn) {
+            cudaFuncSetAttribute(tc_selftest_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            tc_selftest_kernel<true, true><<<1, 128, smem>>>(da, db, n, k, pad, dd, de);
+        } else if (x3) {
+            cudaFuncSetAttribute(tc_selftest_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            tc_selftest_kernel<true, false><<<1, 128, smem>>>(da, db, n, k, pad, dd, de);
         } else {
-            cudaFuncSetAttribute(tc_selftest_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            tc_selftest_kernel<false><<<1, 128, smem>>>(da, db, n, k, dd, de);
+            cudaFuncSetAttribute(tc_selftest_kernel<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            tc_selftest_kernel<false, false><<<1, 128, smem>>>(da, db, n, k, pad, dd, de);
         }
         e = cudaDeviceSynchronize();
         int h = 0;

@@ -73,6 +73,7 @@ struct TcRowShape {
     static_assert(W1 % 16 == 0 && W2 % 16 == 0, "hand-overs in runs of 16 columns; N >= 16");
     static_assert(REGION <= 512, "TMEM");
     static_assert((W * 4) % 16 == 0 && (STR * 4) % 16 == 0 && (XR * 8) % 16 == 0, "16-byte rows");
+    static_assert(MQ * KQ * 2 <= OPND && MP * KS * 2 <= OPND, "MN-major operands fit the operand area");
     static_assert(SMEM <= 232448, "shared memory of one CTA");
 };
 
@@ -94,8 +95,10 @@ __global__ void __launch_bounds__(128, 1)
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_st + 4);
     const int tid = threadIdx.x, warp = tid >> 5;
     constexpr int FMT = S::X3 ? 1 : 2;
-    constexpr uint32_t ID_P = instr_desc(FMT, 128, S::NP), ID_Q = instr_desc(FMT, 128, S::NQ);
-    constexpr uint32_t ID_R = instr_desc(FMT, 128, S::NR), ID_S = instr_desc(FMT, 128, S::NS);
+    // BF16x3: the transposing hand-overs (P -> Q, R -> S) store MN-major A operands, 16 bytes a store
+    // (TF32 keeps every operand K-major)
+    constexpr uint32_t ID_P = instr_desc(FMT, 128, S::NP), ID_Q = instr_desc(FMT, 128, S::NQ, S::X3);
+    constexpr uint32_t ID_R = instr_desc(FMT, 128, S::NR), ID_S = instr_desc(FMT, 128, S::NS, S::X3);
     constexpr int CH = S::X3 ? 8 : 4;  // values per 16-byte operand chunk
 
     if (tid == 0) {
@@ -162,10 +165,13 @@ __global__ void __launch_bounds__(128, 1)
     bool abort = f_failed;
     uint32_t ph_st = 0, ph_mma = 0;
     // issue one GEMM from an elected thread and wait for it; false (on every thread) if the wait gave up
-    auto gemm = [&](int M, int K, uint32_t f_addr, uint32_t f_lo, int fK, int N, uint32_t idesc) {
+    auto gemm = [&](int M, int K, uint32_t f_addr, uint32_t f_lo, int fK, int N, uint32_t idesc, bool amn = false) {
         if (tid == 0) {
             tc_fence_after();
-            issue_gemm_k<S::X3, S::LBO>(tx, smem_u32(op), S::OPND, M, K, K, f_addr, f_lo, fK, N, idesc);
+            if (S::X3 && amn)
+                issue_gemm_amn<S::LBO>(tx, smem_u32(op), S::OPND, M, K, f_addr, f_lo, fK, N, idesc);
+            else
+                issue_gemm_k<S::X3, S::LBO>(tx, smem_u32(op), S::OPND, M, K, K, f_addr, f_lo, fK, N, idesc);
             mma_commit(bar_mma);
         }
         if (__syncthreads_or(!mbar_wait(bar_mma, ph_mma))) {
@@ -232,19 +238,34 @@ __global__ void __launch_bounds__(128, 1)
                 float re[16], im[16];
                 const uint32_t t0 = tx + lane_off + (uint32_t)(b * S::NP + 16 * q);
                 tmem_ld16x2(t0, t0 + S::W1, re, im);
+                if constexpr (S::X3) {
+                    float vr[16], vi[16];
 #pragma unroll
-                for (int u = 0; u < 16; u++) {
-                    const float2 w = lfft::cmul(Aq[q], Au[u]);
-                    const int rr = r * S::W1 + 16 * q + u;
-                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, k2, S::KQ, re[u] * w.x - im[u] * w.y);
-                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::W2 + k2, S::KQ, re[u] * w.y + im[u] * w.x);
+                    for (int u = 0; u < 16; u++) {
+                        const float2 w = lfft::cmul(Aq[q], Au[u]);
+                        vr[u] = re[u] * w.x - im[u] * w.y;
+                        vi[u] = re[u] * w.y + im[u] * w.x;
+                    }
+                    const int m0 = r * S::W1 + 16 * q;
+                    store_mn_chunk(op, S::OPND, m0, k2, S::MQ, vr);
+                    store_mn_chunk(op, S::OPND, m0 + 8, k2, S::MQ, vr + 8);
+                    store_mn_chunk(op, S::OPND, m0, S::W2 + k2, S::MQ, vi);
+                    store_mn_chunk(op, S::OPND, m0 + 8, S::W2 + k2, S::MQ, vi + 8);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const float2 w = lfft::cmul(Aq[q], Au[u]);
+                        const int rr = r * S::W1 + 16 * q + u;
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, k2, S::KQ, re[u] * w.x - im[u] * w.y);
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::W2 + k2, S::KQ, re[u] * w.y + im[u] * w.x);
+                    }
                 }
             }
         }
         tc_fence_before();
         fence_async_smem();
         __syncthreads();
-        if (!gemm(S::MQ, S::KQ, smem_u32(f2), S::F2, 2 * S::W2, S::NQ, ID_Q)) {
+        if (!gemm(S::MQ, S::KQ, smem_u32(f2), S::F2, 2 * S::W2, S::NQ, ID_Q, true)) {
             abort = true;
             break;
         }
@@ -300,19 +321,34 @@ __global__ void __launch_bounds__(128, 1)
                 float re[16], im[16];
                 const uint32_t t0 = tx + lane_off + (uint32_t)(b * S::NR + 16 * q);
                 tmem_ld16x2(t0, t0 + S::W2, re, im);
+                if constexpr (S::X3) {
+                    float vr[16], vi[16];
 #pragma unroll
-                for (int u = 0; u < 16; u++) {
-                    const float2 w = lfft::cmul(Cq[q], Cu[u]);
-                    const int rr = r * S::W2 + 16 * q + u;
-                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, n1, S::KS, re[u] * w.x - im[u] * w.y);
-                    store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::W1 + n1, S::KS, re[u] * w.y + im[u] * w.x);
+                    for (int u = 0; u < 16; u++) {
+                        const float2 w = lfft::cmul(Cq[q], Cu[u]);
+                        vr[u] = re[u] * w.x - im[u] * w.y;
+                        vi[u] = re[u] * w.y + im[u] * w.x;
+                    }
+                    const int m0 = r * S::W2 + 16 * q;
+                    store_mn_chunk(op, S::OPND, m0, n1, S::MP, vr);
+                    store_mn_chunk(op, S::OPND, m0 + 8, n1, S::MP, vr + 8);
+                    store_mn_chunk(op, S::OPND, m0, S::W1 + n1, S::MP, vi);
+                    store_mn_chunk(op, S::OPND, m0 + 8, S::W1 + n1, S::MP, vi + 8);
+                } else {
+#pragma unroll
+                    for (int u = 0; u < 16; u++) {
+                        const float2 w = lfft::cmul(Cq[q], Cu[u]);
+                        const int rr = r * S::W2 + 16 * q + u;
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, n1, S::KS, re[u] * w.x - im[u] * w.y);
+                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::W1 + n1, S::KS, re[u] * w.y + im[u] * w.x);
+                    }
                 }
             }
         }
         tc_fence_before();
         fence_async_smem();
         __syncthreads();
-        if (!gemm(S::MP, S::KS, smem_u32(f1), S::F1, 2 * S::W1, S::NS, ID_S)) {
+        if (!gemm(S::MP, S::KS, smem_u32(f1), S::F1, 2 * S::W1, S::NS, ID_S, true)) {
             abort = true;
             break;
         }

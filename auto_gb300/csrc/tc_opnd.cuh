@@ -56,6 +56,39 @@ __device__ __forceinline__ void store_chunk(uint8_t* op, int opnd_bytes, int r, 
     }
 }
 
+// 8 values of consecutive m (m0 a multiple of 8) at one k of an MN-major bf16 operand with M rows,
+// as hi and lo (BF16x3): one 16-byte store each.
+__device__ __forceinline__ void store_mn_chunk(uint8_t* op, int opnd_bytes, int m0, int k, int M, const float* v) {
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) split_bf16x2(v[2 * i], v[2 * i + 1], hi[i], lo[i]);
+    const uint32_t off = mnmajor_offset(m0, k, M);
+    *reinterpret_cast<uint4*>(op + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(op + opnd_bytes + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+}
+
+// One BF16x3 GEMM with A MN-major (mnmajor_offset, M rows) and F K-major (f_K elements a row, LBO
+// apart): D[rows of M in blocks of 128] (+)= A (M x K) * F^T.  A row block starts 16 core matrices
+// (2048 bytes) further along MN; an MMA consumes 16 K, two K-groups of A.
+template <int LBO>
+__device__ __forceinline__ void issue_gemm_amn(uint32_t d_tmem, uint32_t a_saddr, uint32_t a_lo_off, int M, int K,
+                                               uint32_t f_saddr, uint32_t f_lo_off, int f_K, int N, uint32_t idesc) {
+    const uint32_t a_lbo = (uint32_t)(M / 8) * 128u, a_sbo = 128u, f_sbo = (uint32_t)(f_K * 2 / 16 * LBO);
+    const int ksteps = K / 16;
+    for (int b = 0; b < M / 128; b++) {
+        const uint32_t d = d_tmem + (uint32_t)(b * N);
+        const uint32_t a0 = a_saddr + (uint32_t)b * 2048u;
+        for (int s = 0; s < ksteps; s++) {
+            const uint64_t ad = smem_desc(a0 + 2u * a_lbo * s, a_lbo, a_sbo);
+            const uint32_t fo = f_saddr + 2u * LBO * s;
+            const uint64_t bd = smem_desc(fo, LBO, f_sbo);
+            mma<false>(d, ad, bd, idesc, s > 0 ? 1u : 0u);
+            mma<false>(d, ad, smem_desc(fo + f_lo_off, LBO, f_sbo), idesc, 1u);
+            mma<false>(d, smem_desc(a0 + a_lo_off + 2u * a_lbo * s, a_lbo, a_sbo), bd, idesc, 1u);
+        }
+    }
+}
+
 // One GEMM: D[rows of M in blocks of 128] (+)= A (M x K) * F^T (F: N x K), both K-major with
 // K-adjacent core matrices LBO bytes apart.  A is laid out with a_K elements per row and F with f_K
 // (f_K > K multiplies by the first K columns of F only), so each has its own 8-row-group stride

@@ -30,6 +30,14 @@ __host__ __device__ constexpr int kmajor_bytes(int M, int K, int elem_bytes, int
     return (M / 8) * (K * elem_bytes / 16) * lbo;
 }
 
+// Byte offset of element (m, k) in an MN-major, no-swizzle bf16 operand with M rows: core matrices of
+// 8 K-rows x 16 bytes (8 consecutive m), MN-adjacent core matrices 128 bytes apart (the descriptor's
+// SBO), K-adjacent groups of 8 K (M / 8) * 128 bytes apart (its LBO).  A thread that holds one k for
+// 8 consecutive m writes them with one 16-byte store.
+__host__ __device__ __forceinline__ uint32_t mnmajor_offset(int m, int k, int M) {
+    return (uint32_t)((((k >> 3) * (M >> 3) + (m >> 3)) << 7) + ((k & 7) << 4) + ((m & 7) << 1));
+}
+
 // tcgen05 shared-memory matrix descriptor: start address, LBO, SBO (all >> 4), version 1 in
 // bits 46-48, no swizzle (bits 61-63 = 0).
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -37,11 +45,12 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
            ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
-// Instruction descriptor, dense, D = f32, A and B K-major: kind::f16 with bf16 operands
-// (format 1) or kind::tf32 (format 2); N >> 3 in bits 17-22, M >> 4 in bits 24-28.
-__host__ __device__ constexpr uint32_t instr_desc(int fmt, int M, int N) {
-    return (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((uint32_t)(N >> 3) << 17) |
-           ((uint32_t)(M >> 4) << 24);
+// Instruction descriptor, dense, D = f32, B K-major: kind::f16 with bf16 operands (format 1) or
+// kind::tf32 (format 2); A K-major, or MN-major with a_mn (bit 15); N >> 3 in bits 17-22, M >> 4 in
+// bits 24-28.
+__host__ __device__ constexpr uint32_t instr_desc(int fmt, int M, int N, bool a_mn = false) {
+    return (1u << 4) | ((uint32_t)fmt << 7) | ((uint32_t)fmt << 10) | ((a_mn ? 1u : 0u) << 15) |
+           ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
 // ----------------------------------------------------------------- mbarriers

@@ -484,11 +484,12 @@ def run_ours(args, dist):
     if not args.no_autotune:
         sim.autotune()  # the engine's autotuner: times every launch variant per size class
     # launch shape per size class after autotuning: variants (column: 0/1 scalar at 64/128 registers,
-    # 2 paired; row: 0/1), chunks of worlds run back to back through L2, rows per row item
+    # 2 paired; row: 0/1), chunks of worlds run back to back through L2, rows per row item, the
+    # cluster-resident step, and whether the row pass runs on the tensor cores
     variants = {"%dx%d" % wh: {"column": v["column_variant"], "row": v["row_variant"], "chunks": v["chunks"],
                                "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
                                "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"],
-                               "resident_variant": v["resident_variant"]}
+                               "resident_variant": v["resident_variant"], "tc_rows": v["tc_rows"]}
                 for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step
@@ -627,23 +628,22 @@ def run_ours(args, dist):
                 paths[pth] = {"value": dist.sum(other.cells_per_step) * g * reps / (t_ms * 1e-3),
                               "ms_per_generation": t_ms / (reps * g)}
         if not any(w.channels != 1 or len(w.kernels) != 1 for w in worlds):
-            # the tensor-core step with its row pass on the FP32 CUDA cores instead (column pass only on
-            # the tensor cores), to show what the tensor-core row pass adds
-            with Sim(worlds, seed=0, path="bf16x3") as other:
-                seed_all(other, worlds, seeds)
-                tc_classes = ["%dx%d" % k for k, v in other.shapes().items() if v["tc_rows"]]
-                other.set_tc_rows(False)
-                if not args.no_autotune:
-                    other.autotune()
-                other.step(G)
-                other.wait()
-                reps = max(2, min(args.steps, 20))
-                t_ms = dist.max(other.step_timed(reps * G))
-                paths["bf16x3_fp32_rows"] = {"value": dist.sum(other.cells_per_step) * G * reps / (t_ms * 1e-3),
-                                             "ms_per_generation": t_ms / (reps * G),
-                                             "what": "BF16x3 column pass with the FP32 row pass; the bf16x3 entry "
-                                                     "runs the row pass on the tensor cores for classes %s" %
-                                                     (", ".join(tc_classes) or "none")}
+            # the tensor-core step with every row pass it can take on the tensor cores, and with every row
+            # pass on the FP32 CUDA cores (the autotuned bf16x3 entry chooses per class)
+            for name, on in (("bf16x3_tc_rows", True), ("bf16x3_fp32_rows", False)):
+                with Sim(worlds, seed=0, path="bf16x3") as other:
+                    seed_all(other, worlds, seeds)
+                    if not args.no_autotune:
+                        other.autotune()
+                    other.set_tc_rows(on)
+                    tc_classes = ["%dx%d" % k for k, v in other.shapes().items() if v["tc_rows"]]
+                    other.step(G)
+                    other.wait()
+                    reps = max(2, min(args.steps, 20))
+                    t_ms = dist.max(other.step_timed(reps * G))
+                    paths[name] = {"value": dist.sum(other.cells_per_step) * G * reps / (t_ms * 1e-3),
+                                   "ms_per_generation": t_ms / (reps * G),
+                                   "tc_row_classes": tc_classes}
         if paths.get("fp32", {}).get("value") and paths.get("radix2", {}).get("value"):
             paths["fp32_over_radix2"] = paths["fp32"]["value"] / paths["radix2"]["value"]
         if paths.get("bf16x3", {}).get("value") and paths.get("radix2", {}).get("value"):

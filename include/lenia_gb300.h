@@ -177,7 +177,8 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
 
 /* Autotuner: times the candidate launch shapes of every size class on this context's worlds
  * and keeps the fastest, one dimension after another: the cluster-resident step against the two
- * launches per generation (where it applies), then for two-pass classes the pair of column and row
+ * launches per generation (where it applies), the tensor-core row pass against the FP32 one
+ * (lenia_set_tc_rows, where it applies), then for two-pass classes the pair of column and row
  * launch variants and every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that
  * changes the class's number of chunks; then, for the whole step, the split of small classes onto a
  * second graph branch (lenia_set_branch_split).
@@ -226,7 +227,8 @@ LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells, int32_t* e
  * lenia_sync.  Rebuilds the step graphs.  No reference counterpart (the reference dispatches every
  * pass of every world separately, crates/auto-core/src/sim.rs:297-380). */
 LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t mode);
-/* The tensor-core row pass on (1, the default) or off (0) on the TF32 and BF16X3 paths: the inverse
+/* The tensor-core row pass on (1, the default until lenia_autotune chooses per class) or off (0) on
+ * the TF32 and BF16X3 paths: the inverse
  * row DFT, the growth / dt / clamp update and the forward row DFT of the one-channel, one-kernel
  * Lenia step as DFT-as-GEMM on tcgen05 (step rows of 256, 512 and 1024 cells; other classes, and
  * every class when off, take the FP32 row pass).  Rebuilds the step graphs.  No reference
@@ -242,10 +244,12 @@ LENIA_API int lenia_kernel_spectrum(const LeniaKernel* kernel, uint32_t width, u
                                     size_t count);
 
 /* Diagnostic: one tensor-core GEMM, D (128 x n) = A (128 x k) * B^T (B is n x k), through the
- * shared-memory operand layout, descriptors and TMEM reads the tensor-core column pass uses.
- * A, B, D are row-major float32 on the host; path is LENIA_PATH_TF32 or LENIA_PATH_BF16X3;
- * n in 32..256 (multiple of 32), k in 16..256 (multiple of 16).  No counterpart in the
- * reference (it has no tensor-core code). */
+ * shared-memory operand layouts, descriptors and TMEM reads the tensor-core passes use.
+ * A, B, D are row-major float32 on the host; path is LENIA_PATH_TF32 or LENIA_PATH_BF16X3, or
+ * LENIA_PATH_BF16X3 | LENIA_SELFTEST_A_MN for A in the MN-major layout of the transposing
+ * hand-overs (k <= 64); n in 32..256 (multiple of 32), k in 16..256 (multiple of 16).  No
+ * counterpart in the reference (it has no tensor-core code). */
+#define LENIA_SELFTEST_A_MN 0x100
 LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float* a, const float* b, float* d);
 
 /* Failure-detection test hook: every barrier wait in the tensor-core column passes gives up

@@ -36,6 +36,23 @@ def test_gemm_selftest(path, tol, n, k):
     assert err < tol, err
 
 
+@pytest.mark.parametrize("n,k", [(64, 64), (128, 64), (32, 32), (256, 16)])
+def test_gemm_selftest_mn_major_a(n, k):
+    """The MN-major A operand of the transposing hand-overs (8 consecutive rows of one k in 16 bytes;
+    MN-adjacent core matrices 128 bytes apart, K-adjacent groups of 8 K M/8 core matrices apart),
+    BF16x3, against float64."""
+    rng = np.random.default_rng(n * k + 11)
+    a = rng.standard_normal((128, k)).astype(np.float32)
+    b = rng.standard_normal((n, k)).astype(np.float32)
+    d = np.zeros((128, n), np.float32)
+    rc = _lib.load().lenia_tc_selftest(_lib.PATH_BF16X3 | _lib.SELFTEST_A_MN, n, k, _lib.fptr(a), _lib.fptr(b),
+                                       _lib.fptr(d))
+    assert rc == 0, _lib.load().lenia_last_error(None)
+    want = a.astype(np.float64) @ b.astype(np.float64).T
+    err = np.abs(d - want).max() / np.abs(want).max()
+    assert err < 2e-4, err
+
+
 @pytest.mark.parametrize("path", ["bf16x3", "tf32"])
 @pytest.mark.parametrize("side", [256, 512, 1024, 2048, 4096])
 def test_tc_u_field_vs_fp64(path, side):
