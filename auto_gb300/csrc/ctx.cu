@@ -47,6 +47,7 @@ struct SizeClass {
     RowItem* d_row = nullptr;
     int nrow = 0;
     int var_col = 0, var_row = 0;  // launch variants (see launch_col_fp32)
+    int var_tc = 0;                // tensor-core column pass variant (launch_col_tc)
     int general = 0, planes = 0;
     size_t bytes = 0;          // device bytes the class's worlds touch in a step
     size_t chunk_budget = 0;   // largest chunk in bytes (0: the whole class is one chunk)
@@ -69,6 +70,12 @@ struct SizeClass {
 // less: every budget measured slower (1024 x 1024: 1.91e11 cell-updates/s as one chunk, 1.75e11 in 8
 // chunks, 1.50e11 in 16).  The autotuner still tries budgets per class.
 constexpr size_t DEFAULT_CHUNK_BUDGET = 0;
+// Whether a class the tensor-core row pass serves starts with it.  Off: measured slower than the FP32
+// row pass at every size it serves (1024 x 1024: 354 us a generation for the class of 55 worlds
+// against 188 us), and its BF16x3 inverse feeds U's rounding error straight into the growth (about
+// 3e-5 a step against FP64, where the FP32 row pass leaves 6e-6).  lenia_set_tc_rows turns it on;
+// the autotuner times it and keeps it only where it is faster.
+constexpr int TC_ROWS_DEFAULT = 0;
 // Whether a class the cluster-resident step serves starts with it (the autotuner then times it
 // against the two launches per generation and keeps the faster).
 constexpr int RESIDENT_DEFAULT = 0;
@@ -382,7 +389,7 @@ int flush_spectra(LeniaCtx* ctx) {
 
 // The column pass of one class (or one world's slice of it).
 bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int ncol, const ColItem* tcg, int ntcg,
-                    int variant, cudaStream_t s) {
+                    int variant, int var_tc, cudaStream_t s) {
     if (ntcg <= 0) return launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
     // Tensor-core paths: the FP32 items (each channel's first tile group, which holds the packed
     // DC/Nyquist column) are few.  After the tensor-core launch they ran on an otherwise idle GPU
@@ -390,14 +397,14 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
     // so they run beside it on a side stream, on SMs the persistent tensor-core grid leaves free.
     const int reserve = (ncol + 1) / 2;
     if (ncol <= 0 || reserve > ctx->sms / 16) {
-        const bool ok = launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
+        const bool ok = launch_col_tc(ctx->tc, ctx->path, cl.H, var_tc, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
         return ok && launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
     }
     if (cudaEventRecord(ctx->ev_fork, s) != cudaSuccess || cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0) != cudaSuccess)
         return false;
     bool ok = launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, ctx->side);
     ok = ok && cudaEventRecord(ctx->ev_join, ctx->side) == cudaSuccess;
-    ok = ok && launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s, reserve);
+    ok = ok && launch_col_tc(ctx->tc, ctx->path, cl.H, var_tc, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s, reserve);
     return ok && cudaStreamWaitEvent(s, ctx->ev_join, 0) == cudaSuccess;
 }
 
@@ -412,10 +419,10 @@ bool launch_rows_step(LeniaCtx* ctx, const SizeClass& cl, int variant, const Row
 
 // A launch shape of one size class: launch variants and chunks.
 struct Shape {
-    int var_col, var_row;
+    int var_col, var_row, var_tc;
     const std::vector<Chunk>* chunks;
 };
-Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, &cl.chunks}; }
+Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, cl.var_tc, &cl.chunks}; }
 
 // `steps` steps of one size class, chunk after chunk, in the given launch shape; a resident class is
 // one launch for all its worlds and steps.
@@ -428,7 +435,8 @@ int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps
     }
     for (const Chunk& ch : *sh.chunks) {
         for (int st = 0; st < steps; st++) {
-            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col, s);
+            bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col,
+                                     sh.var_tc, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
             ok = launch_rows_step(ctx, cl, sh.var_row, cl.d_row + ch.row0, ch.nrow, s);
             if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
@@ -738,7 +746,8 @@ int setup_fused(LeniaCtx* ctx) {
                 int trc = tc_row_prepare(ctx->tc, ctx->path, cl.W, &ctx->err);
                 if (trc) return trc;
                 cl.tc_row_stride = rg / (int)item_rows;
-                cl.tc_rows_ok = cl.tc_rows = 1;
+                cl.tc_rows_ok = 1;
+                cl.tc_rows = TC_ROWS_DEFAULT;
             }
         }
         // per-world slices of the class lists
@@ -781,8 +790,9 @@ int setup_fused(LeniaCtx* ctx) {
                                  ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
         }
-        if (cl.ntcg > 0 && !launch_col_tc(ctx->tc, ctx->path, cl.H, ctx->d_worlds, cl.d_tcg, 0, ctx->d_tw, ctx->stream))
-            return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core pass for H=%d", cl.H);
+        for (int v = 0; v < TC_COL_VARIANTS && cl.ntcg > 0; v++)
+            if (!launch_col_tc(ctx->tc, ctx->path, cl.H, v, ctx->d_worlds, cl.d_tcg, 0, ctx->d_tw, ctx->stream))
+                return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core pass for H=%d", cl.H);
         if (cl.tc_rows_ok &&
             !launch_row_tc(ctx->tc, ctx->path, cl.W, ctx->d_worlds, cl.d_row, cl.tc_row_stride, 0, ctx->d_tw, ctx->stream))
             return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core row pass for W=%d", cl.W);
@@ -882,7 +892,7 @@ int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, d
     for (const Chunk& ch : chunks) {
         for (int st = 0; st < steps; st++) {
             bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col,
-                                     ctx->stream);
+                                     sh.var_tc, ctx->stream);
             CK(cudaEventRecord(ev.e[k++], ctx->stream));
             ok = ok && launch_rows_step(ctx, cl, sh.var_row, cl.d_row + ch.row0, ch.nrow, ctx->stream);
             CK(cudaEventRecord(ev.e[k++], ctx->stream));
@@ -1358,7 +1368,7 @@ int lenia_read_field_u(LeniaCtx* ctx, int32_t world, int32_t kernel, float* host
     }
     const WorldBuffers& b = ctx->wb[world];
     const SizeClass& cl = ctx->classes[b.cls];
-    bool ok = launch_columns(ctx, cl, b.d_col, b.ncol, b.d_tcg, b.ntcg, cl.var_col, ctx->stream);
+    bool ok = launch_columns(ctx, cl, b.d_col, b.ncol, b.d_tcg, b.ntcg, cl.var_col, cl.var_tc, ctx->stream);
     ok = ok && launch_row_fp32(cl.W, cl.var_row, MODE_U, cl.general, ctx->d_worlds, b.d_row, b.nrow, cl.planes, ctx->d_tw,
                                ctx->stream);
     if (!ok) return fail(ctx, LENIA_ECUDA, "U launch failed");
@@ -1559,6 +1569,18 @@ int lenia_set_resident(LeniaCtx* ctx, int32_t mode) {
     return 0;
 }
 
+int lenia_set_tc_variant(LeniaCtx* ctx, int32_t variant) {
+    if (!ctx) return LENIA_EINVAL;
+    if (variant < 0 || variant >= TC_COL_VARIANTS)
+        return fail(ctx, LENIA_EINVAL, "tensor-core column variants are 0..%d", TC_COL_VARIANTS - 1);
+    for (auto& cl : ctx->classes) cl.var_tc = variant;
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
 int lenia_set_tc_rows(LeniaCtx* ctx, int32_t on) {
     if (!ctx) return LENIA_EINVAL;
     if (on != 0 && on != 1) return fail(ctx, LENIA_EINVAL, "on must be 0 or 1");
@@ -1594,10 +1616,10 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (count < 11 * ctx->classes.size()) return LENIA_EINVAL;
+    if (count < 12 * ctx->classes.size()) return LENIA_EINVAL;
     for (size_t i = 0; i < ctx->classes.size(); i++) {
         const auto& cl = ctx->classes[i];
-        int32_t* o = out + 11 * i;
+        int32_t* o = out + 12 * i;
         o[0] = cl.W;
         o[1] = cl.H;
         o[2] = cl.var_col;
@@ -1609,6 +1631,7 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
         o[8] = cl.resident;
         o[9] = cl.var_res;
         o[10] = cl.tc_rows;
+        o[11] = cl.ntcg > 0 ? cl.var_tc : -1;
     }
     return 0;
 }
@@ -1682,6 +1705,15 @@ static int autotune_search(LeniaCtx* ctx) {
             }
             if (cl.resident) continue;  // launch variants and chunks do not apply to it
         }
+        if (cl.ntcg > 0) {
+            // the tensor-core column pass's variants (staged tile groups, or L2-prefetched loads with more
+            // CTAs an SM); candidate 0 is the current choice
+            std::vector<Shape> c{shape_of(cl)};
+            for (int v = 0; v < TC_COL_VARIANTS; v++)
+                if (v != cl.var_tc) c.push_back(Shape{cl.var_col, cl.var_row, v, &cl.chunks});
+            if ((rc = pick(c, &bi))) return rc;
+            cl.var_tc = c[bi].var_tc;
+        }
         if (cl.tc_rows_ok) {
             // the tensor-core row pass against the FP32 row pass (TF32 / BF16X3 paths); candidate 0 is
             // the current choice
@@ -1699,7 +1731,7 @@ static int autotune_search(LeniaCtx* ctx) {
             std::vector<Shape> c{shape_of(cl)};
             for (int vc = 0; vc < 3; vc++)
                 for (int vr = 0; vr < 2; vr++)
-                    if (vc != cl.var_col || vr != cl.var_row) c.push_back(Shape{vc, vr, &cl.chunks});
+                    if (vc != cl.var_col || vr != cl.var_row) c.push_back(Shape{vc, vr, cl.var_tc, &cl.chunks});
             if ((rc = pick(c, &bi))) return rc;
             cl.var_col = c[bi].var_col;
             cl.var_row = c[bi].var_row;
@@ -1714,7 +1746,7 @@ static int autotune_search(LeniaCtx* ctx) {
                 if (!seen) lists.push_back(ch), bud.push_back(b);
             }
             std::vector<Shape> c;
-            for (auto& l : lists) c.push_back(Shape{cl.var_col, cl.var_row, &l});
+            for (auto& l : lists) c.push_back(Shape{cl.var_col, cl.var_row, cl.var_tc, &l});
             if ((rc = pick(c, &bi))) return rc;
             cl.chunk_budget = bud[bi];
             cl.chunks = lists[bi];

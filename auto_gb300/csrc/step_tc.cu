@@ -32,10 +32,16 @@
 namespace lenia {
 using namespace tc;
 
-template <int H1_, int H2_, int CT_, bool X3_, int LBO_>
+template <int H1_, int H2_, int CT_, bool X3_, int LBO_, int WG_, int MINB_, bool STAGED_ = true>
 struct TcShape {
     static constexpr int H1 = H1_, H2 = H2_, CT = CT_, H = H1 * H2;
     static constexpr bool X3 = X3_;
+    static constexpr int WG = WG_, NT = 128 * WG_;    // warpgroups sharing each hand-over
+    static constexpr int MINB = MINB_;                // CTAs per SM the register budget is set for
+    // STAGED: the next tile group arrives by a bulk copy into a staging buffer while this one computes;
+    // else stage 0 reads it from global memory (prefetched into L2 a group ahead) and the CTA needs
+    // 32 KB less shared memory, so more CTAs fit an SM
+    static constexpr bool STAGED = STAGED_;
     static constexpr int E = X3 ? 2 : 4;              // operand element bytes
     static constexpr int NOP = X3 ? 2 : 1;            // hi/lo copies
     static constexpr int MA = CT * H1, KA = 2 * H2, NA = 2 * H2;
@@ -49,7 +55,7 @@ struct TcShape {
     static constexpr int OFF_F1 = OFF_F2 + FA * NOP;
     static constexpr int OFF_STG = OFF_F1 + (SAME ? 0 : FB * NOP);
     static constexpr int HQ = (H / 2 + 1 + 3) / 4 * 4;  // kernel-spectrum row stride (floats)
-    static constexpr int OFF_KH = OFF_STG + STG;      // the group's CT kernel-spectrum rows
+    static constexpr int OFF_KH = OFF_STG + (STAGED ? STG : 0);  // the group's CT kernel-spectrum rows
     static constexpr int KHB = CT * HQ * 4;
     static constexpr int OFF_BAR = OFF_KH + KHB;
     static constexpr int SMEM = OFF_BAR + 64;
@@ -59,12 +65,28 @@ struct TcShape {
     static_assert(kmajor_bytes(MB, KB, E, LBO) == OPND, "both GEMM shapes fill one operand area");
     static_assert(OPND * NOP >= STG, "the output staging reuses the operand area");
     static_assert(MA % 128 == 0 && MB % 128 == 0, "row blocks of 128");
-    static_assert(NA % 32 == 0 && NB % 32 == 0, "TMEM loads of 32 columns");
+    static_assert(H1 % 8 == 0 && H2 % 8 == 0 && (H2 / WG) % 8 == 0, "hand-over units of 8 values");
     static_assert(2 * REGION <= 512, "TMEM");
     static_assert(SMEM <= 232448, "shared memory of one CTA");
 };
 
+// t[h] for a run-time h, by selects over the unrolled table (an indexed load would put the table in
+// local memory)
+template <int N>
+__device__ __forceinline__ float2 pick(const float2 (&t)[N], int h) {
+    float2 r = t[0];
+#pragma unroll
+    for (int i = 1; i < N; i++)
+        if (h == i) r = t[i];
+    return r;
+}
+
 // A group is (world, channel, first tile); it covers CT columns = CT / TC consecutive tiles.
+//
+// NT = 128 WG threads: thread t serves GEMM row lt = t mod 128 of every 128-row block (the TMEM lane its
+// warp reads), and the WG warpgroups split each hand-over into units of 16 TMEM columns (8 complex
+// values: one 16-byte operand chunk of real and one of imaginary parts), so that more warps hide the
+// latency of the TMEM loads and shared-memory stores between the GEMMs.
 //
 // Every barrier wait is bounded, and the decision to give up is made for the whole CTA at once
 // (__syncthreads_or), so that no thread is left at a barrier the others skipped.  A CTA that gives
@@ -72,7 +94,7 @@ struct TcShape {
 // DFT-matrix load, a tile-group load, issued MMAs, its output stores -- then sets the error flag
 // (ctl[CTL_ERR]), frees its TMEM and returns.
 template <class S>
-__global__ void __launch_bounds__(128, 1)
+__global__ void __launch_bounds__(S::NT, S::MINB)
     col_pass_tc(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ groups, int ngroups,
                 const uint8_t* __restrict__ fmats, const float2* __restrict__ tw, int* ctl) {
     extern __shared__ __align__(128) uint8_t smem[];
@@ -86,13 +108,14 @@ __global__ void __launch_bounds__(128, 1)
     uint64_t* bar_kh = bar_ld + 3;  // the group's kernel-spectrum rows arrived
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_ld + 4);
     float* khs = reinterpret_cast<float*>(smem + S::OFF_KH);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, lt = tid & 127, wg = tid >> 7;
     constexpr uint32_t IDESC_A = instr_desc(S::X3 ? 1 : 2, 128, S::NA);
     constexpr uint32_t IDESC_B = instr_desc(S::X3 ? 1 : 2, 128, S::NB);
     // BF16x3: the transposing hand-overs (A -> B, C -> D) store MN-major A operands, 16 bytes a store
     // (TF32 keeps every operand K-major)
     constexpr uint32_t IDESC_AM = instr_desc(S::X3 ? 1 : 2, 128, S::NA, S::X3);
     constexpr uint32_t IDESC_BM = instr_desc(S::X3 ? 1 : 2, 128, S::NB, S::X3);
+    constexpr int CH = S::X3 ? 8 : 4;  // values per 16-byte K-major operand chunk
 
     if (tid == 0) {
         mbar_init(bar_ld, 1);
@@ -108,25 +131,23 @@ __global__ void __launch_bounds__(128, 1)
     const uint32_t tbase = *tmem_slot;
     const uint32_t t_b = tbase;                 // D of GEMM B (kept while every kernel of the channel runs)
     const uint32_t t_x = tbase + S::REGION;     // D of GEMMs A, C, D
-    const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
 
-    // The twiddles of the two hand-overs from per-thread tables.  A thread's rows are r = b*128 + tid,
-    // and 128 is a multiple of H1 and of H2, so its y1 (A -> B) and its k2 (C -> D) are the same in
-    // every row block: exp(-2 pi i y1 k2 / H) with k2 = 16 q + u is A_q[q] * A_u[u], and with
-    // y1 = 16 q + u it is C_q[q] * C_u[u] -- two exactly rounded table values and one product,
-    // instead of a load from the 24576-entry table per element.
-    constexpr int QA = S::H2 / 16, QC = S::H1 / 16;
-    float2 Aq[QA], Au[16], Cq[QC], Cu[16];
+    // The twiddles of the two hand-overs from per-thread tables.  A thread's rows are b*128 + lt, and
+    // 128 is a multiple of H1 and of H2, so its y1 (A -> B) and its k2 (C -> D) are the same in every
+    // row block: exp(-2 pi i y1 k2 / H) with k2 = 8 h + j is A8[h] * A1[j], and with y1 = 8 h + j it is
+    // C8[h] * C1[j] -- two exactly rounded table values and one product.
+    float2 A8[S::H2 / 8], A1[8], C8[S::H1 / 8], C1[8];
     {
-        const int y1 = tid % S::H1, k2 = tid % S::H2;
+        const int y1 = lt % S::H1, k2 = lt % S::H2;
 #pragma unroll
-        for (int q = 0; q < QA; q++) Aq[q] = twid<S::H>(tw, y1, 16 * q);
+        for (int h = 0; h < S::H2 / 8; h++) A8[h] = twid<S::H>(tw, y1, 8 * h);
 #pragma unroll
-        for (int q = 0; q < QC; q++) Cq[q] = twid<S::H>(tw, k2, 16 * q);
+        for (int h = 0; h < S::H1 / 8; h++) C8[h] = twid<S::H>(tw, k2, 8 * h);
 #pragma unroll
-        for (int u = 0; u < 16; u++) {
-            Au[u] = twid<S::H>(tw, y1, u);
-            Cu[u] = twid<S::H>(tw, k2, u);
+        for (int j = 0; j < 8; j++) {
+            A1[j] = twid<S::H>(tw, y1, j);
+            C1[j] = twid<S::H>(tw, k2, j);
         }
     }
 
@@ -136,16 +157,29 @@ __global__ void __launch_bounds__(128, 1)
         mbar_arrive_expect_tx(bar_f, fbytes);
         bulk_g2s(f2, fmats, fbytes, bar_f);
     }
-    auto load_group = [&](int g) {
+    // the CT columns of group g: CT / TC consecutive tiles, contiguous
+    auto group_src = [&](int g) {
         const ColItem it = groups[g];
         const DevWorld& wd = worlds[it.world];
-        const float2* src = wd.spec + (size_t)it.chan * (wd.W / 2) * S::H + (size_t)it.tile * S::H * TC;
-        mbar_arrive_expect_tx(bar_ld, S::STG);
-        bulk_g2s(stg, src, S::STG, bar_ld);
+        return wd.spec + (size_t)it.chan * (wd.W / 2) * S::H + (size_t)it.tile * S::H * TC;
+    };
+    auto load_group = [&](int g) {
+        if constexpr (S::STAGED) {
+            mbar_arrive_expect_tx(bar_ld, S::STG);
+            bulk_g2s(stg, group_src(g), S::STG, bar_ld);
+        } else {
+            bulk_prefetch_l2(group_src(g), S::STG);
+        }
+    };
+    // the group's CT kernel-spectrum rows of kernel k (kx0 .. kx0 + CT - 1, HQ floats each, contiguous)
+    // by one bulk copy into shared memory, instead of a global load per element of the hand-over
+    auto load_khat = [&](const DevWorld& wd, int k, int kx0) {
+        mbar_arrive_expect_tx(bar_kh, S::KHB);
+        bulk_g2s(khs, wd.khat + ((size_t)k * (wd.W / 2 + 1) + kx0) * wd.HQ, S::KHB, bar_kh);
     };
     if (tid == 0 && blockIdx.x < ngroups) load_group(blockIdx.x);
     // asynchronous work in flight that an early exit has to wait for (uniform across the CTA)
-    bool ld_pending = blockIdx.x < ngroups, mma_pending = false, kh_pending = false;
+    bool ld_pending = S::STAGED && blockIdx.x < ngroups, mma_pending = false, kh_pending = false;
     uint32_t ph_kh = 0;
     const bool f_failed = __syncthreads_or(!mbar_wait_n(bar_f, 0, f_wait_polls(ctl)));
     bool abort = f_failed;
@@ -169,27 +203,63 @@ __global__ void __launch_bounds__(128, 1)
         tc_fence_after();
         return true;
     };
+    // A transposing hand-over unit: 8 complex values (interleaved re, im) v_j times w(j) = W8 * W1[j],
+    // into an A operand at rows m0..m0+7 (MN-major, BF16x3) or rows m0 + j (K-major), columns k (real
+    // part) and k + KH (imaginary part).
+    auto store_t8 = [&](const float* v, float2 w8, const float2* w1, int m0, int k, int KH, int M, int K) {
+        float vr[8], vi[8];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const float2 w = lfft::cmul(w8, w1[j]);
+            vr[j] = v[2 * j] * w.x - v[2 * j + 1] * w.y;
+            vi[j] = v[2 * j] * w.y + v[2 * j + 1] * w.x;
+        }
+        if constexpr (S::X3) {
+            store_mn_chunk(op, S::OPND, m0, k, M, vr);
+            store_mn_chunk(op, S::OPND, m0, k + KH, M, vi);
+        } else {
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                store_elem<false, S::LBO>(op, S::OPND, m0 + j, k, K, vr[j]);
+                store_elem<false, S::LBO>(op, S::OPND, m0 + j, k + KH, K, vi[j]);
+            }
+        }
+    };
 
     for (int g = blockIdx.x; g < ngroups && !abort; g += gridDim.x) {
         const ColItem it = groups[g];
         const DevWorld& wd = worlds[it.world];
-        const int W = wd.W, HQ = wd.HQ, K = wd.K;
+        const int W = wd.W, K = wd.K;
         const int kx0 = it.tile * TC;
         if (tid == 0) bulk_wait_read0();  // the previous group's output has left the operand area
-        if (__syncthreads_or(!mbar_wait(bar_ld, ph_ld))) {
-            abort = true;
-            break;
+        if constexpr (S::STAGED) {
+            if (__syncthreads_or(!mbar_wait(bar_ld, ph_ld))) {
+                abort = true;
+                break;
+            }
+            ld_pending = false;
+            ph_ld ^= 1;
+        } else {
+            __syncthreads();
+            // the next group's columns into L2 while this one computes
+            if (tid == 0 && g + (int)gridDim.x < ngroups) load_group(g + gridDim.x);
         }
-        ld_pending = false;
-        ph_ld ^= 1;
+        // the kernel-spectrum rows of the first kernel that reads this channel, fetched now so that
+        // they have arrived when the hand-over after GEMM B needs them
+        int kfirst = 0;
+        while (kfirst < K && wd.kern[kfirst].src != it.chan) kfirst++;
+        if (kfirst < K) {
+            if (tid == 0) load_khat(wd, kfirst, kx0);
+            kh_pending = true;
+        }
 
-        // ---- stage 0: tile group (fp32, [tile][y][c][re,im]) -> A_A rows (c, y1), K (re/im, y2)
+        // ---- stage 0: tile group (fp32, [tile][y][c][re,im]) -> A_A rows (c, y1), K (re/im, y2); the
+        //      warpgroups split y2
         for (int b = 0; b < S::MA / 128; b++) {
-            const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
-            const float2* col = stg + (size_t)(c / TC) * S::H * TC + (c % TC);
-            constexpr int CH = S::X3 ? 8 : 4;
+            const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
+            const float2* col = (S::STAGED ? stg : group_src(g)) + (size_t)(c / TC) * S::H * TC + (c % TC);
 #pragma unroll 2
-            for (int y2 = 0; y2 < S::H2; y2 += CH) {
+            for (int y2 = wg * (S::H2 / S::WG); y2 < (wg + 1) * (S::H2 / S::WG); y2 += CH) {
                 float re[CH], im[CH];
 #pragma unroll
                 for (int u = 0; u < CH; u++) {
@@ -204,7 +274,7 @@ __global__ void __launch_bounds__(128, 1)
         fence_async_smem();
         __syncthreads();
         // the staging buffer is free: fetch the next group while this one computes
-        if (g + (int)gridDim.x < ngroups) {
+        if (S::STAGED && g + (int)gridDim.x < ngroups) {
             if (tid == 0) load_group(g + gridDim.x);
             ld_pending = true;
         }
@@ -215,39 +285,13 @@ __global__ void __launch_bounds__(128, 1)
             break;
         }
 
-        // ---- A -> B: twiddle exp(-2 pi i y1 k2 / H), rows (c, k2), K (re/im, y1)
-        for (int b = 0; b < S::MA / 128; b++) {
-            const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
-#pragma unroll
-            for (int q = 0; q < S::NA / 32; q++) {
-                float v[32];
-                tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NA + 32 * q), v);
-                if constexpr (S::X3) {
-                    float vr[16], vi[16];
-#pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        const float2 w = lfft::cmul(Aq[q], Au[u]);
-                        vr[u] = v[2 * u] * w.x - v[2 * u + 1] * w.y;
-                        vi[u] = v[2 * u] * w.y + v[2 * u + 1] * w.x;
-                    }
-                    const int m0 = c * S::H2 + 16 * q;
-                    store_mn_chunk(op, S::OPND, m0, y1, S::MB, vr);
-                    store_mn_chunk(op, S::OPND, m0 + 8, y1, S::MB, vr + 8);
-                    store_mn_chunk(op, S::OPND, m0, S::H1 + y1, S::MB, vi);
-                    store_mn_chunk(op, S::OPND, m0 + 8, S::H1 + y1, S::MB, vi + 8);
-                } else {
-#pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        const int k2 = 16 * q + u;
-                        const float2 w = lfft::cmul(Aq[q], Au[u]);
-                        const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
-                        const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
-                        const int rr = c * S::H2 + k2;
-                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, y1, S::KB, re);
-                        store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H1 + y1, S::KB, im);
-                    }
-                }
-            }
+        // ---- A -> B: twiddle exp(-2 pi i y1 k2 / H), rows (c, k2), K (re/im, y1); units (block, 8 k2)
+        for (int un = wg; un < (S::MA / 128) * (S::NA / 16); un += S::WG) {
+            const int b = un / (S::NA / 16), h = un % (S::NA / 16);
+            const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
+            float v[16];
+            tmem_ld16(t_x + lane_off + (uint32_t)(b * S::NA + 16 * h), v);
+            store_t8(v, pick(A8, h), A1, c * S::H2 + 8 * h, y1, S::H1, S::MB, S::KB);
         }
         tc_fence_before();
         fence_async_smem();
@@ -259,85 +303,59 @@ __global__ void __launch_bounds__(128, 1)
             break;
         }
 
-        for (int k = 0; k < K && !abort; k++) {
+        for (int k = kfirst; k < K && !abort; k++) {
             if (wd.kern[k].src != it.chan) continue;
-            // the group's CT kernel-spectrum rows (kx0 .. kx0 + CT - 1, HQ floats each, contiguous) by
-            // one bulk copy into shared memory, instead of a global load per element of the hand-over
-            if (tid == 0) {
-                mbar_arrive_expect_tx(bar_kh, S::KHB);
-                bulk_g2s(khs, wd.khat + ((size_t)k * (W / 2 + 1) + kx0) * HQ, S::KHB, bar_kh);
-            }
-            kh_pending = true;
             if (__syncthreads_or(!mbar_wait(bar_kh, ph_kh))) {
                 abort = true;
                 break;
             }
             kh_pending = false;
             ph_kh ^= 1;
-            // ---- B -> C: x khat (real, even), conjugate; rows (c, k2), K (re/im, k1)
-            for (int b = 0; b < S::MB / 128; b++) {
-                const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
+            // ---- B -> C: x khat (real, even), conjugate; rows (c, k2), K (re/im, k1); units (block, 8 k1)
+            for (int un = wg; un < (S::MB / 128) * (S::NB / 16); un += S::WG) {
+                const int b = un / (S::NB / 16), h = un % (S::NB / 16);
+                const int r = b * 128 + lt, c = r / S::H2, k2 = r % S::H2;
                 const float* khrow = khs + c * S::HQ;
-                for (int q = 0; q < S::NB / 32; q++) {
-                    float v[32];
-                    tmem_ld32(t_b + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
-                    float re[16], im[16];
+                float v[16];
+                tmem_ld16(t_b + lane_off + (uint32_t)(b * S::NB + 16 * h), v);
+                float re[8], im[8];
 #pragma unroll
-                    for (int u = 0; u < 16; u++) {
-                        const int ky = k2 + S::H2 * (16 * q + u);
-                        const float s = khrow[ky <= S::H / 2 ? ky : S::H - ky];
-                        re[u] = v[2 * u] * s;
-                        im[u] = -v[2 * u + 1] * s;
-                    }
-                    constexpr int CH = S::X3 ? 8 : 4;
+                for (int j = 0; j < 8; j++) {
+                    const int ky = k2 + S::H2 * (8 * h + j);
+                    const float sc = khrow[ky <= S::H / 2 ? ky : S::H - ky];
+                    re[j] = v[2 * j] * sc;
+                    im[j] = -v[2 * j + 1] * sc;
+                }
 #pragma unroll
-                    for (int u = 0; u < 16; u += CH) {
-                        store_chunk<S::X3, S::LBO>(op, S::OPND, r, 16 * q + u, S::KB, re + u);
-                        store_chunk<S::X3, S::LBO>(op, S::OPND, r, S::H1 + 16 * q + u, S::KB, im + u);
-                    }
+                for (int j = 0; j < 8; j += CH) {
+                    store_chunk<S::X3, S::LBO>(op, S::OPND, r, 8 * h + j, S::KB, re + j);
+                    store_chunk<S::X3, S::LBO>(op, S::OPND, r, S::H1 + 8 * h + j, S::KB, im + j);
                 }
             }
             tc_fence_before();
             fence_async_smem();
             __syncthreads();
+            // the next kernel's rows (if another kernel reads this channel) while this one finishes
+            {
+                int kn = k + 1;
+                while (kn < K && wd.kern[kn].src != it.chan) kn++;
+                if (kn < K) {
+                    if (tid == 0) load_khat(wd, kn, kx0);
+                    kh_pending = true;
+                }
+            }
             // ---- GEMM C
             if (!gemm(t_x, S::OPND, S::MB, S::KB, smem_u32(f1), S::FB, S::NB, IDESC_B)) {
                 abort = true;
                 break;
             }
-            // ---- C -> D: twiddle exp(-2 pi i k2 y1 / H); rows (c, y1), K (re/im, k2)
-            for (int b = 0; b < S::MB / 128; b++) {
-                const int r = b * 128 + tid, c = r / S::H2, k2 = r % S::H2;
-#pragma unroll
-                for (int q = 0; q < S::NB / 32; q++) {
-                    float v[32];
-                    tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NB + 32 * q), v);
-                    if constexpr (S::X3) {
-                        float vr[16], vi[16];
-#pragma unroll
-                        for (int u = 0; u < 16; u++) {
-                            const float2 w = lfft::cmul(Cq[q], Cu[u]);
-                            vr[u] = v[2 * u] * w.x - v[2 * u + 1] * w.y;
-                            vi[u] = v[2 * u] * w.y + v[2 * u + 1] * w.x;
-                        }
-                        const int m0 = c * S::H1 + 16 * q;
-                        store_mn_chunk(op, S::OPND, m0, k2, S::MA, vr);
-                        store_mn_chunk(op, S::OPND, m0 + 8, k2, S::MA, vr + 8);
-                        store_mn_chunk(op, S::OPND, m0, S::H2 + k2, S::MA, vi);
-                        store_mn_chunk(op, S::OPND, m0 + 8, S::H2 + k2, S::MA, vi + 8);
-                    } else {
-#pragma unroll
-                        for (int u = 0; u < 16; u++) {
-                            const int y1 = 16 * q + u;
-                            const float2 w = lfft::cmul(Cq[q], Cu[u]);
-                            const float re = v[2 * u] * w.x - v[2 * u + 1] * w.y;
-                            const float im = v[2 * u] * w.y + v[2 * u + 1] * w.x;
-                            const int rr = c * S::H1 + y1;
-                            store_elem<S::X3, S::LBO>(op, S::OPND, rr, k2, S::KA, re);
-                            store_elem<S::X3, S::LBO>(op, S::OPND, rr, S::H2 + k2, S::KA, im);
-                        }
-                    }
-                }
+            // ---- C -> D: twiddle exp(-2 pi i k2 y1 / H); rows (c, y1), K (re/im, k2); units (block, 8 y1)
+            for (int un = wg; un < (S::MB / 128) * (S::NB / 16); un += S::WG) {
+                const int b = un / (S::NB / 16), h = un % (S::NB / 16);
+                const int r = b * 128 + lt, c = r / S::H2, k2 = r % S::H2;
+                float v[16];
+                tmem_ld16(t_x + lane_off + (uint32_t)(b * S::NB + 16 * h), v);
+                store_t8(v, pick(C8, h), C1, c * S::H1 + 8 * h, k2, S::H2, S::MA, S::KA);
             }
             tc_fence_before();
             fence_async_smem();
@@ -347,18 +365,17 @@ __global__ void __launch_bounds__(128, 1)
                 abort = true;
                 break;
             }
-            // ---- output: conjugate, natural order y = y1 + H1*y2, into the operand area
+            // ---- output: conjugate, natural order y = y1 + H1*y2, into the operand area; units (block, 8 y2)
             float2* out = reinterpret_cast<float2*>(op);
-            for (int b = 0; b < S::MA / 128; b++) {
-                const int r = b * 128 + tid, c = r / S::H1, y1 = r % S::H1;
+            for (int un = wg; un < (S::MA / 128) * (S::NA / 16); un += S::WG) {
+                const int b = un / (S::NA / 16), h = un % (S::NA / 16);
+                const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
                 float2* col = out + (size_t)(c / TC) * S::H * TC + (c % TC);
-                for (int q = 0; q < S::NA / 32; q++) {
-                    float v[32];
-                    tmem_ld32(t_x + lane_off + (uint32_t)(b * S::NA + 32 * q), v);
+                float v[16];
+                tmem_ld16(t_x + lane_off + (uint32_t)(b * S::NA + 16 * h), v);
 #pragma unroll
-                    for (int u = 0; u < 16; u++)
-                        col[(size_t)(y1 + S::H1 * (16 * q + u)) * TC] = make_float2(v[2 * u], -v[2 * u + 1]);
-                }
+                for (int j = 0; j < 8; j++)
+                    col[(size_t)(y1 + S::H1 * (8 * h + j)) * TC] = make_float2(v[2 * j], -v[2 * j + 1]);
             }
             tc_fence_before();
             fence_async_smem();
@@ -425,14 +442,16 @@ void build_dft_operand(int n, bool x3, std::vector<uint8_t>& out, int lbo) {
         }
 }
 
-// Column length, its factors H1 x H2, columns per group, and the operand layout's LBO: padded (144,
-// bank-conflict-free hand-over stores) where it fits in shared memory beside the kernel-spectrum
-// rows, packed (128) at 2048 and in the 4096-point kernel (step_tc64.cu).
+// Column length, its factors H1 x H2, columns per group, and the operand layouts' LBO per path: BF16x3
+// packed (128: its transposing hand-overs store MN-major operands, the others whole 16-byte rows),
+// TF32 padded (144: its transposing hand-overs store 4-byte values into K-major operands, and 16 bytes
+// between K-adjacent core matrices spread a warp's stores over the banks) where that fits.
 struct ShapeInfo {
-    int H, H1, H2, CT, LBO;
+    int H, H1, H2, CT, LBO_X3, LBO_TF32;
 };
-constexpr ShapeInfo SHAPES[] = {{4096, 64, 64, 2, 128}, {2048, 64, 32, 4, 128}, {1024, 32, 32, 4, 144},
-                                {512, 32, 16, 8, 144}, {256, 16, 16, 8, 144}};
+constexpr ShapeInfo SHAPES[] = {{4096, 64, 64, 2, 128, 128}, {2048, 64, 32, 4, 128, 128},
+                                {1024, 32, 32, 4, 128, 144}, {512, 32, 16, 8, 128, 144},
+                                {256, 16, 16, 8, 128, 144}};
 
 const ShapeInfo* shape_for(int H) {
     for (const auto& s : SHAPES)
@@ -469,7 +488,7 @@ bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups,
             cudaFuncGetAttributes(&fa, col_pass_tc<S>) != cudaSuccess)
             return false;
         int n = smem_sm / (S::SMEM + reserved);
-        const int by_regs = regs_sm / (128 * (fa.numRegs > 0 ? fa.numRegs : 255));
+        const int by_regs = regs_sm / (S::NT * (fa.numRegs > 0 ? fa.numRegs : 255));
         if (by_regs < n) n = by_regs;
         if (n * S::TCOLS > 512) n = 512 / S::TCOLS;
         per_sm = n < 1 ? 1 : n;
@@ -477,7 +496,7 @@ bool launch_shape(const void* fm, const DevWorld* worlds, const ColItem* groups,
     int grid = (sms - reserve_sms) * per_sm;
     if (grid > ngroups) grid = ngroups;
     if (grid < 1) grid = 1;
-    col_pass_tc<S><<<grid, 128, S::SMEM, st>>>(worlds, groups, ngroups, (const uint8_t*)fm, tw, err);
+    col_pass_tc<S><<<grid, S::NT, S::SMEM, st>>>(worlds, groups, ngroups, (const uint8_t*)fm, tw, err);
     return true;
 }
 
@@ -516,7 +535,7 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
     }
     const bool x3 = path == LENIA_PATH_BF16X3;
     std::vector<uint8_t> host;
-    const int lbo = s->LBO;
+    const int lbo = x3 ? s->LBO_X3 : s->LBO_TF32;
     build_dft_operand(s->H2, x3, host, lbo);                  // F_H2 (hi, lo)
     if (s->H1 != s->H2) build_dft_operand(s->H1, x3, host, lbo);  // F_H1 (hi, lo)
     void* d = nullptr;
@@ -534,8 +553,8 @@ int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err) {
 
 bool tc_supports(int H) { return shape_for(H) != nullptr; }
 
-bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
-                   const float2* tw, cudaStream_t s, int reserve_sms) {
+bool launch_col_tc(const TcPlan& plan, int path, int H, int variant, const DevWorld* worlds, const ColItem* groups,
+                   int ngroups, const float2* tw, cudaStream_t s, int reserve_sms) {
     const void* fm = nullptr;
     for (int i = 0; i < plan.nsizes; i++)
         if (plan.sizes[i] == H) fm = plan.mats[i];
@@ -544,14 +563,23 @@ bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, 
     int* e = (int*)plan.d_err;
     switch (H) {
     case 4096: return launch_col_tc64(x3, fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true, 128>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                         : launch_shape<TcShape<64, 32, 4, false, 128>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 1024: return x3 ? launch_shape<TcShape<32, 32, 4, true, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                         : launch_shape<TcShape<32, 32, 4, false, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 512: return x3 ? launch_shape<TcShape<32, 16, 8, true, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                        : launch_shape<TcShape<32, 16, 8, false, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
-    case 256: return x3 ? launch_shape<TcShape<16, 16, 8, true, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
-                        : launch_shape<TcShape<16, 16, 8, false, 144>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 2048: return x3 ? launch_shape<TcShape<64, 32, 4, true, 128, 2, 1>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                         : launch_shape<TcShape<64, 32, 4, false, 128, 2, 1>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 1024:
+        if (x3)
+            return variant == 1 ? launch_shape<TcShape<32, 32, 4, true, 128, 1, 4, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                                : launch_shape<TcShape<32, 32, 4, true, 128, 1, 2>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+        return launch_shape<TcShape<32, 32, 4, false, 144, 1, 1>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 512:
+        if (x3)
+            return variant == 1 ? launch_shape<TcShape<32, 16, 8, true, 128, 1, 3, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                                : launch_shape<TcShape<32, 16, 8, true, 128, 1, 2>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+        return launch_shape<TcShape<32, 16, 8, false, 144, 1, 1>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+    case 256:
+        if (x3)
+            return variant == 1 ? launch_shape<TcShape<16, 16, 8, true, 128, 1, 4, false>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms)
+                                : launch_shape<TcShape<16, 16, 8, true, 128, 1, 2>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
+        return launch_shape<TcShape<16, 16, 8, false, 144, 1, 1>>(fm, worlds, groups, ngroups, tw, e, s, reserve_sms);
     }
     return false;
 }

@@ -30,9 +30,13 @@ int tc_columns_per_group(int H);
 int tc_setup(TcPlan& plan, int path, std::string* err);
 int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err);
 // groups: (world, channel, first tile) items, each covering tc_columns_per_group(H) columns.
-// reserve_sms: SMs the persistent grid leaves free for a launch that runs beside it.
-bool launch_col_tc(const TcPlan& plan, int path, int H, const DevWorld* worlds, const ColItem* groups, int ngroups,
-                   const float2* tw, cudaStream_t s, int reserve_sms = 0);
+// variant (BF16x3, columns of 256..1024): 0 stages each tile group by a bulk copy into shared memory a
+// group ahead; 1 reads it from global memory after an L2 prefetch, with 32 KB less shared memory a
+// CTA and so more CTAs an SM.  reserve_sms: SMs the persistent grid leaves free for a launch that
+// runs beside it.
+constexpr int TC_COL_VARIANTS = 2;
+bool launch_col_tc(const TcPlan& plan, int path, int H, int variant, const DevWorld* worlds, const ColItem* groups,
+                   int ngroups, const float2* tw, cudaStream_t s, int reserve_sms = 0);
 int tc_check_error(TcPlan& plan, std::string* err);
 // Test hook: limit_plus_one = 0 keeps the default poll limit of the DFT-matrix wait, n > 0 makes it
 // n - 1 polls (1: the wait gives up at once and the pass exits early with the error flag set).

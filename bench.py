@@ -489,7 +489,8 @@ def run_ours(args, dist):
     variants = {"%dx%d" % wh: {"column": v["column_variant"], "row": v["row_variant"], "chunks": v["chunks"],
                                "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
                                "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"],
-                               "resident_variant": v["resident_variant"], "tc_rows": v["tc_rows"]}
+                               "resident_variant": v["resident_variant"], "tc_rows": v["tc_rows"],
+                               "tc_column_variant": v["tc_column_variant"]}
                 for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step

@@ -177,8 +177,9 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
 
 /* Autotuner: times the candidate launch shapes of every size class on this context's worlds
  * and keeps the fastest, one dimension after another: the cluster-resident step against the two
- * launches per generation (where it applies), the tensor-core row pass against the FP32 one
- * (lenia_set_tc_rows, where it applies), then for two-pass classes the pair of column and row
+ * launches per generation (where it applies), the tensor-core column pass's variants and the
+ * tensor-core row pass against the FP32 one (lenia_set_tc_rows, where they apply), then for
+ * two-pass classes the pair of column and row
  * launch variants and every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that
  * changes the class's number of chunks; then, for the whole step, the split of small classes onto a
  * second graph branch (lenia_set_branch_split).
@@ -196,10 +197,12 @@ LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
 LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
 /* The launch shape of every size class, as the autotuner left it: *nclasses = the number of classes;
- * with `out` (count >= 11 * classes) eleven int32 per class: width, height, column variant, row
+ * with `out` (count >= 12 * classes) twelve int32 per class: width, height, column variant, row
  * variant, chunks, worlds, chunk budget in MiB (0: the class is one chunk), rows per row-pass item,
  * 1 if the class runs the cluster-resident step (lenia_set_resident) else 0, that step's launch
- * variant, and 1 if its row pass runs on the tensor cores (lenia_set_tc_rows) else 0.
+ * variant, 1 if its row pass runs on the tensor cores (lenia_set_tc_rows) else 0, and the variant of
+ * its tensor-core column pass (0: tile groups staged by bulk copies, 1: read after an L2 prefetch,
+ * more CTAs an SM; -1: no tensor-core column pass).
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
@@ -227,13 +230,19 @@ LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells, int32_t* e
  * lenia_sync.  Rebuilds the step graphs.  No reference counterpart (the reference dispatches every
  * pass of every world separately, crates/auto-core/src/sim.rs:297-380). */
 LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t mode);
-/* The tensor-core row pass on (1, the default until lenia_autotune chooses per class) or off (0) on
+/* The tensor-core row pass on (1) or off (0, the default until lenia_autotune chooses per class) on
  * the TF32 and BF16X3 paths: the inverse
  * row DFT, the growth / dt / clamp update and the forward row DFT of the one-channel, one-kernel
  * Lenia step as DFT-as-GEMM on tcgen05 (step rows of 256, 512 and 1024 cells; other classes, and
  * every class when off, take the FP32 row pass).  Rebuilds the step graphs.  No reference
  * counterpart: the reference's row transforms are radix-2 dispatches (spectral.rs:225-264). */
 LENIA_API int lenia_set_tc_rows(LeniaCtx* ctx, int32_t on);
+/* Pins the variant of every size class's tensor-core column pass (BF16X3, columns of 256..1024), in
+ * place of the default (0) or the autotuner's choice: 0 stages each tile group in shared memory by a
+ * bulk copy a group ahead; 1 reads it from global memory after an L2 prefetch, which leaves 32 KB of
+ * shared memory a CTA free for more CTAs an SM.  Results do not depend on it (bit for bit).  Rebuilds
+ * the step graphs.  No reference counterpart. */
+LENIA_API int lenia_set_tc_variant(LeniaCtx* ctx, int32_t variant);
 
 /* Host-only (no GPU): the kernel's real, even spectrum as the engine uses it, computed in FP64
  * and rounded to float32, with the inverse-FFT normalisation 1/(width*height) folded in.

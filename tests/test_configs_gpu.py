@@ -5,7 +5,8 @@ a single step (crates/auto-core/tests/automata.rs:300-362).
 
 Tolerances (per-step max-abs against FP64):
   * FP32 path: 1e-5 on the one-channel configurations, 1e-4 on the 3-channel world
-  * BF16x3 tensor-core path: 1e-4, the metric's bound
+  * BF16x3 tensor-core path (column pass, and with +tc_rows the row pass too): 1e-4, the metric's
+    bound
 Each checkpoint also reports the world's mass, so a run that has died out (a trivial comparison)
 shows as such: the 3-channel configuration does die out, at step 8 in FP64 and on the GPU alike,
 which the test asserts.
@@ -18,7 +19,7 @@ from oracle.oracle import fp64_khats, fp64_step
 
 pytestmark = pytest.mark.gpu
 
-TOL = {"fp32": 1e-5, "bf16x3": 1e-4}
+TOL = {"fp32": 1e-5, "bf16x3": 1e-4, "bf16x3+tc_rows": 1e-4}
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -43,14 +44,17 @@ def batched384():
     return worlds, [fp64_khats(w) for w in worlds]
 
 
-@pytest.mark.parametrize("path", ["fp32", "bf16x3"])
+@pytest.mark.parametrize("path", ["fp32", "bf16x3", "bf16x3+tc_rows"])
 def test_config3_all_384_worlds_at_checkpoints(batched384, path):
     """Configuration 3 whole: all 384 uneven worlds (sides 128..1024, per-world R, mu, sigma, dt) in
     one context, seeded with their 25%-area patches, checked at generations 1, 16 and 64 -- the
-    64-step graph the bench replays."""
+    64-step graph the bench replays.  bf16x3+tc_rows runs the row pass on the tensor cores too, where
+    it applies (sides 256, 512, 1024)."""
     worlds, khats = batched384
     worst, dead = 0.0, 0
-    with Sim(worlds, seed=0, path=path) as sim:
+    with Sim(worlds, seed=0, path=path.split("+")[0]) as sim:
+        if path.endswith("tc_rows"):
+            sim.set_tc_rows(True)
         for i, w in enumerate(worlds):
             sim.seed_patches(i, i, w.seed.patches)
         done = 0

@@ -175,6 +175,7 @@ def test_tc_row_pass_batched_many_steps():
     with Sim(worlds, seed=0, path="bf16x3") as sim:
         for i, w in enumerate(worlds):
             sim.seed_patches(i, i, w.seed.patches)
+        sim.set_tc_rows(True)
         assert all(v["tc_rows"] == 1 for v in sim.shapes().values())
         sim.step(63)
         before = [sim.read_state(i) for i in range(len(worlds))]
@@ -188,3 +189,28 @@ def test_tc_row_pass_batched_many_steps():
           (worst, alive, len(worlds)))
     assert worst < 1e-4, worst
     assert alive > len(worlds) // 2
+
+
+def test_tc_column_variants_bit_identical():
+    """The tensor-core column pass's two variants (tile groups staged by bulk copies, or read from L2
+    with more CTAs an SM) run the same arithmetic on the same values: bit-identical states after 8
+    steps on batched worlds of every tensor-core column length, and within 1e-4 of FP64."""
+    worlds = [w for w in configs.batched(96) if w.width in (256, 512, 1024)][:18]
+    out = []
+    for v in (0, 1):
+        with Sim(worlds, seed=0, path="bf16x3") as sim:
+            for i, w in enumerate(worlds):
+                sim.seed_patches(i, i, w.seed.patches)
+            sim.set_tc_variant(v)
+            assert all(s["tc_column_variant"] == v for s in sim.shapes().values())
+            sim.step(7)
+            before = [sim.read_state(i) for i in range(len(worlds))]
+            sim.step(1)
+            out.append(sim.read_states().copy())
+    assert np.array_equal(out[0], out[1])
+    off = 0
+    for i, w in enumerate(worlds):
+        n = w.width * w.height
+        err = float(np.abs(out[1][off:off + n].reshape(1, w.height, w.width) - fp64_step(w, before[i])).max())
+        assert err < 1e-4, (i, err)
+        off += n
