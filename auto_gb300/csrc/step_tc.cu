@@ -203,6 +203,23 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
         tc_fence_after();
         return true;
     };
+    // Units [0, U) of a hand-over, this warpgroup's share (u = wg, wg + WG, ...), two at a time: both
+    // units' TMEM columns are loaded before one wait (tmem_ld16x2), so the two loads' latencies overlap.
+    // col(u) is a unit's first TMEM column, fn(u, v) its work on the 16 values v.
+    auto units2 = [&](int U, auto col, auto fn) {
+        int u = wg;
+        for (; u + S::WG < U; u += 2 * S::WG) {
+            float va[16], vb[16];
+            tmem_ld16x2(col(u), col(u + S::WG), va, vb);
+            fn(u, va);
+            fn(u + S::WG, vb);
+        }
+        if (u < U) {
+            float v[16];
+            tmem_ld16(col(u), v);
+            fn(u, v);
+        }
+    };
     // A transposing hand-over unit: 8 complex values (interleaved re, im) v_j times w(j) = W8 * W1[j],
     // into an A operand at rows m0..m0+7 (MN-major, BF16x3) or rows m0 + j (K-major), columns k (real
     // part) and k + KH (imaginary part).
@@ -286,13 +303,13 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
         }
 
         // ---- A -> B: twiddle exp(-2 pi i y1 k2 / H), rows (c, k2), K (re/im, y1); units (block, 8 k2)
-        for (int un = wg; un < (S::MA / 128) * (S::NA / 16); un += S::WG) {
-            const int b = un / (S::NA / 16), h = un % (S::NA / 16);
-            const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
-            float v[16];
-            tmem_ld16(t_x + lane_off + (uint32_t)(b * S::NA + 16 * h), v);
-            store_t8(v, pick(A8, h), A1, c * S::H2 + 8 * h, y1, S::H1, S::MB, S::KB);
-        }
+        units2((S::MA / 128) * (S::NA / 16),
+               [&](int un) { return t_x + lane_off + (uint32_t)((un / (S::NA / 16)) * S::NA + 16 * (un % (S::NA / 16))); },
+               [&](int un, const float* v) {
+                   const int b = un / (S::NA / 16), h = un % (S::NA / 16);
+                   const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
+                   store_t8(v, pick(A8, h), A1, c * S::H2 + 8 * h, y1, S::H1, S::MB, S::KB);
+               });
         tc_fence_before();
         fence_async_smem();
         __syncthreads();
@@ -312,12 +329,12 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
             kh_pending = false;
             ph_kh ^= 1;
             // ---- B -> C: x khat (real, even), conjugate; rows (c, k2), K (re/im, k1); units (block, 8 k1)
-            for (int un = wg; un < (S::MB / 128) * (S::NB / 16); un += S::WG) {
+            units2((S::MB / 128) * (S::NB / 16),
+                   [&](int un) { return t_b + lane_off + (uint32_t)((un / (S::NB / 16)) * S::NB + 16 * (un % (S::NB / 16))); },
+                   [&](int un, const float* v) {
                 const int b = un / (S::NB / 16), h = un % (S::NB / 16);
                 const int r = b * 128 + lt, c = r / S::H2, k2 = r % S::H2;
                 const float* khrow = khs + c * S::HQ;
-                float v[16];
-                tmem_ld16(t_b + lane_off + (uint32_t)(b * S::NB + 16 * h), v);
                 float re[8], im[8];
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
@@ -331,7 +348,7 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
                     store_chunk<S::X3, S::LBO>(op, S::OPND, r, 8 * h + j, S::KB, re + j);
                     store_chunk<S::X3, S::LBO>(op, S::OPND, r, S::H1 + 8 * h + j, S::KB, im + j);
                 }
-            }
+            });
             tc_fence_before();
             fence_async_smem();
             __syncthreads();
@@ -350,13 +367,13 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
                 break;
             }
             // ---- C -> D: twiddle exp(-2 pi i k2 y1 / H); rows (c, y1), K (re/im, k2); units (block, 8 y1)
-            for (int un = wg; un < (S::MB / 128) * (S::NB / 16); un += S::WG) {
-                const int b = un / (S::NB / 16), h = un % (S::NB / 16);
-                const int r = b * 128 + lt, c = r / S::H2, k2 = r % S::H2;
-                float v[16];
-                tmem_ld16(t_x + lane_off + (uint32_t)(b * S::NB + 16 * h), v);
-                store_t8(v, pick(C8, h), C1, c * S::H1 + 8 * h, k2, S::H2, S::MA, S::KA);
-            }
+            units2((S::MB / 128) * (S::NB / 16),
+                   [&](int un) { return t_x + lane_off + (uint32_t)((un / (S::NB / 16)) * S::NB + 16 * (un % (S::NB / 16))); },
+                   [&](int un, const float* v) {
+                       const int b = un / (S::NB / 16), h = un % (S::NB / 16);
+                       const int r = b * 128 + lt, c = r / S::H2, k2 = r % S::H2;
+                       store_t8(v, pick(C8, h), C1, c * S::H1 + 8 * h, k2, S::H2, S::MA, S::KA);
+                   });
             tc_fence_before();
             fence_async_smem();
             __syncthreads();
@@ -367,16 +384,16 @@ __global__ void __launch_bounds__(S::NT, S::MINB)
             }
             // ---- output: conjugate, natural order y = y1 + H1*y2, into the operand area; units (block, 8 y2)
             float2* out = reinterpret_cast<float2*>(op);
-            for (int un = wg; un < (S::MA / 128) * (S::NA / 16); un += S::WG) {
-                const int b = un / (S::NA / 16), h = un % (S::NA / 16);
-                const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
-                float2* col = out + (size_t)(c / TC) * S::H * TC + (c % TC);
-                float v[16];
-                tmem_ld16(t_x + lane_off + (uint32_t)(b * S::NA + 16 * h), v);
+            units2((S::MA / 128) * (S::NA / 16),
+                   [&](int un) { return t_x + lane_off + (uint32_t)((un / (S::NA / 16)) * S::NA + 16 * (un % (S::NA / 16))); },
+                   [&](int un, const float* v) {
+                       const int b = un / (S::NA / 16), h = un % (S::NA / 16);
+                       const int r = b * 128 + lt, c = r / S::H1, y1 = r % S::H1;
+                       float2* col = out + (size_t)(c / TC) * S::H * TC + (c % TC);
 #pragma unroll
-                for (int j = 0; j < 8; j++)
-                    col[(size_t)(y1 + S::H1 * (8 * h + j)) * TC] = make_float2(v[2 * j], -v[2 * j + 1]);
-            }
+                       for (int j = 0; j < 8; j++)
+                           col[(size_t)(y1 + S::H1 * (8 * h + j)) * TC] = make_float2(v[2 * j], -v[2 * j + 1]);
+                   });
             tc_fence_before();
             fence_async_smem();
             __syncthreads();

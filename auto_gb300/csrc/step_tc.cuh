@@ -30,7 +30,7 @@ int tc_columns_per_group(int H);
 int tc_setup(TcPlan& plan, int path, std::string* err);
 int tc_prepare_size(TcPlan& plan, int path, int H, std::string* err);
 // groups: (world, channel, first tile) items, each covering tc_columns_per_group(H) columns.
-// variant (BF16x3, columns of 256..1024): 0 stages each tile group by a bulk copy into shared memory a
+// variant (BF16x3, columns of 256..1024; other shapes ignore it): 0 stages each tile group by a bulk copy into shared memory a
 // group ahead; 1 reads it from global memory after an L2 prefetch, with 32 KB less shared memory a
 // CTA and so more CTAs an SM.  reserve_sms: SMs the persistent grid leaves free for a launch that
 // runs beside it.

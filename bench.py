@@ -66,6 +66,9 @@ def parse(argv=None):
     p.add_argument("--gens", type=int, default=64, help="generations per bench step")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--tc-rows", action="store_true",
+                   help="tensor-core paths: run the row pass on the tensor cores too where it applies (after "
+                        "autotuning, which otherwise keeps the faster row pass per class)")
     p.add_argument("--no-autotune", action="store_true",
                    help="keep the default launch variants instead of timing both per size class")
     p.add_argument("--jsonl", default=None, help="also append a sample in the reference's results/*.jsonl format")
@@ -456,6 +459,8 @@ def profile_window(args, dist):
     seed_all(sim, worlds, seeds)
     if not args.no_autotune:
         sim.autotune()
+    if args.tc_rows:
+        sim.set_tc_rows(True)
     for _ in range(args.warmup):
         sim.step(args.gens)
     sim.wait()
@@ -483,6 +488,8 @@ def run_ours(args, dist):
     seed_all(sim, worlds, seeds)
     if not args.no_autotune:
         sim.autotune()  # the engine's autotuner: times every launch variant per size class
+    if args.tc_rows:
+        sim.set_tc_rows(True)
     # launch shape per size class after autotuning: variants (column: 0/1 scalar at 64/128 registers,
     # 2 paired; row: 0/1), chunks of worlds run back to back through L2, rows per row item, the
     # cluster-resident step, and whether the row pass runs on the tensor cores
@@ -676,7 +683,8 @@ def run_ours(args, dist):
         cpu = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
 
     if dist.rank == 0:
-        cfg.update({"path": args.path, "gens_per_step": G, "cells_per_generation": cells, "worlds": len(worlds),
+        cfg.update({"path": args.path + ("+tc_rows" if args.tc_rows and args.path in ("bf16x3", "tf32") else ""),
+                    "gens_per_step": G, "cells_per_generation": cells, "worlds": len(worlds),
                     "l2": "no flush: per-generation working set (state + half-spectrum + kernel spectrum) "
                           "exceeds the 129 MB L2" if cells >= 4096 * 4096 else "no flush",
                     "parallelism": ("replicas" if scaling == "weak" else "worlds sharded") if dist.world > 1

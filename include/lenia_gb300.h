@@ -238,7 +238,7 @@ LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t mode);
  * counterpart: the reference's row transforms are radix-2 dispatches (spectral.rs:225-264). */
 LENIA_API int lenia_set_tc_rows(LeniaCtx* ctx, int32_t on);
 /* Pins the variant of every size class's tensor-core column pass (BF16X3, columns of 256..1024), in
- * place of the default (0) or the autotuner's choice: 0 stages each tile group in shared memory by a
+ * place of the default (1) or the autotuner's choice: 0 stages each tile group in shared memory by a
  * bulk copy a group ahead; 1 reads it from global memory after an L2 prefetch, which leaves 32 KB of
  * shared memory a CTA free for more CTAs an SM.  Results do not depend on it (bit for bit).  Rebuilds
  * the step graphs.  No reference counterpart. */
