@@ -63,6 +63,12 @@ struct SizeClass {
     // TF32 / BF16X3 paths whose row length it serves; `tc_rows` selects it over the FP32 row pass.
     // Its groups are tc_row_stride consecutive FP32 row items.
     int tc_rows_ok = 0, tc_rows = 0, tc_row_stride = 1;
+    // persistent step (persist.cu): possible for square one-channel, one-kernel Lenia classes on the
+    // FP32 path; `persist` selects one launch per class and step call over the two launches per
+    // generation.  d_pctl: its control words.
+    int persist_ok = 0, persist = 0;
+    int var_per = 0;  // its launch variant (persist.cu)
+    int* d_pctl = nullptr;
 };
 
 // Default chunk budget: 0, every class is one chunk.  Chunks of up to 32 MiB do keep their worlds in
@@ -71,6 +77,12 @@ struct SizeClass {
 // less: every budget measured slower (1024 x 1024: 1.91e11 cell-updates/s as one chunk, 1.75e11 in 8
 // chunks, 1.50e11 in 16).  The autotuner still tries budgets per class.
 constexpr size_t DEFAULT_CHUNK_BUDGET = 0;
+// Whether a class the persistent step serves starts with it (the autotuner times it against the two
+// launches per generation and keeps the faster).  Off: on the batched workload every class measured
+// slower persistent (1024 x 1024: 1.73e11 cell-updates/s against 1.92e11; 128 x 128: 3.5e10 against
+// 8.8e10; one 4096 x 4096 world: 1.31e11 against 1.54e11), the two-pass kernels' own register budgets
+// and builds mattering more than the launches and HBM round trips it saves.
+constexpr int PERSIST_DEFAULT = 0;
 // Whether a class the tensor-core row pass serves starts with it.  Off: measured slower than the FP32
 // row pass at every size it serves (1024 x 1024: 354 us a generation for the class of 55 worlds
 // against 188 us), and its BF16x3 inverse feeds U's rounding error straight into the growth (about
@@ -428,6 +440,14 @@ Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, cl.va
 // `steps` steps of one size class, chunk after chunk, in the given launch shape; a resident class is
 // one launch for all its worlds and steps.
 int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, cudaStream_t s) {
+    if (cl.persist) {
+        const int nw = (int)cl.worlds.size();
+        CK(cudaMemsetAsync(cl.d_pctl, 0, persist_ctl_words(nw) * sizeof(int), s));
+        if (!launch_persist(cl.W, cl.var_per, ctx->d_worlds, cl.d_col, cl.d_row, nw, cl.ncol / nw, cl.nrow / nw, steps,
+                            ctx->d_tw, cl.d_pctl, ctx->d_flags, s))
+            return fail(ctx, LENIA_ECUDA, "persistent launch failed (%dx%d)", cl.W, cl.H);
+        return 0;
+    }
     if (cl.resident) {
         if (!launch_resident(cl.W, cl.var_res, ctx->d_worlds, cl.d_world_ids, (int)cl.worlds.size(), steps, ctx->d_tw,
                              ctx->d_flags, s))
@@ -784,6 +804,25 @@ int setup_fused(LeniaCtx* ctx) {
                 cl.var_res = 0;
             }
         }
+        // the persistent step: square one-channel, one-kernel Lenia worlds on the FP32 path, every world of
+        // the class with the same number of column and row items
+        if (ctx->path == LENIA_PATH_FP32 && !general && cl.W == cl.H && persist_supported(cl.W)) {
+            const int nw = (int)cl.worlds.size();
+            bool even = cl.ncol % nw == 0 && cl.nrow % nw == 0;
+            for (int wi : cl.worlds) even = even && ctx->wb[wi].ncol == cl.ncol / nw && ctx->wb[wi].nrow == cl.nrow / nw;
+            int cap0 = 0, cap1 = 0;
+            if (even &&
+                launch_persist(cl.W, 0, ctx->d_worlds, cl.d_col, cl.d_row, 0, 0, 0, 0, ctx->d_tw, nullptr, nullptr,
+                               ctx->stream, &cap0) &&
+                launch_persist(cl.W, 1, ctx->d_worlds, cl.d_col, cl.d_row, 0, 0, 0, 0, ctx->d_tw, nullptr, nullptr,
+                               ctx->stream, &cap1) &&
+                cap0 > 0 && cap1 > 0) {
+                if ((rc = dalloc(ctx, &cl.d_pctl, (size_t)persist_ctl_words(nw)))) return rc;
+                cl.persist_ok = 1;
+                cl.persist = PERSIST_DEFAULT;
+            }
+            cudaGetLastError();
+        }
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
         for (int v = 0; v < 2; v++) {
             if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
@@ -863,7 +902,7 @@ struct EventList {
     }
 };
 int time_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps, double* col_ms, double* row_ms) {
-    if (cl.resident) {
+    if (cl.resident || cl.persist) {
         // one launch: its whole time is reported as the column share
         Events ev;
         CK(cudaEventCreate(&ev.e[0]));
@@ -966,7 +1005,8 @@ int check_device_errors(LeniaCtx* ctx) {
     CK(cudaMemcpy(&h, ctx->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
     if (h) {
         CK(cudaMemset(ctx->d_flags, 0, sizeof(int)));
-        return fail(ctx, LENIA_ECUDA, "a cluster-resident step gave up waiting on a cluster sync; results of that step are invalid");
+        return fail(ctx, LENIA_ECUDA,
+                    "a cluster-resident or persistent step gave up waiting on another CTA; results of that step are invalid");
     }
     return 0;
 }
@@ -1561,7 +1601,26 @@ int lenia_set_resident(LeniaCtx* ctx, int32_t mode) {
     for (auto& cl : ctx->classes) {
         const int v = mode >= 2 ? mode - 2 : cl.var_res;
         cl.resident = mode != 0 && cl.resident_ok && cl.res_fits[v] > 0;
-        if (cl.resident) cl.var_res = v;
+        if (cl.resident) cl.var_res = v, cl.persist = 0;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_set_persistent(LeniaCtx* ctx, int32_t mode) {
+    if (!ctx) return LENIA_EINVAL;
+    if (mode < 0 || mode > 1 + PERSIST_VARIANTS)
+        return fail(ctx, LENIA_EINVAL, "mode must be 0 (off), 1 (on) or 2..%d (on, launch variant mode - 2)",
+                    1 + PERSIST_VARIANTS);
+    for (auto& cl : ctx->classes) {
+        cl.persist = mode != 0 && cl.persist_ok;
+        if (cl.persist) {
+            cl.resident = 0;
+            if (mode >= 2) cl.var_per = mode - 2;
+        }
     }
     CK(cudaStreamSynchronize(ctx->stream));
     int rc = rebuild_graphs(ctx);
@@ -1617,10 +1676,10 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (count < 12 * ctx->classes.size()) return LENIA_EINVAL;
+    if (count < 13 * ctx->classes.size()) return LENIA_EINVAL;
     for (size_t i = 0; i < ctx->classes.size(); i++) {
         const auto& cl = ctx->classes[i];
-        int32_t* o = out + 12 * i;
+        int32_t* o = out + 13 * i;
         o[0] = cl.W;
         o[1] = cl.H;
         o[2] = cl.var_col;
@@ -1633,6 +1692,7 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
         o[9] = cl.var_res;
         o[10] = cl.tc_rows;
         o[11] = cl.ntcg > 0 ? cl.var_tc : -1;
+        o[12] = cl.persist ? cl.var_per : -1;
     }
     return 0;
 }
@@ -1655,7 +1715,8 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
 }
 
 // The autotuner's search, on states it may advance.  For every size class, in turn: the cluster-
-// resident step against two launches a generation (FP32 path, where it applies), the tensor-core row
+// resident and persistent steps against two launches a generation (FP32 path, where they apply), the
+// tensor-core row
 // pass against the FP32 one (TF32 / BF16X3 paths, where it applies), every pair of column and row
 // launch variants, then every chunk budget that gives a different number of chunks.
 // Each candidate is timed as a captured graph of a few steps (time_class_graph), and a class keeps
@@ -1680,31 +1741,43 @@ static int autotune_search(LeniaCtx* ctx) {
             return 0;
         };
         int bi = 0, rc = 0;
-        if (cl.resident_ok) {
-            // every variant of the cluster-resident step that fits, against the two-pass step in its
-            // current shape; candidate 0 is the current choice
-            const int was_res = cl.resident, was_var = cl.var_res;
-            std::vector<std::pair<int, int>> cands{{was_res, was_var}};  // (resident, variant)
-            if (was_res) cands.push_back({0, was_var});
-            for (int v = 0; v < RESIDENT_VARIANTS; v++)
-                if (cl.res_fits[v] > 0 && !(was_res && v == was_var)) cands.push_back({1, v});
+        if (cl.resident_ok || cl.persist_ok) {
+            // one launch per class and step call -- every variant of the cluster-resident step that fits,
+            // and the persistent step -- against the two-pass step in its current shape; candidate 0 is
+            // the current choice
+            struct Cand {
+                int res, var, per, pvar;
+            };
+            const Cand was{cl.resident, cl.var_res, cl.persist, cl.var_per};
+            std::vector<Cand> cands{was};
+            if (was.res || was.per) cands.push_back({0, was.var, 0, was.pvar});
+            for (int v = 0; v < RESIDENT_VARIANTS && cl.resident_ok; v++)
+                if (cl.res_fits[v] > 0 && !(was.res && v == was.var)) cands.push_back({1, v, 0, was.pvar});
+            for (int v = 0; v < PERSIST_VARIANTS && cl.persist_ok; v++)
+                if (!(was.per && v == was.pvar)) cands.push_back({0, was.var, 1, v});
             std::vector<double> t(cands.size());
             for (size_t i = 0; i < cands.size() && !rc; i++) {
-                cl.resident = cands[i].first;
-                cl.var_res = cands[i].second;
+                cl.resident = cands[i].res;
+                cl.var_res = cands[i].var;
+                cl.persist = cands[i].per;
+                cl.var_per = cands[i].pvar;
                 rc = timed(shape_of(cl), &t[i]);
             }
-            cl.resident = was_res;
-            cl.var_res = was_var;
+            cl.resident = was.res;
+            cl.var_res = was.var;
+            cl.persist = was.per;
+            cl.var_per = was.pvar;
             if (rc) return rc;
             size_t b = 0;
             for (size_t i = 1; i < cands.size(); i++)
                 if (t[i] < t[b]) b = i;
             if (t[b] < 0.97 * t[0]) {
-                cl.resident = cands[b].first;
-                cl.var_res = cands[b].second;
+                cl.resident = cands[b].res;
+                cl.var_res = cands[b].var;
+                cl.persist = cands[b].per;
+                cl.var_per = cands[b].pvar;
             }
-            if (cl.resident) continue;  // launch variants and chunks do not apply to it
+            if (cl.resident || cl.persist) continue;  // launch variants and chunks do not apply to them
         }
         if (cl.ntcg > 0) {
             // the tensor-core column pass's variants (staged tile groups, or L2-prefetched loads with more

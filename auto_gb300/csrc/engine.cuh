@@ -79,6 +79,20 @@ int resident_clusters_that_fit(int N, int variant);
 bool launch_resident(int N, int variant, const DevWorld* worlds, const int* world_ids, int nworlds, int gens,
                      const float2* tw, int* err, cudaStream_t s);
 
+// Persistent step (persist.cu): one launch advances every world of a square, one-channel, one-kernel
+// Lenia size class of side N through `gens` generations, with the two-pass step's column and row
+// items (cols: nc a world, rows: nr a world, world after world) claimed in order by a grid of
+// resident CTAs.  ctl: persist_ctl_words(nworlds) ints, zeroed before every launch.  err: a device
+// int set to 1 if a wait gave up.  capacity (optional): CTAs the GPU holds at once.  A zero-world
+// call only configures the kernel (outside any stream capture).
+// variant: 0 at most 64 registers a thread, 1 at most 128 (as the two-pass step's launch variants).
+constexpr int PERSIST_VARIANTS = 2;
+bool persist_supported(int N);
+int persist_ctl_words(int nworlds);
+bool launch_persist(int N, int variant, const DevWorld* worlds, const ColItem* cols, const RowItem* rows, int nworlds,
+                    int ncol, int nrow, int gens, const float2* tw, int* ctl, int* err, cudaStream_t s,
+                    int* capacity = nullptr);
+
 // Seeding and statistics (seed.cu).
 void launch_seed_patches(float* state, int W, int H, uint32_t seed, const int4* patches, int npatch,
                          cudaStream_t s);

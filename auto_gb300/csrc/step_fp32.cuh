@@ -238,7 +238,7 @@ __device__ __forceinline__ float* row_extra_smem(float2* stw) {
 // One element per lane and column, consecutive lanes on consecutive columns: the shared-memory
 // writes of a warp are contiguous (a tile per lane, with both its columns, would write at
 // stride 2 and conflict; measured 4% slower at 4096 x 4096).
-template <int W, int S, int NT>
+template <int W, int S, int NT, bool CG = false>
 __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __restrict__ sp, int H, int r0) {
     constexpr int SEQ = seq_stride(W);
     constexpr int E = W / 2 * S, IT = (E + NT - 1) / NT;
@@ -250,8 +250,8 @@ __device__ __forceinline__ void load_rows_spectrum(float2* Z, const float2* __re
             const int t = e / (S * TC), p = (e / TC) % S, c = e % TC;
             const float2* src = sp + ((size_t)t * H + r0 + 2 * p) * TC + c;
             const uint64_t keep = hint::policy_keep();
-            A[i] = hint::ld2(src, keep);
-            B[i] = hint::ld2(src + TC, keep);
+            A[i] = hint::ld2c<CG>(src, keep);
+            B[i] = hint::ld2c<CG>(src + TC, keep);
         }
     }
     // When every iteration moves kx by the same multiple of 16 (D), the padded positions of kx and
@@ -364,6 +364,52 @@ __device__ __noinline__ void row_item_u(float2* Z, const float2* stw, const DevW
     }
 }
 
+// The one-channel, one-kernel Lenia row step of rows r0..r0+3 of world wd: inverse row FFT of U, growth,
+// dt update and clamp against the state, forward row FFT of the new rows.  Z: the two packed
+// sequences, stw: the stage tables.  CG: spectrum and state loads bypass L1 (the persistent step,
+// where another CTA of the same launch wrote them).
+template <int W, int NT, bool CG>
+__device__ __forceinline__ void row_item_simple(const DevWorld& wd, int r0, float2* Z, const float2* stw) {
+    constexpr int S = row_seqs(W, false), ROWS = 2 * S;
+    const int H = wd.H;
+    const DevKernel kp = wd.kern[0];
+    const float dtw = wd.dt * kp.weight;
+    const Growth growth(kp.mu, kp.sigma);
+    float* st = wd.state + (size_t)r0 * W;
+    const uint64_t stream = hint::policy_stream();
+    // The growth update runs in registers between the inverse and the forward row FFT (every
+    // built width has a plan with equal first and last radix).  The item's state rows are
+    // pulled into L2 when the CTA starts, and each thread's 2 x R state values are loaded into
+    // registers just before the last inverse stage.
+    static_assert(fusable<W>(), "row widths need a plan with equal first and last radix");
+    constexpr int R = plan_radix(W, 0), NB = W / R;
+    static_assert(S * NB <= NT, "one butterfly per thread in the fused stage");
+    if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, ROWS * W * (uint32_t)sizeof(float));
+    load_rows_spectrum<W, S, NT, CG>(Z, wd.conv, H, r0);
+    __syncthreads();
+    float sa[R], sb[R];
+    fft_fused<W, S, NT, true, false>(
+        Z, stw,
+        [&](int s, int j, float2* v) {
+            float* ga = st + (2 * s) * W + j;
+            static_for<0, R>([&](auto m) {
+                const float n0 = __saturatef(fmaf(dtw, growth(v[m].x), sa[m]));
+                const float n1 = __saturatef(fmaf(dtw, growth(v[m].y), sb[m]));
+                hint::st1_at<decltype(m)::value * NB * 4>(ga, n0, stream);
+                hint::st1_at<(W + decltype(m)::value * NB) * 4>(ga, n1, stream);
+                v[m] = make_float2(n0, n1);
+            });
+        },
+        [&](int s, int j) {
+            const float* ga = st + (2 * s) * W + j;
+            static_for<0, R>([&](auto m) {
+                sa[m] = hint::ld1_atc<decltype(m)::value * NB * 4, CG>(ga, stream);
+                sb[m] = hint::ld1_atc<(W + decltype(m)::value * NB) * 4, CG>(ga, stream);
+            });
+        });
+    store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
+}
+
 // GEN: the instantiation for size classes with worlds that need the general step (several
 // channels or kernels, SmoothLife, MNCA).  Without it the kernel carries only the one-channel,
 // one-kernel Lenia step (and the forward and U modes), so the general path's register pressure
@@ -396,46 +442,8 @@ __global__ void __launch_bounds__(NT, MINB) row_pass(const DevWorld* __restrict_
     }
 
     if constexpr (!GEN) {
-        // One channel, one kernel, Lenia growth (every world of a class that launches this build).
-        const DevKernel kp = wd.kern[0];
-        const float dtw = wd.dt * kp.weight;
-        const Growth growth(kp.mu, kp.sigma);
-        float* st = wd.state + (size_t)r0 * W;
-        const uint64_t stream = hint::policy_stream();
-        {
-            // The growth update runs in registers between the inverse and the forward row FFT (every
-            // built width has a plan with equal first and last radix).  The item's state rows are
-            // pulled into L2 when the CTA starts, and each thread's 2 x R state values are loaded into
-            // registers just before the last inverse stage.
-            static_assert(fusable<W>(), "row widths need a plan with equal first and last radix");
-            constexpr int R = plan_radix(W, 0), NB = W / R;
-            static_assert(S * NB <= NT, "one butterfly per thread in the fused stage");
-            if (threadIdx.x == 0) tc::bulk_prefetch_l2(st, ROWS * W * (uint32_t)sizeof(float));
-            load_rows_spectrum<W, S, NT>(Z, wd.conv, H, r0);
-            __syncthreads();
-            float sa[R], sb[R];
-            fft_fused<W, S, NT, true, false>(
-                Z, stw,
-                [&](int s, int j, float2* v) {
-                    float* ga = st + (2 * s) * W + j;
-                    static_for<0, R>([&](auto m) {
-                        const float n0 = __saturatef(fmaf(dtw, growth(v[m].x), sa[m]));
-                        const float n1 = __saturatef(fmaf(dtw, growth(v[m].y), sb[m]));
-                        hint::st1_at<decltype(m)::value * NB * 4>(ga, n0, stream);
-                        hint::st1_at<(W + decltype(m)::value * NB) * 4>(ga, n1, stream);
-                        v[m] = make_float2(n0, n1);
-                    });
-                },
-                [&](int s, int j) {
-                    const float* ga = st + (2 * s) * W + j;
-                    static_for<0, R>([&](auto m) {
-                        sa[m] = hint::ld1_at<decltype(m)::value * NB * 4>(ga, stream);
-                        sb[m] = hint::ld1_at<(W + decltype(m)::value * NB) * 4>(ga, stream);
-                    });
-                });
-            store_rows_spectrum<W, S, NT>(Z, wd.spec, H, r0);
-            return;
-        }
+        row_item_simple<W, NT, false>(wd, r0, Z, stw);
+        return;
     }
 
     // General: several channels and/or kernels, or SmoothLife / MNCA (one channel, two kernels); also
@@ -564,7 +572,7 @@ __device__ __forceinline__ void multiply_khat(const float2* X, float2* T, const 
 }
 
 // One tile (H rows x TC columns, contiguous) <-> TC sequences in shared memory.
-template <int H, int NT>
+template <int H, int NT, bool CG = false>
 __device__ __forceinline__ void load_tile(float2* X, const float2* __restrict__ src) {
     static_assert(TC == 2, "tile loads move one float4 (two columns) per row");
     constexpr int SEQ = seq_stride(H);
@@ -574,7 +582,7 @@ __device__ __forceinline__ void load_tile(float2* X, const float2* __restrict__ 
 #pragma unroll
     for (int i = 0; i < IT; i++) {
         const int y = threadIdx.x + i * NT;
-        if (IT * NT == H || y < H) v[i] = hint::ld4(s4 + y, hint::policy_keep());
+        if (IT * NT == H || y < H) v[i] = hint::ld4c<CG>(s4 + y, hint::policy_keep());
     }
     // pad(tid + i NT) = pad(tid) + i (NT + NT / 16) when NT is a multiple of 16
     float2* x0 = X + pad(threadIdx.x);
@@ -604,10 +612,10 @@ __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__
 // Unchained column item: tile 0 (its column 0 packs the DC and Nyquist columns, paired ky with
 // H - ky in the khat multiply) or a khat array that is not 16-byte aligned.  Not inlined: one item
 // in W/4 takes this path, and as a separate function its registers do not add to the chained path's.
-template <int H, int NT>
+template <int H, int NT, bool CG = false>
 __device__ __noinline__ void col_item_unchained(float2* X, const float2* stw, const float2* src, float2* dst,
                                                 const float* kh, int HQ, int W, int t) {
-    load_tile<H, NT>(X, src);
+    load_tile<H, NT, CG>(X, src);
     __syncthreads();
     fft_seqs<H, TC, NT, false>(X, stw);
     multiply_khat<H, NT>(X, X, kh, HQ, W, t);
@@ -620,16 +628,9 @@ __device__ __noinline__ void col_item_unchained(float2* X, const float2* stw, co
 // `kernel` (which reads that channel).  A channel read by several kernels has one item per kernel, each
 // repeating the channel's forward column transform: that keeps every item on the chained path and
 // multiplies the items, which the multichannel world needs more than it needs the saved transforms.
-template <int H, int NT, int MINB>
-__global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
-                                                const float2* __restrict__ tw) {
-    extern __shared__ float4 smem_raw[];
-    constexpr int SEQ = seq_stride(H);
-    float2* X = reinterpret_cast<float2*>(smem_raw);
-    float2* stw = X + TC * SEQ;
-    fill_stage_twiddles<H>(stw, tw, threadIdx.x, NT);
-    const ColItem it = items[blockIdx.x];
-    const DevWorld& wd = worlds[it.world];
+// CG: the tile loads bypass L1 (the persistent step, where another CTA of the same launch wrote them).
+template <int H, int NT, bool CG>
+__device__ __forceinline__ void col_item(const DevWorld& wd, const ColItem it, float2* X, float2* stw) {
     const int W = wd.W, c = it.chan, t = it.tile, k = it.kernel, HQ = wd.HQ;
     const size_t cplane = (size_t)(W / 2) * H;
     const float2* src = wd.spec + c * cplane + (size_t)t * H * TC;
@@ -641,7 +642,7 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
     if (fusable<H>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
         float* ksm = col_khat_smem<H>(stw);
         for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
-        load_tile<H, NT>(X, src);
+        load_tile<H, NT, CG>(X, src);
         cp_async_wait_all();
         __syncthreads();
         fft_fused<H, TC, NT, false, true>(X, stw, [&](int s, int j, float2* v) {
@@ -656,8 +657,20 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
         store_tile<H, NT>(X, wd.conv + k * cplane + (size_t)t * H * TC);
         return;
     }
-    col_item_unchained<H, NT>(X, stw, src, wd.conv + k * cplane + (size_t)t * H * TC,
-                              wd.khat + (size_t)k * (W / 2 + 1) * HQ, HQ, W, t);
+    col_item_unchained<H, NT, CG>(X, stw, src, wd.conv + k * cplane + (size_t)t * H * TC,
+                                  wd.khat + (size_t)k * (W / 2 + 1) * HQ, HQ, W, t);
+}
+
+template <int H, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
+                                                const float2* __restrict__ tw) {
+    extern __shared__ float4 smem_raw[];
+    constexpr int SEQ = seq_stride(H);
+    float2* X = reinterpret_cast<float2*>(smem_raw);
+    float2* stw = X + TC * SEQ;
+    fill_stage_twiddles<H>(stw, tw, threadIdx.x, NT);
+    const ColItem it = items[blockIdx.x];
+    col_item<H, NT, false>(worlds[it.world], it, X, stw);
 }
 
 // ------------------------------------------------------------------ paired column pass

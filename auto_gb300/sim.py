@@ -201,15 +201,15 @@ class Sim:
     def shapes(self):
         """{(width, height): {...}} for every size class: launch variants, chunks (L2-resident runs of
         worlds), worlds, chunk budget (MiB, 0 = one chunk), rows per row-pass item and whether the class runs
-        the cluster-resident step, whether its row pass runs on the tensor cores, and its tensor-core
-        column pass variant (-1: none)."""
+        the cluster-resident step, whether its row pass runs on the tensor cores, its tensor-core column
+        pass variant (-1: none), and its persistent step's launch variant (-1: it does not run it)."""
         n = ctypes.c_size_t(0)
         self._check(self._L.lenia_class_shapes(self._ctx, None, 0, ctypes.byref(n)))
-        out = (ctypes.c_int32 * (12 * n.value))()
-        self._check(self._L.lenia_class_shapes(self._ctx, out, 12 * n.value, ctypes.byref(n)))
+        out = (ctypes.c_int32 * (13 * n.value))()
+        self._check(self._L.lenia_class_shapes(self._ctx, out, 13 * n.value, ctypes.byref(n)))
         keys = ("column_variant", "row_variant", "chunks", "worlds", "chunk_budget_mib", "rows_per_row_item",
-                "resident", "resident_variant", "tc_rows", "tc_column_variant")
-        return {(out[12 * i], out[12 * i + 1]): dict(zip(keys, out[12 * i + 2:12 * i + 12])) for i in range(n.value)}
+                "resident", "resident_variant", "tc_rows", "tc_column_variant", "persistent")
+        return {(out[13 * i], out[13 * i + 1]): dict(zip(keys, out[13 * i + 2:13 * i + 13])) for i in range(n.value)}
 
     def set_resident(self, on: bool, variant: int = -1):
         """Cluster-resident step on or off where it applies, optionally in launch variant `variant`
@@ -219,6 +219,11 @@ class Sim:
     def set_tc_rows(self, on: bool):
         """Tensor-core row pass on or off on the TF32 / BF16X3 paths (see lenia_set_tc_rows)."""
         self._check(self._L.lenia_set_tc_rows(self._ctx, 1 if on else 0))
+
+    def set_persistent(self, on: bool, variant: int = -1):
+        """Persistent step on or off where it applies, optionally in launch variant `variant` (see
+        lenia_set_persistent)."""
+        self._check(self._L.lenia_set_persistent(self._ctx, (2 + variant if variant >= 0 else 1) if on else 0))
 
     def set_tc_variant(self, variant: int):
         """Tensor-core column pass variant of every class (see lenia_set_tc_variant)."""

@@ -497,7 +497,7 @@ def run_ours(args, dist):
                                "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
                                "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"],
                                "resident_variant": v["resident_variant"], "tc_rows": v["tc_rows"],
-                               "tc_column_variant": v["tc_column_variant"]}
+                               "tc_column_variant": v["tc_column_variant"], "persistent": v["persistent"]}
                 for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step
@@ -542,9 +542,9 @@ def run_ours(args, dist):
     shapes = sim.shapes()
     launches_per_gen = sum(3 if args.path in ("tf32", "bf16x3") and h in tc_sizes else 2
                            for (wd, h) in {(w.width, w.height) for w in worlds}
-                           if not shapes.get((wd, h), {}).get("resident"))
-    # a cluster-resident class is one launch per bench step (all G generations)
-    launches_per_step_resident = sum(1 for v in shapes.values() if v.get("resident"))
+                           if not shapes.get((wd, h), {}).get("resident") and shapes.get((wd, h), {}).get("persistent", -1) < 0)
+    # a cluster-resident or persistent class is one launch per bench step (all G generations)
+    launches_per_step_resident = sum(1 for v in shapes.values() if v.get("resident") or v.get("persistent", -1) >= 0)
     if args.path == "radix2":
         n = worlds[0].width
         lg = int(np.log2(n))

@@ -177,7 +177,8 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
 
 /* Autotuner: times the candidate launch shapes of every size class on this context's worlds
  * and keeps the fastest, one dimension after another: the cluster-resident step against the two
- * launches per generation (where it applies), the tensor-core column pass's variants and the
+ * launches per generation and the persistent step (where they apply), the tensor-core column
+ * pass's variants and the
  * tensor-core row pass against the FP32 one (lenia_set_tc_rows, where they apply), then for
  * two-pass classes the pair of column and row
  * launch variants and every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that
@@ -197,12 +198,13 @@ LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
 LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
 /* The launch shape of every size class, as the autotuner left it: *nclasses = the number of classes;
- * with `out` (count >= 12 * classes) twelve int32 per class: width, height, column variant, row
+ * with `out` (count >= 13 * classes) thirteen int32 per class: width, height, column variant, row
  * variant, chunks, worlds, chunk budget in MiB (0: the class is one chunk), rows per row-pass item,
  * 1 if the class runs the cluster-resident step (lenia_set_resident) else 0, that step's launch
- * variant, 1 if its row pass runs on the tensor cores (lenia_set_tc_rows) else 0, and the variant of
+ * variant, 1 if its row pass runs on the tensor cores (lenia_set_tc_rows) else 0, the variant of
  * its tensor-core column pass (0: tile groups staged by bulk copies, 1: read after an L2 prefetch,
- * more CTAs an SM; -1: no tensor-core column pass).
+ * more CTAs an SM; -1: no tensor-core column pass), and the launch variant of its persistent step
+ * (lenia_set_persistent; -1: the class does not run it).
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
@@ -230,6 +232,18 @@ LENIA_API int lenia_branch_split(const LeniaCtx* ctx, int64_t* cells, int32_t* e
  * lenia_sync.  Rebuilds the step graphs.  No reference counterpart (the reference dispatches every
  * pass of every world separately, crates/auto-core/src/sim.rs:297-380). */
 LENIA_API int lenia_set_resident(LeniaCtx* ctx, int32_t mode);
+/* The persistent step, on (mode 1; 2 + v: on in launch variant v, at most 64 or 128 registers a
+ * thread for v = 0, 1) or off (mode 0, the default until lenia_autotune chooses) for every size
+ * class it applies to: square worlds of 128, 192, 256, 384, 512, 768, 1024, 2048 or 4096 with one
+ * channel and one Lenia kernel on the FP32 path.  One launch then advances all of a class's worlds
+ * through every generation of a step call: a grid of resident CTAs claims the two-pass step's column
+ * and row items in order, world after world (a world's row items right after the next world's column
+ * items, so its half-spectrum is read back from L2), each item waiting, bounded, for the items of the
+ * same world it depends on.  The arithmetic is the two-pass step's, bit for bit.  A wait that gives
+ * up is reported as LENIA_ECUDA by lenia_sync.  Turning it on turns the cluster-resident step off.
+ * Rebuilds the step graphs.  No reference counterpart (the reference dispatches every pass of every
+ * world separately, crates/auto-core/src/sim.rs:297-380). */
+LENIA_API int lenia_set_persistent(LeniaCtx* ctx, int32_t mode);
 /* The tensor-core row pass on (1) or off (0, the default until lenia_autotune chooses per class) on
  * the TF32 and BF16X3 paths: the inverse
  * row DFT, the growth / dt / clamp update and the forward row DFT of the one-channel, one-kernel
