@@ -409,7 +409,9 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
     // (a 4096-point column item takes about as long as a quarter of the whole tensor-core launch),
     // so they run beside it on a side stream, on SMs the persistent tensor-core grid leaves free.
     const int reserve = (ncol + 1) / 2;
-    if (ncol <= 0 || reserve > ctx->sms / 16) {
+    // on a side branch of the step graph the FP32 items follow the tensor-core launch on the branch's
+    // own stream: the fork to the context's side stream is the main branch's
+    if (ncol <= 0 || reserve > ctx->sms / 16 || s != ctx->stream) {
         const bool ok = launch_col_tc(ctx->tc, ctx->path, cl.H, var_tc, ctx->d_worlds, tcg, ntcg, ctx->d_tw, s);
         return ok && launch_col_fp32(cl.H, variant, ctx->d_worlds, col, ncol, ctx->d_tw, s);
     }
@@ -520,7 +522,7 @@ int enqueue_steps(LeniaCtx* ctx, int steps) {
     // work a launch) run one after another on a second branch beside the large ones, whose launches
     // fill the GPU; lenia_autotune decides whether that pays.
     cudaStream_t s = ctx->stream;
-    const bool split = ctx->branch_cells > 0 && ctx->path == LENIA_PATH_FP32;
+    const bool split = ctx->branch_cells > 0;
     int used = 0;  // side branches in use
     if (split) CK(cudaEventRecord(ctx->ev_bfork, s));
     for (auto& cl : ctx->classes) {
@@ -1655,7 +1657,7 @@ int lenia_set_tc_rows(LeniaCtx* ctx, int32_t on) {
 int lenia_set_branch_split(LeniaCtx* ctx, int64_t cells, int32_t each) {
     if (!ctx) return LENIA_EINVAL;
     if (cells < 0 || (each != 0 && each != 1)) return fail(ctx, LENIA_EINVAL, "cells must be >= 0, each 0 or 1");
-    if (ctx->path != LENIA_PATH_FP32) return 0;  // one branch on the other paths
+    if (ctx->path == LENIA_PATH_RADIX2) return 0;  // no size classes
     ctx->branch_cells = cells;
     ctx->branch_each = each;
     CK(cudaStreamSynchronize(ctx->stream));
@@ -1828,7 +1830,7 @@ static int autotune_search(LeniaCtx* ctx) {
     }
     // The whole step: the small classes on a second graph branch beside the large ones, for every
     // split point between class sizes, against one branch (kept unless another is 3% faster).
-    if (ctx->path == LENIA_PATH_FP32 && ctx->classes.size() > 1) {
+    if (ctx->classes.size() > 1) {
         std::vector<int64_t> sizes;
         for (auto& cl : ctx->classes) sizes.push_back((int64_t)cl.W * cl.H);
         std::sort(sizes.begin(), sizes.end());

@@ -213,7 +213,7 @@ LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */
 LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
-/* Branches of the step graph (FP32 path): size classes of at most `cells` cells a world run on graph
+/* Branches of the step graph (FP32, TF32 and BF16X3 paths): size classes of at most `cells` cells a world run on graph
  * branches beside the larger classes -- one after another on one side branch (each = 0), or each on
  * a branch of its own (each = 1) -- so that the small classes' latency-bound launches share the GPU
  * with the large classes' (cells = 0: one branch, every class in turn, the default).  lenia_autotune

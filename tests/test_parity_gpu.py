@@ -508,14 +508,15 @@ def test_resident_step_applies_only_where_it_can():
         assert all(v["resident"] == 0 for v in sim.shapes().values())
 
 
-def test_two_branch_graph_gives_the_same_bits():
+@pytest.mark.parametrize("path", ["fp32", "bf16x3"])
+def test_two_branch_graph_gives_the_same_bits(path):
     """Running the small size classes on side graph branches beside the large ones (one side branch,
     or one each) only reorders independent launches: every state after 5 steps is bit-identical to
-    one branch."""
+    one branch.  On the tensor-core path the side branches hold tensor-core classes too (256, 512)."""
     worlds = configs.batched(64)
     outs = []
     for split, each in ((0, False), (256 * 256, False), (512 * 512, False), (384 * 384, True)):
-        with Sim(worlds, seed=0) as sim:
+        with Sim(worlds, seed=0, path=path) as sim:
             for i, w in enumerate(worlds):
                 sim.seed_patches(i, i, w.seed.patches)
             sim.set_branch_split(split, each)
