@@ -61,7 +61,7 @@ struct SizeClass {
     int* d_world_ids = nullptr;
     // tensor-core row pass (step_tc_row.cu): possible for one-channel, one-kernel Lenia classes on the
     // TF32 / BF16X3 paths whose row length it serves; `tc_rows` selects it over the FP32 row pass.
-    // Its groups are tc_row_stride consecutive FP32 row items.
+    // Its groups are tc_row_stride consecutive FP32 row items, or -tc_row_stride groups an item.
     int tc_rows_ok = 0, tc_rows = 0, tc_row_stride = 1;
     // persistent step (persist.cu): possible for square one-channel, one-kernel Lenia classes on the
     // FP32 path; `persist` selects one launch per class and step call over the two launches per
@@ -426,9 +426,10 @@ bool launch_columns(LeniaCtx* ctx, const SizeClass& cl, const ColItem* col, int 
 // The row pass of one step over a run of a class's row items: on the tensor cores where the class
 // takes them, else the FP32 pass.
 bool launch_rows_step(LeniaCtx* ctx, const SizeClass& cl, int variant, const RowItem* items, int nrow, cudaStream_t s) {
-    if (cl.tc_rows)
-        return launch_row_tc(ctx->tc, ctx->path, cl.W, ctx->d_worlds, items, cl.tc_row_stride, nrow / cl.tc_row_stride,
-                             ctx->d_tw, s);
+    if (cl.tc_rows) {
+        const int st = cl.tc_row_stride, ngroups = st > 0 ? nrow / st : nrow * -st;
+        return launch_row_tc(ctx->tc, ctx->path, cl.W, ctx->d_worlds, items, st, ngroups, ctx->d_tw, s);
+    }
     return launch_row_fp32(cl.W, variant, MODE_STEP, cl.general, ctx->d_worlds, items, nrow, cl.planes, ctx->d_tw, s);
 }
 
@@ -763,12 +764,13 @@ int setup_fused(LeniaCtx* ctx) {
         // their heights are whole groups of its rows
         if (tc_path && !general && tc_row_supports(cl.W)) {
             const int rg = tc_row_group_rows(cl.W);
-            bool fits = rg % (int)item_rows == 0;
+            bool fits = rg % (int)item_rows == 0 || (int)item_rows % rg == 0;
             for (int wi : cl.worlds) fits = fits && ctx->desc[wi].height % rg == 0;
             if (fits) {
                 int trc = tc_row_prepare(ctx->tc, ctx->path, cl.W, &ctx->err);
                 if (trc) return trc;
-                cl.tc_row_stride = rg / (int)item_rows;
+                // groups of rg rows: several items a group, or several groups an item (negative)
+                cl.tc_row_stride = rg >= (int)item_rows ? rg / (int)item_rows : -((int)item_rows / rg);
                 cl.tc_rows_ok = 1;
                 cl.tc_rows = TC_ROWS_DEFAULT;
             }

@@ -52,9 +52,9 @@ __global__ void __launch_bounds__(NT, MINB)
     extern __shared__ float4 smem_raw[];
     __shared__ long long s_item;
     __shared__ int s_stop;
-    constexpr int SEQ = seq_stride(N);
+    constexpr int SEQ = seq_stride(N), NSEQ = row_seqs(N, false) > TC ? row_seqs(N, false) : TC;
     float2* X = reinterpret_cast<float2*>(smem_raw);
-    float2* stw = X + TC * SEQ;  // the column pass's two tile sequences and the row pass's two packed rows
+    float2* stw = X + NSEQ * SEQ;  // after the column pass's tile sequences and the row pass's packed rows
     fill_stage_twiddles<N>(stw, tw, threadIdx.x, NT);
     int* cols_done = ctl + PST_COUNTERS;
     int* rows_done = cols_done + nw;
@@ -130,24 +130,26 @@ __global__ void __launch_bounds__(NT, MINB)
 
 namespace {
 
+// the larger of the column and row items' thread counts (an item with fewer butterflies than threads
+// leaves the rest idle in its stages)
 template <int N>
-constexpr int persist_nt() { return nt_of<N>(); }
+constexpr int persist_nt() { return nt_of<N>() > row_nt<N, false>() ? nt_of<N>() : row_nt<N, false>(); }
 // Two launch variants, as the two-pass step's: 0 caps registers at 64 a thread (twice the resident
 // CTAs; the column and row item bodies in one kernel spill 24-52 bytes a thread at 512 and above, and
 // 300-700 bytes below), 1 at 128 (no spills from 512 up).
 template <int N, int V>
-constexpr int persist_minb() { return minb_of<N, V>(); }
+constexpr int persist_minb() { return (V == 0 ? 1024 : 512) / persist_nt<N>() < 1 ? 1 : (V == 0 ? 1024 : 512) / persist_nt<N>(); }
 
 template <int N>
 size_t persist_smem() {
-    return (size_t)TC * seq_stride(N) * sizeof(float2) + stage_table_bytes<N>() + col_khat_bytes<N>();
+    constexpr int NSEQ = row_seqs(N, false) > TC ? row_seqs(N, false) : TC;
+    return (size_t)NSEQ * seq_stride(N) * sizeof(float2) + stage_table_bytes<N>() + col_khat_bytes<N>();
 }
 
 template <int N, int V>
 bool persist_go(const DevWorld* worlds, const ColItem* cols, const RowItem* rows, int nw, int nc, int nr, int gens,
                 const float2* tw, int* ctl, int* err, cudaStream_t s, int* capacity) {
     constexpr int NT = persist_nt<N>(), MINB = persist_minb<N, V>();
-    static_assert(NT == row_nt<N, false>(), "column and row items of a square class use the same threads");
     auto kern = persist_class<N, NT, MINB>;
     const size_t smem = persist_smem<N>();
     static int per_sm = -1, sms = 0;

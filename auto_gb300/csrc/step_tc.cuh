@@ -51,7 +51,8 @@ void tc_release(TcPlan& plan);
 bool tc_row_supports(int W);
 int tc_row_group_rows(int W);  // rows per group (a multiple of the FP32 row item's 4)
 int tc_row_prepare(TcPlan& plan, int path, int W, std::string* err);
-// items: the FP32 row pass's items (4 rows each); group g starts at items[g * item_stride].
+// items: the FP32 row pass's items; item_stride > 0: group g starts at items[g * item_stride]; < 0: an
+// item holds -item_stride groups of tc_row_group_rows(W) rows.
 bool launch_row_tc(const TcPlan& plan, int path, int W, const DevWorld* worlds, const RowItem* items, int item_stride,
                    int ngroups, const float2* tw, cudaStream_t s);
 void tc_row_release(TcPlan& plan);

@@ -77,8 +77,7 @@ struct TcRowShape {
     static_assert(SMEM <= 232448, "shared memory of one CTA");
 };
 
-// One group: RG rows starting at a row item; items[g * item_stride] gives its world and first row.
-// The item list is the FP32 row pass's (4 rows an item), so item_stride = RG / 4.
+// One group: RG rows of one world, from the FP32 row pass's item list (group_at).
 template <class S>
 __global__ void __launch_bounds__(128, 1)
     row_pass_tc(const DevWorld* __restrict__ worlds, const RowItem* __restrict__ items, int item_stride, int ngroups,
@@ -133,9 +132,18 @@ __global__ void __launch_bounds__(128, 1)
         }
     }
 
+    // Group g's world and first row, from the row items.  item_stride > 0:
+    // a group spans item_stride items; < 0: an item holds -item_stride groups.
+    auto group_at = [&](int g) {
+        if (item_stride > 0) return items[(size_t)g * item_stride];
+        const int sub = -item_stride;
+        RowItem it = items[g / sub];
+        it.row0 += (g % sub) * S::RG;
+        return it;
+    };
     // The group's half-spectrum rows, 16 bytes (one tile's two columns of one row) per copy.
     auto fetch_rows = [&](int g, float2* dst) {
-        const RowItem it = items[(size_t)g * item_stride];
+        const RowItem it = group_at(g);
         const DevWorld& wd = worlds[it.world];
         const float2* src = wd.conv + (size_t)it.row0 * TC;
         const int H = wd.H;
@@ -146,7 +154,7 @@ __global__ void __launch_bounds__(128, 1)
     };
     // The group's state rows by bulk copies (one thread).
     auto fetch_state = [&](int g) {
-        const RowItem it = items[(size_t)g * item_stride];
+        const RowItem it = group_at(g);
         const float* src = worlds[it.world].state + (size_t)it.row0 * S::W;
         mbar_arrive_expect_tx(bar_st, S::RG * S::W * 4);
         for (int r = 0; r < S::RG; r++) bulk_g2s(st + r * S::STR, src + (size_t)r * S::W, S::W * 4, bar_st);
@@ -185,7 +193,7 @@ __global__ void __launch_bounds__(128, 1)
 
     int buf = 0;
     for (int g = blockIdx.x; g < ngroups && !abort; g += gridDim.x, buf ^= 1) {
-        const RowItem it = items[(size_t)g * item_stride];
+        const RowItem it = group_at(g);
         const DevWorld& wd = worlds[it.world];
         const int H = wd.H;
         float2* xs = xsb + buf * (S::XSB / 8);
