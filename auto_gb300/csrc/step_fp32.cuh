@@ -210,8 +210,9 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 // 1024 wide: an item then reads and writes each tile's spectrum as 128 contiguous bytes (8 rows x 16
 // B) instead of 64, and on the 384-world batched workload the row pass went from 189 to 166 us a
 // generation for the 1024 x 1024 class (512: 41 -> 34 us), the step from 1.75e11 to 1.87e11 cell-updates/s.
-// Wider rows keep S = 2: measured at 4096 x 4096, S = 1 (256 threads, three or four CTAs per SM) was
-// 5-30% slower than S = 2 (512 threads, two CTAs per SM).  The general step keeps a plane of W x 2S floats besides
+// Wider rows keep S = 2: measured at 4096 x 4096, S = 4 (1024 threads, one CTA per SM) was 10% slower
+// (row pass 76 against 68 us) and S = 1 (256 threads, three or four CTAs per SM) 5-30% slower than
+// S = 2 (512 threads, two CTAs per SM).  The general step keeps a plane of W x 2S floats besides
 // the sequences; from W = 2048 up it uses S = 1 (at S = 2 a 4096-wide item needed 138 KB of shared
 // memory, one CTA per SM; MNCA at 4096 x 4096 measured 7% faster at S = 1), below it S = 2 (the
 // 3-channel 1024 x 1024 world measured 5% slower at S = 1).
