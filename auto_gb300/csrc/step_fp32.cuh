@@ -216,10 +216,18 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 // the sequences; from W = 2048 up it uses S = 1 (at S = 2 a 4096-wide item needed 138 KB of shared
 // memory, one CTA per SM; MNCA at 4096 x 4096 measured 7% faster at S = 1), below it S = 2 (the
 // 3-channel 1024 x 1024 world measured 5% slower at S = 1).
+// Threads of a row item of S sequences of length N: one first-stage butterfly per thread; for sides
+// 3 * 2^k at least one per four radix-3 butterflies as well.  768 = 16.3.16 with 192 threads for four
+// sequences ran its radix-3 stage in six rounds, the last a third full, and needed 128 registers a
+// thread; with 256 it fits 64, and the batched workload's 768 x 768 row pass went from 104 to 89 us a
+// generation (the step from 1.87e11 to 1.93e11 cell-updates/s).
+FFT_CHD constexpr int seq_threads(int N, int S) {
+    return N % 3 == 0 && S * N / 12 > S * N / plan_radix(N, 0) ? S * N / 12 : S * N / plan_radix(N, 0);
+}
 FFT_CHD constexpr int row_seqs(int W, bool gen) { return gen ? (W >= 2048 ? 1 : 2) : (W <= 1024 ? 4 : 2); }
 template <int W, bool GEN>
 constexpr int row_nt() {
-    constexpr int n = row_seqs(W, GEN) * W / plan_radix(W, 0);
+    constexpr int n = seq_threads(W, row_seqs(W, GEN));
     return n < 64 ? 64 : (n > 1024 ? 1024 : n);
 }
 // variant 0: at most 1024 threads' worth of registers per SM (64 a thread at 512 threads);
@@ -797,6 +805,8 @@ __global__ void __launch_bounds__(NT, MINB) col_pass_pair(const DevWorld* __rest
 // thread for the two sequences a CTA holds (2N / first radix), between 64 and 1024.
 #define LENIA_SIZES_SMALL(X) X(32) X(48) X(64) X(96) X(128) X(192) X(256) X(384) X(512) X(768)
 #define LENIA_SIZES_LARGE(X) X(1024) X(1536) X(2048) X(3072) X(4096) X(6144) X(8192)
+// (The column pass keeps one first-stage butterfly per thread at every size: at 768 the balanced count,
+// 128 threads, made it slower, 66 -> 73 us a generation on the batched workload's class.)
 template <int N> constexpr int nt_of() {
     constexpr int n = 2 * N / plan_radix(N, 0);  // one first-stage butterfly per thread, two sequences
     return n < 64 ? 64 : (n > 1024 ? 1024 : n);
