@@ -224,7 +224,7 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 FFT_CHD constexpr int seq_threads(int N, int S) {
     return N % 3 == 0 && S * N / 12 > S * N / plan_radix(N, 0) ? S * N / 12 : S * N / plan_radix(N, 0);
 }
-FFT_CHD constexpr int row_seqs(int W, bool gen) { return gen ? (W >= 2048 ? 1 : 2) : (W <= 1024 ? 4 : 2); }
+FFT_CHD constexpr int row_seqs(int W, bool gen) { return gen ? (W >= 2048 ? 1 : (W <= 1024 ? 4 : 2)) : (W <= 1024 ? 4 : 2); }
 template <int W, bool GEN>
 constexpr int row_nt() {
     constexpr int n = seq_threads(W, row_seqs(W, GEN));
