@@ -214,8 +214,9 @@ __device__ __forceinline__ float mnca_update(float s, float c0, float c1) {
 // (row pass 76 against 68 us) and S = 1 (256 threads, three or four CTAs per SM) 5-30% slower than
 // S = 2 (512 threads, two CTAs per SM).  The general step keeps a plane of W x 2S floats besides
 // the sequences; from W = 2048 up it uses S = 1 (at S = 2 a 4096-wide item needed 138 KB of shared
-// memory, one CTA per SM; MNCA at 4096 x 4096 measured 7% faster at S = 1), below it S = 2 (the
-// 3-channel 1024 x 1024 world measured 5% slower at S = 1).
+// memory, one CTA per SM; MNCA at 4096 x 4096 measured 7% faster at S = 1), up to 1024 wide S = 4 (the
+// 3-channel 1024 x 1024 world: 5.97e10 -> 6.33e10 channel-cell updates/s from S = 2, and 5% slower at
+// S = 1 than at S = 2), in between S = 2.
 // Threads of a row item of S sequences of length N: one first-stage butterfly per thread; for sides
 // 3 * 2^k at least one per four radix-3 butterflies as well.  768 = 16.3.16 with 192 threads for four
 // sequences ran its radix-3 stage in six rounds, the last a third full, and needed 128 registers a
