@@ -536,11 +536,12 @@ def run_ours(args, dist):
                                            "cell_updates_per_s": n / ((cms + rms) * 1e-3) if cms + rms > 0 else None,
                                            "launch_variant": v}
     nclasses = len({(w.width, w.height) for w in worlds})
-    # per size class and generation: one column and one row launch; the tensor-core paths add the
-    # FP32 column launch for each channel's first tile group (sizes 256..4096)
+    # per size class (per chunk of a chunked class) and generation: one column and one row launch; the
+    # tensor-core paths add the FP32 column launch for each channel's first tile group (sizes 256..4096)
     tc_sizes = (256, 512, 1024, 2048, 4096)
     shapes = sim.shapes()
-    launches_per_gen = sum(3 if args.path in ("tf32", "bf16x3") and h in tc_sizes else 2
+    launches_per_gen = sum((3 if args.path in ("tf32", "bf16x3") and h in tc_sizes else 2) *
+                           max(1, shapes.get((wd, h), {}).get("chunks", 1))  # a chunked class: per chunk
                            for (wd, h) in {(w.width, w.height) for w in worlds}
                            if not shapes.get((wd, h), {}).get("resident") and shapes.get((wd, h), {}).get("persistent", -1) < 0)
     # a cluster-resident or persistent class is one launch per bench step (all G generations)
