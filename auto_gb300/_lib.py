@@ -23,7 +23,7 @@ EXPORTS = [
     "lenia_last_error", "lenia_create", "lenia_destroy", "lenia_write_state", "lenia_read_state",
     "lenia_write_state_device", "lenia_read_state_device", "lenia_write_states", "lenia_read_states", "lenia_write_states_async", "lenia_read_states_async", "lenia_step", "lenia_step_timed", "lenia_sync",
     "lenia_tick", "lenia_seed_tiles", "lenia_seed_patches", "lenia_cells_per_step", "lenia_memory_bytes",
-    "lenia_read_field_u", "lenia_read_spectrum", "lenia_world_stats", "lenia_autotune", "lenia_set_variants", "lenia_class_variants", "lenia_class_shapes", "lenia_set_chunk_budget", "lenia_set_resident", "lenia_set_persistent", "lenia_set_tc_rows", "lenia_set_tc_variant", "lenia_set_branch_split", "lenia_branch_split", "lenia_profile_step", "lenia_profile_classes",
+    "lenia_read_field_u", "lenia_read_spectrum", "lenia_world_stats", "lenia_autotune", "lenia_set_variants", "lenia_class_variants", "lenia_class_shapes", "lenia_set_chunk_budget", "lenia_set_chunk_lanes", "lenia_set_resident", "lenia_set_persistent", "lenia_set_tc_rows", "lenia_set_tc_variant", "lenia_set_branch_split", "lenia_branch_split", "lenia_profile_step", "lenia_profile_classes",
     "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_tc_set_wait_limit", "lenia_step_noalloc",
     "lenia_mlp_create", "lenia_mlp_destroy", "lenia_mlp_param_count", "lenia_mlp_set_params",
     "lenia_mlp_get_params", "lenia_mlp_gradients", "lenia_mlp_train_step", "lenia_mlp_predict",
@@ -91,6 +91,7 @@ def _declare(L):
         "lenia_class_variants": [vp, ctypes.POINTER(ctypes.c_int32), sz, ctypes.POINTER(ctypes.c_size_t)],
         "lenia_class_shapes": [vp, ctypes.POINTER(ctypes.c_int32), sz, ctypes.POINTER(ctypes.c_size_t)],
         "lenia_set_chunk_budget": [vp, u32],
+        "lenia_set_chunk_lanes": [vp, i32],
         "lenia_set_resident": [vp, i32],
         "lenia_set_persistent": [vp, i32],
         "lenia_set_tc_rows": [vp, i32],

@@ -53,6 +53,7 @@ struct SizeClass {
     size_t bytes = 0;          // device bytes the class's worlds touch in a step
     size_t chunk_budget = 0;   // largest chunk in bytes (0: the whole class is one chunk)
     std::vector<Chunk> chunks;
+    int lanes = 1;             // concurrent lanes its chunks run on (enqueue_class)
     // cluster-resident step (resident.cu): possible for square one-channel, one-kernel Lenia classes
     // of 128..512 on the FP32 path; `resident` selects it over the two launches per generation
     int resident_ok = 0, resident = 0;
@@ -71,12 +72,16 @@ struct SizeClass {
     int* d_pctl = nullptr;
 };
 
-// Default chunk budget: 0, every class is one chunk.  Chunks of up to 32 MiB do keep their worlds in
-// L2 (measured with ncu on the 55 worlds of 1024 x 1024: DRAM traffic 1.4 GB -> 23 MB per
-// generation), but the passes are not bound by HBM there, and launches over a few worlds fill the GPU
-// less: every budget measured slower (1024 x 1024: 1.91e11 cell-updates/s as one chunk, 1.75e11 in 8
-// chunks, 1.50e11 in 16).  The autotuner still tries budgets per class.
-constexpr size_t DEFAULT_CHUNK_BUDGET = 0;
+// Default chunk budget and lanes: a class of more than 64 MiB of per-step data runs in chunks of at
+// most 64 MiB, two chunks at a time on concurrent lanes.  A chunk keeps its worlds in L2 across its
+// generations (ncu on the 55 worlds of 1024 x 1024 in 32 MiB chunks: DRAM traffic 1.4 GB -> 23 MB per
+// generation), but a launch over a few worlds fills the GPU less, and chunks one after another
+// measured slower than one chunk (1024 x 1024: 2.07e11 cell-updates/s as one chunk, 1.87e11 in 8
+// chunks of 64 MiB, 1.53e11 in 16 of 32 MiB).  On two lanes the chunks' launches fill the GPU
+// together: 2.23e11 in 8 chunks of 64 MiB (768 x 768: 1.55e11 -> 1.79e11).  The autotuner tries
+// other budgets and 1 to 4 lanes per class.
+constexpr size_t DEFAULT_CHUNK_BUDGET = 64ull << 20;
+constexpr int DEFAULT_LANES = 2;
 // Whether a class the persistent step serves starts with it (the autotuner times it against the two
 // launches per generation and keeps the faster).  Off: on the batched workload every class measured
 // slower persistent (1024 x 1024: 1.73e11 cell-updates/s against 1.92e11; 128 x 128: 3.5e10 against
@@ -121,6 +126,11 @@ struct LeniaCtx {
     cudaEvent_t ev_bfork = nullptr, ev_bjoin[MAX_BRANCHES] = {};
     int64_t branch_cells = 0;
     int branch_each = 0;
+    // chunk lanes: the chunks of a class on the main branch may run on up to MAX_LANES concurrent
+    // graph branches (SizeClass::lanes), chunk c on lane c mod lanes
+    static constexpr int MAX_LANES = 4;
+    cudaStream_t lane[MAX_LANES] = {};
+    cudaEvent_t ev_lfork = nullptr, ev_ljoin[MAX_LANES] = {};
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // asynchronous state copies (lenia_write_states_async / lenia_read_states_async): uploads on
     // `up`, downloads on `down`, through device staging buffers, so that they overlap the
@@ -433,12 +443,13 @@ bool launch_rows_step(LeniaCtx* ctx, const SizeClass& cl, int variant, const Row
     return launch_row_fp32(cl.W, variant, MODE_STEP, cl.general, ctx->d_worlds, items, nrow, cl.planes, ctx->d_tw, s);
 }
 
-// A launch shape of one size class: launch variants and chunks.
+// A launch shape of one size class: launch variants, chunks and the lanes the chunks run on.
 struct Shape {
     int var_col, var_row, var_tc;
     const std::vector<Chunk>* chunks;
+    int lanes;
 };
-Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, cl.var_tc, &cl.chunks}; }
+Shape shape_of(const SizeClass& cl) { return Shape{cl.var_col, cl.var_row, cl.var_tc, &cl.chunks, cl.lanes}; }
 
 // `steps` steps of one size class, chunk after chunk, in the given launch shape; a resident class is
 // one launch for all its worlds and steps.
@@ -457,15 +468,30 @@ int enqueue_class(LeniaCtx* ctx, const SizeClass& cl, const Shape& sh, int steps
             return fail(ctx, LENIA_ECUDA, "resident launch failed (%dx%d)", cl.W, cl.H);
         return 0;
     }
-    for (const Chunk& ch : *sh.chunks) {
+    // chunks of a class on the main branch may run on concurrent lanes (each lane's chunks one after
+    // another); lanes fork from and join into the class's stream
+    const int nch = (int)sh.chunks->size();
+    const int lanes = (s == ctx->stream && nch > 1) ? std::min(std::min(sh.lanes, nch), LeniaCtx::MAX_LANES) : 1;
+    if (lanes > 1) {
+        CK(cudaEventRecord(ctx->ev_lfork, s));
+        for (int l = 0; l < lanes; l++) CK(cudaStreamWaitEvent(ctx->lane[l], ctx->ev_lfork, 0));
+    }
+    for (int c = 0; c < nch; c++) {
+        const Chunk& ch = (*sh.chunks)[c];
+        cudaStream_t on = lanes > 1 ? ctx->lane[c % lanes] : s;
         for (int st = 0; st < steps; st++) {
             bool ok = launch_columns(ctx, cl, cl.d_col + ch.col0, ch.ncol, cl.d_tcg + ch.tcg0, ch.ntcg, sh.var_col,
-                                     sh.var_tc, s);
+                                     sh.var_tc, on);
             if (!ok) return fail(ctx, LENIA_ECUDA, "column launch failed (H=%d)", cl.H);
-            ok = launch_rows_step(ctx, cl, sh.var_row, cl.d_row + ch.row0, ch.nrow, s);
+            ok = launch_rows_step(ctx, cl, sh.var_row, cl.d_row + ch.row0, ch.nrow, on);
             if (!ok) return fail(ctx, LENIA_ECUDA, "row launch failed (W=%d)", cl.W);
         }
     }
+    if (lanes > 1)
+        for (int l = 0; l < lanes; l++) {
+            CK(cudaEventRecord(ctx->ev_ljoin[l], ctx->lane[l]));
+            CK(cudaStreamWaitEvent(s, ctx->ev_ljoin[l], 0));
+        }
     return 0;
 }
 
@@ -789,6 +815,7 @@ int setup_fused(LeniaCtx* ctx) {
             cl.bytes += world_step_bytes(ctx->desc[wi]);
         }
         cl.chunk_budget = DEFAULT_CHUNK_BUDGET;
+        cl.lanes = DEFAULT_LANES;
         cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
         // the cluster-resident step: square one-channel, one-kernel Lenia worlds of 128..512 on the
         // FP32 path, where the GPU can hold at least one of its clusters
@@ -1076,6 +1103,16 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
             fail(ctx, LENIA_ECUDA, "stream creation failed");
             return bail(LENIA_ECUDA);
         }
+    if (cudaEventCreateWithFlags(&ctx->ev_lfork, cudaEventDisableTiming) != cudaSuccess) {
+        fail(ctx, LENIA_ECUDA, "stream creation failed");
+        return bail(LENIA_ECUDA);
+    }
+    for (int l = 0; l < LeniaCtx::MAX_LANES; l++)
+        if (cudaStreamCreateWithFlags(&ctx->lane[l], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&ctx->ev_ljoin[l], cudaEventDisableTiming) != cudaSuccess) {
+            fail(ctx, LENIA_ECUDA, "stream creation failed");
+            return bail(LENIA_ECUDA);
+        }
     // twiddles exp(-2 pi i t / TWN) from FP64
     {
         std::vector<float2> tw(lfft::TWN);
@@ -1142,6 +1179,11 @@ int lenia_destroy(LeniaCtx* ctx) {
         if (ctx->ev_bjoin[b]) cudaEventDestroy(ctx->ev_bjoin[b]);
     }
     if (ctx->ev_bfork) cudaEventDestroy(ctx->ev_bfork);
+    for (int l = 0; l < LeniaCtx::MAX_LANES; l++) {
+        if (ctx->lane[l]) cudaStreamSynchronize(ctx->lane[l]), cudaStreamDestroy(ctx->lane[l]);
+        if (ctx->ev_ljoin[l]) cudaEventDestroy(ctx->ev_ljoin[l]);
+    }
+    if (ctx->ev_lfork) cudaEventDestroy(ctx->ev_lfork);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return 0;
@@ -1508,7 +1550,7 @@ int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t coun
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (steps == 0 || count < 4 * ctx->classes.size()) return fail(ctx, LENIA_EINVAL, "need steps > 0 and 4 floats per class");
+    if (steps == 0 || count < 5 * ctx->classes.size()) return fail(ctx, LENIA_EINVAL, "need steps > 0 and 5 floats per class");
     if (ctx->path == LENIA_PATH_RADIX2) return fail(ctx, LENIA_ESTATE, "the radix-2 path has no size classes");
     int frc = flush_spectra(ctx);
     if (frc) return frc;
@@ -1517,12 +1559,18 @@ int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t coun
         double col_ms = 0, row_ms = 0;
         int rc = time_class(ctx, cl, shape_of(cl), (int)steps, &col_ms, &row_ms);
         if (rc) return rc;
-        out[4 * c] = (float)cl.W;
-        out[4 * c + 1] = (float)cl.H;
-        out[4 * c + 2] = (float)(col_ms / steps);
-        out[4 * c + 3] = (float)(row_ms / steps);
+        // the class as the step graph runs it: launches back to back, chunks on their lanes (replayed
+        // twice, the second timed)
+        double graph_ms = 0;
+        rc = time_class_graph(ctx, cl, shape_of(cl), (int)steps, &graph_ms);
+        if (rc) return rc;
+        out[5 * c] = (float)cl.W;
+        out[5 * c + 1] = (float)cl.H;
+        out[5 * c + 2] = (float)(col_ms / steps);
+        out[5 * c + 3] = (float)(row_ms / steps);
+        out[5 * c + 4] = (float)(graph_ms / steps);
     }
-    ctx->tick += steps;
+    ctx->tick += 3 * steps;
     return check_device_errors(ctx);
 }
 
@@ -1590,6 +1638,19 @@ int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib) {
         cl.chunk_budget = (size_t)mib << 20;
         cl.chunks = make_chunks(ctx, cl, cl.chunk_budget);
     }
+    CK(cudaStreamSynchronize(ctx->stream));
+    int rc = rebuild_graphs(ctx);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return 0;
+}
+
+int lenia_set_chunk_lanes(LeniaCtx* ctx, int32_t lanes) {
+    if (!ctx) return LENIA_EINVAL;
+    if (lanes < 1 || lanes > LeniaCtx::MAX_LANES)
+        return fail(ctx, LENIA_EINVAL, "lanes must be 1..%d, got %d", LeniaCtx::MAX_LANES, lanes);
+    if (ctx->path == LENIA_PATH_RADIX2) return 0;  // no size classes
+    for (auto& cl : ctx->classes) cl.lanes = lanes;
     CK(cudaStreamSynchronize(ctx->stream));
     int rc = rebuild_graphs(ctx);
     if (rc) return rc;
@@ -1680,10 +1741,10 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
     if (!ctx || !nclasses) return LENIA_EINVAL;
     *nclasses = ctx->classes.size();
     if (!out) return 0;
-    if (count < 13 * ctx->classes.size()) return LENIA_EINVAL;
+    if (count < 14 * ctx->classes.size()) return LENIA_EINVAL;
     for (size_t i = 0; i < ctx->classes.size(); i++) {
         const auto& cl = ctx->classes[i];
-        int32_t* o = out + 13 * i;
+        int32_t* o = out + 14 * i;
         o[0] = cl.W;
         o[1] = cl.H;
         o[2] = cl.var_col;
@@ -1697,6 +1758,7 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
         o[10] = cl.tc_rows;
         o[11] = cl.ntcg > 0 ? cl.var_tc : -1;
         o[12] = cl.persist ? cl.var_per : -1;
+        o[13] = cl.lanes;
     }
     return 0;
 }
@@ -1722,7 +1784,8 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
 // resident and persistent steps against two launches a generation (FP32 path, where they apply), the
 // tensor-core row
 // pass against the FP32 one (TF32 / BF16X3 paths, where it applies), every pair of column and row
-// launch variants, then every chunk budget that gives a different number of chunks.
+// launch variants, then every chunk budget that gives a different number of chunks, with the chunks
+// one after another or on 2..MAX_LANES concurrent lanes.
 // Each candidate is timed as a captured graph of a few steps (time_class_graph), and a class keeps
 // its current choice of a dimension unless another is at least 3% faster, so that timing noise does
 // not flip it.
@@ -1788,7 +1851,7 @@ static int autotune_search(LeniaCtx* ctx) {
             // CTAs an SM); candidate 0 is the current choice
             std::vector<Shape> c{shape_of(cl)};
             for (int v = 0; v < TC_COL_VARIANTS; v++)
-                if (v != cl.var_tc) c.push_back(Shape{cl.var_col, cl.var_row, v, &cl.chunks});
+                if (v != cl.var_tc) c.push_back(Shape{cl.var_col, cl.var_row, v, &cl.chunks, cl.lanes});
             if ((rc = pick(c, &bi))) return rc;
             cl.var_tc = c[bi].var_tc;
         }
@@ -1809,7 +1872,8 @@ static int autotune_search(LeniaCtx* ctx) {
             std::vector<Shape> c{shape_of(cl)};
             for (int vc = 0; vc < 3; vc++)
                 for (int vr = 0; vr < 2; vr++)
-                    if (vc != cl.var_col || vr != cl.var_row) c.push_back(Shape{vc, vr, cl.var_tc, &cl.chunks});
+                    if (vc != cl.var_col || vr != cl.var_row)
+                        c.push_back(Shape{vc, vr, cl.var_tc, &cl.chunks, cl.lanes});
             if ((rc = pick(c, &bi))) return rc;
             cl.var_col = c[bi].var_col;
             cl.var_row = c[bi].var_row;
@@ -1823,11 +1887,20 @@ static int autotune_search(LeniaCtx* ctx) {
                 for (auto& l : lists) seen = seen || l.size() == ch.size();
                 if (!seen) lists.push_back(ch), bud.push_back(b);
             }
-            std::vector<Shape> c;
-            for (auto& l : lists) c.push_back(Shape{cl.var_col, cl.var_row, cl.var_tc, &l});
+            // each list of chunks one after another and on 2..MAX_LANES concurrent lanes; candidate 0 is
+            // the current choice
+            std::vector<Shape> c{Shape{cl.var_col, cl.var_row, cl.var_tc, &lists[0], cl.lanes}};
+            std::vector<size_t> which{0};
+            for (size_t li = 0; li < lists.size(); li++)
+                for (int ln = 1; ln <= LeniaCtx::MAX_LANES && ln <= (int)lists[li].size(); ln++)
+                    if (!(li == 0 && ln == c[0].lanes)) {
+                        c.push_back(Shape{cl.var_col, cl.var_row, cl.var_tc, &lists[li], ln});
+                        which.push_back(li);
+                    }
             if ((rc = pick(c, &bi))) return rc;
-            cl.chunk_budget = bud[bi];
-            cl.chunks = lists[bi];
+            cl.chunk_budget = bud[which[bi]];
+            cl.lanes = c[bi].lanes;
+            cl.chunks = lists[which[bi]];
         }
     }
     // The whole step: the small classes on a second graph branch beside the large ones, for every

@@ -202,14 +202,15 @@ class Sim:
         """{(width, height): {...}} for every size class: launch variants, chunks (L2-resident runs of
         worlds), worlds, chunk budget (MiB, 0 = one chunk), rows per row-pass item and whether the class runs
         the cluster-resident step, whether its row pass runs on the tensor cores, its tensor-core column
-        pass variant (-1: none), and its persistent step's launch variant (-1: it does not run it)."""
+        pass variant (-1: none), its persistent step's launch variant (-1: it does not run it), and the
+        concurrent lanes its chunks run on."""
         n = ctypes.c_size_t(0)
         self._check(self._L.lenia_class_shapes(self._ctx, None, 0, ctypes.byref(n)))
-        out = (ctypes.c_int32 * (13 * n.value))()
-        self._check(self._L.lenia_class_shapes(self._ctx, out, 13 * n.value, ctypes.byref(n)))
+        out = (ctypes.c_int32 * (14 * n.value))()
+        self._check(self._L.lenia_class_shapes(self._ctx, out, 14 * n.value, ctypes.byref(n)))
         keys = ("column_variant", "row_variant", "chunks", "worlds", "chunk_budget_mib", "rows_per_row_item",
-                "resident", "resident_variant", "tc_rows", "tc_column_variant", "persistent")
-        return {(out[13 * i], out[13 * i + 1]): dict(zip(keys, out[13 * i + 2:13 * i + 13])) for i in range(n.value)}
+                "resident", "resident_variant", "tc_rows", "tc_column_variant", "persistent", "lanes")
+        return {(out[14 * i], out[14 * i + 1]): dict(zip(keys, out[14 * i + 2:14 * i + 14])) for i in range(n.value)}
 
     def set_resident(self, on: bool, variant: int = -1):
         """Cluster-resident step on or off where it applies, optionally in launch variant `variant`
@@ -245,6 +246,10 @@ class Sim:
         """Pin every size class's chunk budget in MiB (see lenia_set_chunk_budget); 0 = one chunk."""
         self._check(self._L.lenia_set_chunk_budget(self._ctx, int(mib)))
 
+    def set_chunk_lanes(self, lanes: int):
+        """Pin every size class's chunk lanes, 1..4 (see lenia_set_chunk_lanes)."""
+        self._check(self._L.lenia_set_chunk_lanes(self._ctx, int(lanes)))
+
     def set_variants(self, column: int = -1, row: int = -1):
         """Pin every size class's launch variants (see lenia_set_variants); -1 keeps one."""
         self._check(self._L.lenia_set_variants(self._ctx, int(column), int(row)))
@@ -256,10 +261,11 @@ class Sim:
         return out
 
     def profile_classes(self, steps: int = 5):
-        """Per size class: {(width, height): (column ms, row ms)} per step, each class timed alone."""
+        """Per size class: {(width, height): (column ms, row ms, graph ms)} per step, each class timed
+        alone: its column and row launches one at a time, and the class as the step graph runs it."""
         n = ctypes.c_size_t()
         self._check(self._L.lenia_profile_classes(self._ctx, int(steps), None, 0, ctypes.byref(n)))
-        out = np.zeros(4 * n.value, np.float32)
+        out = np.zeros(5 * n.value, np.float32)
         self._check(self._L.lenia_profile_classes(self._ctx, int(steps), fptr(out), out.size, ctypes.byref(n)))
-        return {(int(out[4 * i]), int(out[4 * i + 1])): (float(out[4 * i + 2]), float(out[4 * i + 3]))
+        return {(int(out[5 * i]), int(out[5 * i + 1])): tuple(float(x) for x in out[5 * i + 2:5 * i + 5])
                 for i in range(n.value)}

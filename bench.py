@@ -85,6 +85,9 @@ def parse(argv=None):
     p.add_argument("--traffic-from", default=None, metavar="CSV",
                    help="summarise an ncu --csv capture of --profile-window (dram__bytes_read.sum, "
                         "dram__bytes_write.sum, gpu__time_duration.sum) into profiles/traffic.json and exit")
+    p.add_argument("--traffic-graph", action="store_true",
+                   help="with --traffic-from: the capture profiled the whole graph replay as one workload (ncu "
+                        "--graph-profiling graph), so concurrent branches and lanes ran as in the timed run")
     return p.parse_args(argv)
 
 
@@ -411,10 +414,11 @@ def parse_ncu_csv(path):
     return rows
 
 
-def summarise_traffic(csv_path, config, path, gens):
+def summarise_traffic(csv_path, config, path, gens, graph=False):
     """DRAM bytes per generation of one graph replay (``--profile-window``): every launch's
     dram__bytes_read.sum + dram__bytes_write.sum summed and divided by the generations the replay
-    ran, with the share of each kernel family.  Written to profiles/traffic.json under
+    ran, with the share of each kernel family.  With ``graph`` the capture holds one result, the
+    whole replay profiled as one workload.  Written to profiles/traffic.json under
     "<config>/<path>"."""
     rows = parse_ncu_csv(csv_path)
     if not rows:
@@ -439,10 +443,15 @@ def summarise_traffic(csv_path, config, path, gens):
     key = "%s/%s" % (config, path)
     data[key] = total_b / gens
     details = data.setdefault("details", {})
-    details[key] = {"launches": len(rows), "generations": gens, "dram_bytes_per_generation": total_b / gens,
-                    "cache": "warm (ncu --cache-control none, one graph replay after warm-up)", "kernels": fam}
-    data["note"] = ("DRAM bytes per generation: dram__bytes_read.sum + dram__bytes_write.sum over every launch "
-                    "of one graph replay, divided by its generations; command in profiles/traffic.md")
+    details[key] = {"results": len(rows), "generations": gens, "dram_bytes_per_generation": total_b / gens,
+                    "cache": "warm (ncu --cache-control none, one graph replay after warm-up)",
+                    "profiled": ("the whole graph replay as one workload (ncu --graph-profiling graph): branches and "
+                                 "lanes concurrent as in the timed run") if graph else
+                                ("every launch on its own (ncu serialises them: a graph's concurrent lanes run one "
+                                 "after another)"),
+                    "kernels": fam}
+    data["note"] = ("DRAM bytes per generation: dram__bytes_read.sum + dram__bytes_write.sum over one graph "
+                    "replay, divided by its generations; command in profiles/traffic.md")
     with open(TRAFFIC_JSON, "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
         f.write("\n")
@@ -497,7 +506,8 @@ def run_ours(args, dist):
                                "worlds": v["worlds"], "chunk_budget_mib": v["chunk_budget_mib"],
                                "rows_per_row_item": v["rows_per_row_item"], "resident": v["resident"],
                                "resident_variant": v["resident_variant"], "tc_rows": v["tc_rows"],
-                               "tc_column_variant": v["tc_column_variant"], "persistent": v["persistent"]}
+                               "tc_column_variant": v["tc_column_variant"], "persistent": v["persistent"],
+                               "lanes": v["lanes"]}
                 for wh, v in sim.shapes().items()}
     G = args.gens
     cells = sim.cells_per_step
@@ -528,12 +538,14 @@ def run_ours(args, dist):
         class_cells[(w.width, w.height)] = class_cells.get((w.width, w.height), 0) + w.channels * w.width * w.height
     classes = {}
     if len(class_cells) > 1 and args.path != "radix2":
-        for (cw, ch), (cms, rms) in sorted(sim.profile_classes(3).items()):
+        # per class, alone: column and row launches each under events (serial), and the class as the
+        # step graph runs it (chunks on their lanes), which gives its rate
+        for (cw, ch), (cms, rms, gms) in sorted(sim.profile_classes(3).items()):
             n = class_cells[(cw, ch)]
             v = variants.get("%dx%d" % (cw, ch), {})
             classes["%dx%d" % (cw, ch)] = {"worlds": sum(1 for w in worlds if (w.width, w.height) == (cw, ch)),
-                                           "column_ms": cms, "row_ms": rms,
-                                           "cell_updates_per_s": n / ((cms + rms) * 1e-3) if cms + rms > 0 else None,
+                                           "column_ms": cms, "row_ms": rms, "graph_ms": gms,
+                                           "cell_updates_per_s": n / (gms * 1e-3) if gms > 0 else None,
                                            "launch_variant": v}
     nclasses = len({(w.width, w.height) for w in worlds})
     # per size class (per chunk of a chunked class) and generation: one column and one row launch; the
@@ -787,7 +799,7 @@ def main():
     dist.gpu_index = gpu
     try:
         if args.traffic_from:
-            per_gen, det = summarise_traffic(args.traffic_from, args.config, args.path, args.gens)
+            per_gen, det = summarise_traffic(args.traffic_from, args.config, args.path, args.gens, args.traffic_graph)
             print(json.dumps({"traffic_per_generation": per_gen, "details": det}))
         elif args.profile_window:
             profile_window(args, dist)

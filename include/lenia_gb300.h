@@ -182,7 +182,8 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
  * tensor-core row pass against the FP32 one (lenia_set_tc_rows, where they apply), then for
  * two-pass classes the pair of column and row
  * launch variants and every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that
- * changes the class's number of chunks; then, for the whole step, the split of small classes onto a
+ * changes the class's number of chunks, with its chunks one after another or on 2 to 4 concurrent
+ * lanes (lenia_set_chunk_lanes); then, for the whole step, the split of small classes onto a
  * second graph branch (lenia_set_branch_split).
  * The states are saved first and restored afterwards, also when it fails.  Rebuilds the step
  * graphs.  Optional; defaults are reasonable. */
@@ -198,21 +199,28 @@ LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */
 LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
 /* The launch shape of every size class, as the autotuner left it: *nclasses = the number of classes;
- * with `out` (count >= 13 * classes) thirteen int32 per class: width, height, column variant, row
+ * with `out` (count >= 14 * classes) fourteen int32 per class: width, height, column variant, row
  * variant, chunks, worlds, chunk budget in MiB (0: the class is one chunk), rows per row-pass item,
  * 1 if the class runs the cluster-resident step (lenia_set_resident) else 0, that step's launch
  * variant, 1 if its row pass runs on the tensor cores (lenia_set_tc_rows) else 0, the variant of
  * its tensor-core column pass (0: tile groups staged by bulk copies, 1: read after an L2 prefetch,
- * more CTAs an SM; -1: no tensor-core column pass), and the launch variant of its persistent step
- * (lenia_set_persistent; -1: the class does not run it).
+ * more CTAs an SM; -1: no tensor-core column pass), the launch variant of its persistent step
+ * (lenia_set_persistent; -1: the class does not run it), and the lanes its chunks run on
+ * (lenia_set_chunk_lanes).
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
-/* Pins the chunk budget of every size class, in place of the default (0) or the autotuner's
+/* Pins the chunk budget of every size class, in place of the default (64) or the autotuner's
  * choice: a class is split into runs of consecutive worlds of at most `mib` MiB of per-step data each
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */
 LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
+/* Pins the lanes of every size class, in place of the default (2) or the autotuner's choice: the
+ * chunks of a class on the step graph's main branch run on `lanes` (1..4) concurrent graph branches,
+ * chunk c on lane c mod lanes, each lane's chunks one after another, so that the launches of
+ * several L2-sized chunks fill the GPU together.  A class of one chunk is unaffected.  Results do
+ * not depend on it (bit for bit).  Rebuilds the step graphs.  No reference counterpart. */
+LENIA_API int lenia_set_chunk_lanes(LeniaCtx* ctx, int32_t lanes);
 /* Branches of the step graph (FP32, TF32 and BF16X3 paths): size classes of at most `cells` cells a world run on graph
  * branches beside the larger classes -- one after another on one side branch (each = 0), or each on
  * a branch of its own (each = 1) -- so that the small classes' latency-bound launches share the GPU
@@ -333,10 +341,12 @@ LENIA_API int lenia_mlp_predict(LeniaMlp* mlp, const float* x, uint32_t count, f
 /* Event-timed average device time of the dominant launches of one step, in milliseconds:
  * out[0] = column passes, out[1] = row passes, out[2] = whole step.  Runs `steps` steps. */
 LENIA_API int lenia_profile_step(LeniaCtx* ctx, uint32_t steps, float* out3);
-/* The same per size class: *nclasses = the number of classes; with `out` (count >= 4 * classes)
- * four floats per class: width, height, column-pass ms and row-pass ms, each the event-timed
- * average over `steps` steps of that class alone (its launches one after another, every other
- * class idle).  Advances every class by `steps`. */
+/* The same per size class: *nclasses = the number of classes; with `out` (count >= 5 * classes)
+ * five floats per class: width, height, column-pass ms and row-pass ms, each the event-timed
+ * average over `steps` steps of that class alone (its launches one after another, an event around
+ * each, every other class idle), and the ms per step of that class alone as the step graph runs it
+ * (a captured graph of `steps` steps: launches back to back, chunks on their lanes).  Advances every
+ * class by 3 * `steps`. */
 LENIA_API int lenia_profile_classes(LeniaCtx* ctx, uint32_t steps, float* out, size_t count, size_t* nclasses);
 
 #ifdef __cplusplus

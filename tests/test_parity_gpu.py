@@ -527,6 +527,32 @@ def test_two_branch_graph_gives_the_same_bits(path):
         assert np.array_equal(outs[0], o)
 
 
+@pytest.mark.parametrize("path", ["fp32", "bf16x3"])
+def test_chunk_lanes_give_the_same_bits(path):
+    """A class's chunks on 2..4 concurrent graph lanes (each lane's chunks one after another) only
+    reorder independent worlds' launches: every state after 9 steps is bit-identical to one chunk, and
+    to the same chunks one after another.  The lanes sit on the main graph branch, with the small
+    classes on a side branch."""
+    ws = configs.batched(384)
+    worlds = [w for w in ws if w.width in (256, 512, 768)][:30]
+    outs = []
+    for budget, lanes in ((0, 1), (8, 1), (8, 2), (8, 3), (8, 4)):
+        with Sim(worlds, seed=0, path=path) as sim:
+            for i, w in enumerate(worlds):
+                sim.seed_patches(i, i, w.seed.patches)
+            sim.set_branch_split(256 * 256, False)
+            sim.set_chunk_budget(budget)
+            sim.set_chunk_lanes(lanes)
+            sh = sim.shapes()
+            assert all(v["lanes"] == lanes for v in sh.values())
+            if budget:
+                assert sh[(768, 768)]["chunks"] > lanes
+            sim.step(9)
+            outs.append(sim.read_states().copy())
+    for o in outs[1:]:
+        assert np.array_equal(outs[0], o)
+
+
 @pytest.mark.parametrize("variant", [0, 1])
 def test_persistent_step_matches_two_pass_bit_for_bit(variant):
     """The persistent step (one launch a class and step call, items claimed in order with per-world
