@@ -1783,9 +1783,9 @@ int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) 
 // The autotuner's search, on states it may advance.  For every size class, in turn: the cluster-
 // resident and persistent steps against two launches a generation (FP32 path, where they apply), the
 // tensor-core row
-// pass against the FP32 one (TF32 / BF16X3 paths, where it applies), every pair of column and row
-// launch variants, then every chunk budget that gives a different number of chunks, with the chunks
-// one after another or on 2..MAX_LANES concurrent lanes.
+// pass against the FP32 one (TF32 / BF16X3 paths, where it applies), then every pair of column and
+// row launch variants jointly with every chunk budget that gives a different number of chunks, the
+// chunks one after another or on 2..MAX_LANES concurrent lanes.
 // Each candidate is timed as a captured graph of a few steps (time_class_graph), and a class keeps
 // its current choice of a dimension unless another is at least 3% faster, so that timing noise does
 // not flip it.
@@ -1869,16 +1869,11 @@ static int autotune_search(LeniaCtx* ctx) {
             if (t[1] < 0.97 * t[0]) cl.tc_rows = !was;
         }
         {
-            std::vector<Shape> c{shape_of(cl)};
-            for (int vc = 0; vc < 3; vc++)
-                for (int vr = 0; vr < 2; vr++)
-                    if (vc != cl.var_col || vr != cl.var_row)
-                        c.push_back(Shape{vc, vr, cl.var_tc, &cl.chunks, cl.lanes});
-            if ((rc = pick(c, &bi))) return rc;
-            cl.var_col = c[bi].var_col;
-            cl.var_row = c[bi].var_row;
-        }
-        {
+            // launch variants jointly with the chunk budget and lanes: their best pairs differ (on the
+            // batched workload's 1024 x 1024 class the radix-32 column build was fastest in 32 MiB chunks
+            // on four lanes, the paired build in 64 MiB chunks on two).  Every pair of column and row
+            // variants, for every list of chunks (each budget that changes the number of chunks) one
+            // after another and on 2..MAX_LANES lanes; candidate 0 is the current shape.
             std::vector<std::vector<Chunk>> lists{cl.chunks};
             std::vector<size_t> bud{cl.chunk_budget};
             for (size_t b : budgets) {
@@ -1887,17 +1882,19 @@ static int autotune_search(LeniaCtx* ctx) {
                 for (auto& l : lists) seen = seen || l.size() == ch.size();
                 if (!seen) lists.push_back(ch), bud.push_back(b);
             }
-            // each list of chunks one after another and on 2..MAX_LANES concurrent lanes; candidate 0 is
-            // the current choice
             std::vector<Shape> c{Shape{cl.var_col, cl.var_row, cl.var_tc, &lists[0], cl.lanes}};
             std::vector<size_t> which{0};
             for (size_t li = 0; li < lists.size(); li++)
                 for (int ln = 1; ln <= LeniaCtx::MAX_LANES && ln <= (int)lists[li].size(); ln++)
-                    if (!(li == 0 && ln == c[0].lanes)) {
-                        c.push_back(Shape{cl.var_col, cl.var_row, cl.var_tc, &lists[li], ln});
-                        which.push_back(li);
-                    }
+                    for (int vc = 0; vc < 3; vc++)
+                        for (int vr = 0; vr < 2; vr++)
+                            if (!(li == 0 && ln == c[0].lanes && vc == c[0].var_col && vr == c[0].var_row)) {
+                                c.push_back(Shape{vc, vr, cl.var_tc, &lists[li], ln});
+                                which.push_back(li);
+                            }
             if ((rc = pick(c, &bi))) return rc;
+            cl.var_col = c[bi].var_col;
+            cl.var_row = c[bi].var_row;
             cl.chunk_budget = bud[which[bi]];
             cl.lanes = c[bi].lanes;
             cl.chunks = lists[which[bi]];

@@ -46,6 +46,18 @@ FFT_CHD constexpr float c16(int t) {
          : 0.92387953251128674f;
 }
 FFT_CHD constexpr float s16(int t) { return c16((t + 12) & 15); }  // sin(x) = cos(x - pi/2)
+// cos/sin(2*pi*t/32), t = 0..31, from cos(pi*q/16) for q = 0..8 and the quadrant symmetries; the even
+// t are c16(t/2)'s values
+FFT_CHD constexpr float c32q(int q) {
+    return q == 0 ? 1.0f : q == 1 ? 0.98078528040323044913f : q == 2 ? 0.92387953251128675613f
+         : q == 3 ? 0.83146961230254523708f : q == 4 ? 0.70710678118654752440f : q == 5 ? 0.55557023301960222474f
+         : q == 6 ? 0.38268343236508977173f : q == 7 ? 0.19509032201612826785f : 0.0f;
+}
+FFT_CHD constexpr float c32(int t) {
+    return (t & 31) <= 8 ? c32q(t & 31) : (t & 31) <= 16 ? -c32q(16 - (t & 31)) : (t & 31) <= 24 ? -c32q((t & 31) - 16)
+                                                                                                  : c32q(32 - (t & 31));
+}
+FFT_CHD constexpr float s32(int t) { return c32((t + 24) & 31); }
 constexpr float SQRT3_2 = 0.86602540378443865f;
 
 FFT_HD float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
@@ -70,7 +82,8 @@ struct alignas(16) tw2 {
 };
 // Largest radix of a plan, by element (or twiddle) type: 16 for scalar and paired elements alike
 // (paired elements with radix-8 plans, 8 registers of data a thread instead of 16, measured 50%
-// slower at 4096: more stages, spills at 64 registers, bank conflicts of 16-byte elements).
+// slower at 4096: more stages, spills at 64 registers, bank conflicts of 16-byte elements).  A pass
+// may ask for radix-32 plans where they save a stage (make_plan).
 template <class T> FFT_CHD constexpr int max_radix() { return 16; }
 FFT_HD float2 f2(float v) { return make_float2(v, v); }
 FFT_HD float2 f2add(float2 a, float2 b) {
@@ -122,20 +135,25 @@ FFT_HD cpair cmulc(cpair a, tw2 w) { return {f2fma(a.im, w.ii, f2mul(a.re, w.rr)
 FFT_HD cpair cmul(cpair a, float2 w) { return cmul(a, splat(w)); }
 FFT_HD tw2 cmul(tw2 a, tw2 b) { return {f2sub(f2mul(a.rr, b.rr), f2mul(a.ii, b.ii)), f2fma(a.rr, b.ii, f2mul(a.ii, b.rr))}; }
 
-// exp(sign*2*pi*i*j/R) for compile-time R in {2,4,8,16} and j, via the 16-entry table
+// exp(sign*2*pi*i*j/R) for compile-time R in {2,4,8,16,32} and j, via the 16- or 32-entry table
 template <int R, bool INV> FFT_HD float2 wR(int j) {
-    int t = (j * (16 / R)) & 15;
-    return make_float2(c16(t), INV ? s16(t) : -s16(t));
+    if constexpr (R == 32) {
+        const int t = j & 31;
+        return make_float2(c32(t), INV ? s32(t) : -s32(t));
+    } else {
+        const int t = (j * (16 / R)) & 15;
+        return make_float2(c16(t), INV ? s16(t) : -s16(t));
+    }
 }
 
 // z * exp(sign*2*pi*i*j/R) for compile-time j: quarter turns are exact swaps and negations
 // (a general complex multiply by 0 and +-1 would cost four instructions under IEEE rules).
 template <int R, bool INV, class T> FFT_HD T cmul_wR(T z, int j) {
-    const int t = (j * (16 / R)) & 15;
+    const int t = R == 32 ? (j & 31) : 2 * ((j * (16 / R)) & 15);  // in 32nds of a turn
     if (t == 0) return z;
-    if (t == 8) return cneg(z);
-    if (t == 4) return rot90<INV>(z);
-    if (t == 12) return rot90<!INV>(z);
+    if (t == 16) return cneg(z);
+    if (t == 8) return rot90<INV>(z);
+    if (t == 24) return rot90<!INV>(z);
     return cmul(z, wR<R, INV>(j));
 }
 
@@ -224,6 +242,7 @@ template <int R1, int R2, bool INV, class T> FFT_HD void dft_split(T* v) {
 
 template <bool INV> struct Dft<8, INV> { template <class T> FFT_HD static void run(T* v) { dft_split<4, 2, INV>(v); } };
 template <bool INV> struct Dft<16, INV> { template <class T> FFT_HD static void run(T* v) { dft_split<4, 4, INV>(v); } };
+template <bool INV> struct Dft<32, INV> { template <class T> FFT_HD static void run(T* v) { dft_split<8, 4, INV>(v); } };
 
 // ------------------------------------------------------------------ radix plans
 // N = 2^a * 3^b (b <= 1).  Every plan starts and ends with the same "outer" radix -- 16 when the
@@ -231,12 +250,15 @@ template <bool INV> struct Dft<16, INV> { template <class T> FFT_HD static void 
 // remaining factor of two and any further 16s in between: 4096 = 16.16.16, 3072 = 16.3.4.16,
 // 384 = 8.3.2.8, 96 = 4.3.2.4.  Equal first and last radix let two transforms be chained in
 // registers (fft_fused), which every size then does.
-// maxr caps the radix (16: 4096 = 16.16.16; 8: 4096 = 8.8.8.8, 2048 = 8.4.8.8).
+// maxr caps the radix (16: 4096 = 16.16.16; 8: 4096 = 8.8.8.8, 2048 = 8.4.8.8).  With maxr = 32 the
+// radix-32 plan is taken only where it has fewer stages than the radix-16 one (1024 = 32.32 against
+// 16.4.16, 3072 = 32.3.32, 8192 = 32.8.32): one shared-memory round trip fewer per transform, for 32
+// elements a thread in registers.
 struct Plan {
     int len;
     int r[14];
 };
-FFT_CHD constexpr Plan make_plan(int n, int maxr = 16) {
+FFT_CHD constexpr Plan make_plan_capped(int n, int maxr) {
     Plan P = {0, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
     const bool three = n % 3 == 0;
     const int p = three ? n / 3 : n;
@@ -259,6 +281,11 @@ FFT_CHD constexpr Plan make_plan(int n, int maxr = 16) {
     for (int i = 0; i < inner; i++) P.r[P.len++] = maxr;
     P.r[P.len++] = outer;
     return P;
+}
+FFT_CHD constexpr Plan make_plan(int n, int maxr = 16) {
+    return maxr <= 16 ? make_plan_capped(n, maxr)
+         : (make_plan_capped(n, 32).len < make_plan_capped(n, 16).len ? make_plan_capped(n, 32)
+                                                                      : make_plan_capped(n, 16));
 }
 FFT_CHD constexpr int plan_len(int n, int maxr = 16) { return make_plan(n, maxr).len; }
 FFT_CHD constexpr int plan_radix(int n, int i, int maxr = 16) { return make_plan(n, maxr).r[i]; }
@@ -290,9 +317,8 @@ FFT_HD void set_twiddle(float2& d, float2 w) { d = w; }
 FFT_HD void set_twiddle(tw2& d, float2 w) { d = splat(w); }
 // One stage per template instance, so that each stage's L, R and table offset are compile-time
 // constants (a runtime loop over the stages would evaluate the plan in every thread).
-template <int N, class W, int I = 0>
+template <int N, class W, int I = 0, int MR = max_radix<W>()>
 FFT_HD void fill_stage_twiddles(W* stw, const float2* tw, int tid, int nth) {
-    constexpr int MR = max_radix<W>();
     if constexpr (I < plan_len(N, MR)) {
         constexpr int L = plan_L(N, I, MR), R = plan_radix(N, I, MR), off = stage_tw_offset(N, I, MR);
         if constexpr (L > 1) {
@@ -302,7 +328,7 @@ FFT_HD void fill_stage_twiddles(W* stw, const float2* tw, int tid, int nth) {
                 if (R >= 8) set_twiddle(stw[off + L + k], tw[4 * k * step]);
             }
         }
-        fill_stage_twiddles<N, W, I + 1>(stw, tw, tid, nth);
+        fill_stage_twiddles<N, W, I + 1, MR>(stw, tw, tid, nth);
     }
 }
 
@@ -333,6 +359,14 @@ FFT_HD void twiddle_powers(W w1, W w4, W* w) {
         w[12] = cmul(w[8], w[4]);
 #pragma unroll
         for (int m = 13; m < 16; m++) w[m] = cmul(w[12], w[m - 12]);
+    }
+    if (R >= 32) {
+        w[16] = cmul(w[8], w[8]);
+        w[24] = cmul(w[16], w[8]);
+#pragma unroll
+        for (int m = 17; m < 24; m++) w[m] = cmul(w[16], w[m - 16]);
+#pragma unroll
+        for (int m = 25; m < 32; m++) w[m] = cmul(w[24], w[m - 24]);
     }
 }
 
@@ -372,6 +406,11 @@ FFT_HD void stage_store(T* seq, int j, const T* v) {
         T* p = seq + pad(base);
 #pragma unroll
         for (int m = 0; m < R; m++) p[m * STEP] = v[m];
+    } else if constexpr (L == 1 && R % 16 == 0) {
+        // L = 1, R = 32: base = R j is a multiple of 16, so pad(base + m) = pad(base) + m + m / 16
+        T* p = seq + pad(base);
+#pragma unroll
+        for (int m = 0; m < R; m++) p[m + m / 16] = v[m];
     } else {
 #pragma unroll
         for (int m = 0; m < R; m++) seq[pad(base + m * L)] = v[m];

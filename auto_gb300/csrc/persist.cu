@@ -55,7 +55,10 @@ __global__ void __launch_bounds__(NT, MINB)
     constexpr int SEQ = seq_stride(N), NSEQ = row_seqs(N, false) > TC ? row_seqs(N, false) : TC;
     float2* X = reinterpret_cast<float2*>(smem_raw);
     float2* stw = X + NSEQ * SEQ;  // after the column pass's tile sequences and the row pass's packed rows
+    // the row items' stage tables, then the column items' (their plans may differ: CMR)
+    float2* stwc = stw + tw_table_size(N) + 1;
     fill_stage_twiddles<N>(stw, tw, threadIdx.x, NT);
+    fill_stage_twiddles<N, float2, 0, CMR>(stwc, tw, threadIdx.x, NT);
     int* cols_done = ctl + PST_COUNTERS;
     int* rows_done = cols_done + nw;
     const long long per_gen = (long long)nw * (nc + nr), total = per_gen * gens;
@@ -112,7 +115,7 @@ __global__ void __launch_bounds__(NT, MINB)
         if (s_stop) break;
         if (is_col) {
             const ColItem it = cols[(size_t)w * nc + idx];
-            col_item<N, NT, true>(worlds[it.world], it, X, stw);
+            col_item<N, NT, true>(worlds[it.world], it, X, stwc);
         } else {
             const RowItem it = rows[(size_t)w * nr + idx];
             row_item_simple<N, NT, true>(worlds[it.world], it.row0, X, stw);
@@ -143,7 +146,8 @@ constexpr int persist_minb() { return (V == 0 ? 1024 : 512) / persist_nt<N>() < 
 template <int N>
 size_t persist_smem() {
     constexpr int NSEQ = row_seqs(N, false) > TC ? row_seqs(N, false) : TC;
-    return (size_t)NSEQ * seq_stride(N) * sizeof(float2) + stage_table_bytes<N>() + col_khat_bytes<N>();
+    return (size_t)NSEQ * seq_stride(N) * sizeof(float2) + stage_table_bytes<N>() + stage_table_bytes<N, CMR>() +
+           col_khat_bytes<N>();
 }
 
 template <int N, int V>

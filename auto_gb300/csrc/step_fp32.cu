@@ -15,7 +15,7 @@ static size_t col_khat_bytes_of(int H) {
 // the larger of the scalar and paired builds (same sequence bytes; the paired stage tables hold
 // each twiddle twice)
 size_t col_smem_bytes(int H) {
-    const size_t scalar_tables = (lfft::tw_table_size(H) + 1) * sizeof(float2);
+    const size_t scalar_tables = (lfft::tw_table_size(H, CMR) + 1) * sizeof(float2);
     const size_t paired_tables = (lfft::tw_table_size(H, PMR) + 1) * sizeof(lfft::tw2);
     return (size_t)TC * lfft::seq_stride(H) * sizeof(float2) + (scalar_tables > paired_tables ? scalar_tables : paired_tables) +
            col_khat_bytes_of(H);

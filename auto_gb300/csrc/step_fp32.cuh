@@ -53,10 +53,11 @@ __device__ __forceinline__ void static_for(F&& f) {
 // Stages [I, I1) of the transform of S sequences of length N in shared memory (stride
 // seq_stride(N)), in place, by NT threads; stw holds the per-stage twiddle tables
 // (fill_stage_twiddles).  Starts after the caller's barrier; ends with a barrier.
-template <int N, int S, int NT, bool INV, int I, int I1, class T, class W>
+// MR: the plan's radix cap (make_plan); 16 for every pass but the scalar column pass.
+template <int N, int S, int NT, bool INV, int I, int I1, int MR = 16, class T, class W>
 __device__ __forceinline__ void fft_stages(T* buf, const W* stw) {
+    static_assert(MR == 32 || MR == max_radix<T>(), "radix-32 plans are built for scalar elements only");
     if constexpr (I < I1) {
-        constexpr int MR = max_radix<T>();
         constexpr int R = plan_radix(N, I, MR);
         constexpr int L = plan_L(N, I, MR);
         constexpr int NB = N / R;
@@ -82,13 +83,13 @@ __device__ __forceinline__ void fft_stages(T* buf, const W* stw) {
             }
         }
         __syncthreads();
-        fft_stages<N, S, NT, INV, I + 1, I1>(buf, stw);
+        fft_stages<N, S, NT, INV, I + 1, I1, MR>(buf, stw);
     }
 }
 
-template <int N, int S, int NT, bool INV, class T, class W>
+template <int N, int S, int NT, bool INV, int MR = 16, class T, class W>
 __device__ __forceinline__ void fft_seqs(T* buf, const W* stw) {
-    fft_stages<N, S, NT, INV, 0, plan_len(N, max_radix<T>())>(buf, stw);
+    fft_stages<N, S, NT, INV, 0, plan_len(N, MR), MR>(buf, stw);
 }
 
 // Two transforms back to back (A, then B) with work on the values in between.  When the plan's
@@ -106,14 +107,13 @@ struct NoPre {
     __device__ void operator()(int, int) const {}
 };
 
-template <int N, int S, int NT, bool INV_A, bool INV_B, class T, class W, class Mid, class Pre = NoPre>
+template <int N, int S, int NT, bool INV_A, bool INV_B, int MR = 16, class T, class W, class Mid, class Pre = NoPre>
 __device__ __forceinline__ void fft_fused(T* buf, const W* stw, Mid mid, Pre pre = Pre()) {
-    constexpr int MR = max_radix<T>();
     constexpr int LAST = plan_len(N, MR) - 1;
     constexpr int R = plan_radix(N, LAST, MR), L = plan_L(N, LAST, MR), NB = N / R;
     static_assert(L == NB && plan_radix(N, 0, MR) == R, "fusable plans only");
     constexpr int TOT = NB * S, PER = (TOT + NT - 1) / NT, SEQ = seq_stride(N);
-    fft_stages<N, S, NT, INV_A, 0, LAST>(buf, stw);
+    fft_stages<N, S, NT, INV_A, 0, LAST, MR>(buf, stw);
     T v[PER][R];
 #pragma unroll
     for (int p = 0; p < PER; p++) {
@@ -133,21 +133,27 @@ __device__ __forceinline__ void fft_fused(T* buf, const W* stw, Mid mid, Pre pre
         if ((TOT % NT) == 0 || b < TOT) stage_store<N, R, 1>(buf + (b / NB) * SEQ, b % NB, v[p]);
     }
     __syncthreads();
-    fft_stages<N, S, NT, INV_B, 1, plan_len(N, MR)>(buf, stw);
+    fft_stages<N, S, NT, INV_B, 1, plan_len(N, MR), MR>(buf, stw);
 }
 
 // Shared memory of a pass: the sequences, then (float2-aligned) the stage twiddle tables.
-template <int N>
-constexpr size_t stage_table_bytes() { return (size_t)(tw_table_size(N) + 1) * sizeof(float2); }
+template <int N, int MR = 16>
+constexpr size_t stage_table_bytes() { return (size_t)(tw_table_size(N, MR) + 1) * sizeof(float2); }
+
+// The scalar column pass's radix cap: radix-32 plans where they save a stage (1024 = 32.32 against
+// 16.4.16: one shared-memory round trip fewer per transform; 3072, 8192), the radix-16 plan elsewhere.
+// The column item holds its 32 elements a thread in registers between stages; the row pass, which also
+// holds the state values of its rows there, keeps radix 16.
+constexpr int CMR = 32;
 
 // Column pass, fused form: after the stage tables (16-byte aligned), the tile's TC khat columns.
 template <int H>
 FFT_CHD constexpr int khat_cols_stride() { return (H / 2 + 1 + 3) / 4 * 4; }
 template <int H>
-constexpr size_t col_khat_bytes() { return fusable<H>() ? (size_t)TC * khat_cols_stride<H>() * sizeof(float) : 0; }
+constexpr size_t col_khat_bytes() { return fusable<H, CMR>() ? (size_t)TC * khat_cols_stride<H>() * sizeof(float) : 0; }
 template <int H>
 __device__ __forceinline__ float* col_khat_smem(float2* stw) {
-    constexpr int TWS = tw_table_size(H);
+    constexpr int TWS = tw_table_size(H, CMR);
     return reinterpret_cast<float*>(((uintptr_t)(stw + TWS) + 15) & ~(uintptr_t)15);
 }
 
@@ -630,10 +636,10 @@ __device__ __noinline__ void col_item_unchained(float2* X, const float2* stw, co
                                                 const float* kh, int HQ, int W, int t) {
     load_tile<H, NT, CG>(X, src);
     __syncthreads();
-    fft_seqs<H, TC, NT, false>(X, stw);
+    fft_seqs<H, TC, NT, false, CMR>(X, stw);
     multiply_khat<H, NT>(X, X, kh, HQ, W, t);
     __syncthreads();
-    fft_seqs<H, TC, NT, true>(X, stw);
+    fft_seqs<H, TC, NT, true, CMR>(X, stw);
     store_tile<H, NT>(X, dst);
 }
 
@@ -652,14 +658,14 @@ __device__ __forceinline__ void col_item(const DevWorld& wd, const ColItem it, f
     // each) are copied to shared memory while the tile loads.
     constexpr int HQC = khat_cols_stride<H>();
     const float* kh = wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)TC * t) * HQC;
-    if (fusable<H>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
+    if (fusable<H, CMR>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
         float* ksm = col_khat_smem<H>(stw);
         for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
         load_tile<H, NT, CG>(X, src);
         cp_async_wait_all();
         __syncthreads();
-        fft_fused<H, TC, NT, false, true>(X, stw, [&](int s, int j, float2* v) {
-            constexpr int R = plan_radix(H, 0), NB = H / R;
+        fft_fused<H, TC, NT, false, true, CMR>(X, stw, [&](int s, int j, float2* v) {
+            constexpr int R = plan_radix(H, 0, CMR), NB = H / R;
             const float* kc = ksm + s * HQC;
 #pragma unroll
             for (int m = 0; m < R; m++) {
@@ -681,7 +687,7 @@ __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict_
     constexpr int SEQ = seq_stride(H);
     float2* X = reinterpret_cast<float2*>(smem_raw);
     float2* stw = X + TC * SEQ;
-    fill_stage_twiddles<H>(stw, tw, threadIdx.x, NT);
+    fill_stage_twiddles<H, float2, 0, CMR>(stw, tw, threadIdx.x, NT);
     const ColItem it = items[blockIdx.x];
     col_item<H, NT, false>(worlds[it.world], it, X, stw);
 }
@@ -809,11 +815,13 @@ __global__ void __launch_bounds__(NT, MINB) col_pass_pair(const DevWorld* __rest
 // (The column pass keeps one first-stage butterfly per thread at every size: at 768 the balanced count,
 // 128 threads, made it slower, 66 -> 73 us a generation on the batched workload's class.)
 template <int N> constexpr int nt_of() {
-    constexpr int n = 2 * N / plan_radix(N, 0);  // one first-stage butterfly per thread, two sequences
+    constexpr int n = 2 * N / plan_radix(N, 0, CMR);  // one first-stage butterfly per thread, two sequences
     return n < 64 ? 64 : (n > 1024 ? 1024 : n);
 }
-// variant 0: at most 64 registers per thread; variant 1: at most 128
-template <int N, int V> constexpr int minb_of() { return (V == 0 ? 1024 : 512) / nt_of<N>() < 1 ? 1 : (V == 0 ? 1024 : 512) / nt_of<N>(); }
+// variant 0: at most 64 registers per thread (80 for radix-32 plans: the 1024 build spilled 508 B at
+// 64 and needs none at 80); variant 1: at most 128
+template <int N, int V> constexpr int minb_threads() { return V == 0 ? (plan_radix(N, 0, CMR) == 32 ? 768 : 1024) : 512; }
+template <int N, int V> constexpr int minb_of() { return minb_threads<N, V>() / nt_of<N>() < 1 ? 1 : minb_threads<N, V>() / nt_of<N>(); }
 // paired column build: one first-stage butterfly per thread for the one (paired) sequence, at most
 // 128 registers a thread
 template <int N> constexpr int nt_pair_of() {
@@ -826,7 +834,7 @@ template <int N> constexpr int minb_pair_of() { return 512 / nt_pair_of<N>() < 1
 // its first launch and before any stream capture that contains it; a zero-item call does just that.
 template <int H, int NT, int MINB>
 bool col_go(const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
-    const size_t smem = (size_t)TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H>() + col_khat_bytes<H>();
+    const size_t smem = (size_t)TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H, CMR>() + col_khat_bytes<H>();
     static int attr_max = 0;
     if ((int)smem > attr_max) {
         if (cudaFuncSetAttribute(col_pass<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=

@@ -180,10 +180,10 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
  * launches per generation and the persistent step (where they apply), the tensor-core column
  * pass's variants and the
  * tensor-core row pass against the FP32 one (lenia_set_tc_rows, where they apply), then for
- * two-pass classes the pair of column and row
- * launch variants and every chunk budget (worlds per L2-resident run, see lenia_class_shapes) that
- * changes the class's number of chunks, with its chunks one after another or on 2 to 4 concurrent
- * lanes (lenia_set_chunk_lanes); then, for the whole step, the split of small classes onto a
+ * two-pass classes every pair of column and row launch variants jointly with every chunk budget
+ * (worlds per L2-resident run, see lenia_class_shapes) that changes the class's number of chunks,
+ * its chunks one after another or on 2 to 4 concurrent lanes (lenia_set_chunk_lanes); then, for
+ * the whole step, the split of small classes onto a
  * second graph branch (lenia_set_branch_split).
  * The states are saved first and restored afterwards, also when it fails.  Rebuilds the step
  * graphs.  Optional; defaults are reasonable. */

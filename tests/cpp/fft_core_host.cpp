@@ -8,26 +8,27 @@
 
 using namespace lfft;
 
-template <int N, int I, bool INV>
+template <int N, int I, bool INV, int MR = 16>
 static void run_stage(float2* seq, const float2* tw) {
-    if constexpr (I < plan_len(N)) {
-        constexpr int R = plan_radix(N, I);
-        constexpr int L = plan_L(N, I);
+    if constexpr (I < plan_len(N, MR)) {
+        constexpr int R = plan_radix(N, I, MR);
+        constexpr int L = plan_L(N, I, MR);
         std::vector<float2> v((N / R) * R);
-        for (int j = 0; j < N / R; j++) stage_load<N, R, L, INV>(seq, j, &v[j * R], tw + stage_tw_offset(N, I));
+        for (int j = 0; j < N / R; j++) stage_load<N, R, L, INV>(seq, j, &v[j * R], tw + stage_tw_offset(N, I, MR));
         for (int j = 0; j < N / R; j++) stage_store<N, R, L>(seq, j, &v[j * R]);
-        run_stage<N, I + 1, INV>(seq, tw);
+        run_stage<N, I + 1, INV, MR>(seq, tw);
     }
 }
 
-template <int N>
+// MR = 32: the plans a pass that asks for radix 32 gets (radix 32 where it saves a stage)
+template <int N, int MR = 16>
 static int fft_n(int inverse, const float* in, float* out, const float2* tw) {
     std::vector<float2> seq(seq_stride(N));
-    std::vector<float2> stw(tw_table_size(N) + 1);
-    fill_stage_twiddles<N>(stw.data(), tw, 0, 1);
+    std::vector<float2> stw(tw_table_size(N, MR) + 1);
+    fill_stage_twiddles<N, float2, 0, MR>(stw.data(), tw, 0, 1);
     for (int i = 0; i < N; i++) seq[pad(i)] = make_float2(in[2 * i], in[2 * i + 1]);
-    if (inverse) run_stage<N, 0, true>(seq.data(), stw.data());
-    else run_stage<N, 0, false>(seq.data(), stw.data());
+    if (inverse) run_stage<N, 0, true, MR>(seq.data(), stw.data());
+    else run_stage<N, 0, false, MR>(seq.data(), stw.data());
     for (int i = 0; i < N; i++) { out[2 * i] = seq[pad(i)].x; out[2 * i + 1] = seq[pad(i)].y; }
     return 0;
 }
@@ -83,6 +84,15 @@ static const float2* table() {
 extern "C" int fft_host(int n, int inverse, const float* in, float* out) {
     switch (n) {
 #define CASE(N) case N: return fft_n<N>(inverse, in, out, table());
+        FFT_SIZES(CASE)
+#undef CASE
+    }
+    return -1;
+}
+
+extern "C" int fft_host_r32(int n, int inverse, const float* in, float* out) {
+    switch (n) {
+#define CASE(N) case N: return fft_n<N, 32>(inverse, in, out, table());
         FFT_SIZES(CASE)
 #undef CASE
     }

@@ -432,7 +432,7 @@ def test_headless_view_matches_oracle(ref, palette, samples, scale, origin):
 def test_chunked_classes_give_the_same_bits():
     """Splitting size classes into L2-sized runs of worlds only regroups the launches: every world's
     state after 6 steps is bit-identical with one run per class and with runs of a few worlds, and
-    within rounding after the autotuner's choice; the shapes report the chunking."""
+    with the autotuner's shapes a step stays within 1e-5 of FP64; the shapes report the chunking."""
     worlds = configs.batched(64)
     outs = []
     for budget in (0, 8, 1):
@@ -448,13 +448,24 @@ def test_chunked_classes_give_the_same_bits():
             sim.step(6)
             outs.append(sim.read_states().copy())
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+    # the autotuner's shapes: its launch variants may run other radix plans (radix 32, or the paired
+    # radix-16 build), whose rounding differs and compounds over the steps; each step stays within
+    # 1e-5 of FP64
     with Sim(worlds, seed=0) as sim:
         for i, w in enumerate(worlds):
             sim.seed_patches(i, i, w.seed.patches)
         sim.autotune()
-        sim.step(6)
+        sim.step(5)
+        before = [sim.read_state(i) for i in range(len(worlds))]
+        sim.step(1)
         got = sim.read_states()
-    assert np.abs(got - outs[0]).max() < 1e-5  # launch variants may differ in rounding
+    assert np.abs(got - outs[0]).max() < 1e-4
+    off, worst = 0, 0.0
+    for w, s in zip(worlds, before):
+        n = w.channels * w.height * w.width
+        worst = max(worst, float(np.abs(got[off:off + n] - fp64_step(w, s).ravel()).max()))
+        off += n
+    assert worst < 1e-5, worst
 
 
 def test_resident_step_matches_two_pass_and_fp64():
