@@ -78,6 +78,9 @@ def parse(argv=None):
     p.add_argument("--only-side", type=int, default=0,
                    help="keep only the workload's worlds of this side (a size class alone, e.g. for a profile)")
     p.add_argument("--max-worlds", type=int, default=0, help="keep at most this many of the workload's worlds")
+    p.add_argument("--variants", default=None, metavar="COL,ROW",
+                   help="with --profile-window: pin every class's column and row launch variants (lenia_set_variants) "
+                        "after any autotuning, e.g. 1,0")
     p.add_argument("--profile-window", action="store_true",
                    help="set up, autotune and warm up the workload, then run exactly one bench step (one graph "
                         "replay) between cudaProfilerStart and cudaProfilerStop and exit: for ncu "
@@ -470,6 +473,9 @@ def profile_window(args, dist):
         sim.autotune()
     if args.tc_rows:
         sim.set_tc_rows(True)
+    if args.variants:
+        vc, vr = (int(x) for x in args.variants.split(","))
+        sim.set_variants(vc, vr)
     for _ in range(args.warmup):
         sim.step(args.gens)
     sim.wait()
