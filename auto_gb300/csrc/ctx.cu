@@ -855,12 +855,13 @@ int setup_fused(LeniaCtx* ctx) {
             cudaGetLastError();
         }
         // zero-item launches only set each kernel's shared-memory limit, outside any capture
-        for (int v = 0; v < 2; v++) {
-            if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream) ||
-                !launch_row_fp32(cl.W, v, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw,
+        for (int v = 0; v < COL_VARIANTS; v++)
+            if (!launch_col_fp32(cl.H, v, ctx->d_worlds, cl.d_col, 0, ctx->d_tw, ctx->stream))
+                return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
+        for (int v = 0; v < 2; v++)
+            if (!launch_row_fp32(cl.W, v, MODE_STEP, cl.general, ctx->d_worlds, cl.d_row, 0, cl.planes, ctx->d_tw,
                                  ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure launches for %dx%d", cl.W, cl.H);
-        }
         for (int v = 0; v < TC_COL_VARIANTS && cl.ntcg > 0; v++)
             if (!launch_col_tc(ctx->tc, ctx->path, cl.H, v, ctx->d_worlds, cl.d_tcg, 0, ctx->d_tw, ctx->stream))
                 return fail(ctx, LENIA_ECUDA, "cannot configure the tensor-core pass for H=%d", cl.H);
@@ -1765,9 +1766,9 @@ int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* 
 
 int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant) {
     if (!ctx) return LENIA_EINVAL;
-    if (col_variant < -1 || col_variant > 2 || row_variant < -1 || row_variant > 1)
-        return fail(ctx, LENIA_EINVAL, "launch variants are -1..2 (column) and -1..1 (row), got %d and %d", col_variant,
-                    row_variant);
+    if (col_variant < -1 || col_variant >= COL_VARIANTS || row_variant < -1 || row_variant > 1)
+        return fail(ctx, LENIA_EINVAL, "launch variants are -1..%d (column) and -1..1 (row), got %d and %d",
+                    COL_VARIANTS - 1, col_variant, row_variant);
     if (ctx->path == LENIA_PATH_RADIX2) return 0;  // one build per stage: nothing to choose
     for (auto& cl : ctx->classes) {
         if (col_variant >= 0) cl.var_col = col_variant;
@@ -1886,9 +1887,10 @@ static int autotune_search(LeniaCtx* ctx) {
             std::vector<size_t> which{0};
             for (size_t li = 0; li < lists.size(); li++)
                 for (int ln = 1; ln <= LeniaCtx::MAX_LANES && ln <= (int)lists[li].size(); ln++)
-                    for (int vc = 0; vc < 3; vc++)
+                    for (int vc = 0; vc < COL_VARIANTS; vc++)
                         for (int vr = 0; vr < 2; vr++)
-                            if (!(li == 0 && ln == c[0].lanes && vc == c[0].var_col && vr == c[0].var_row)) {
+                            if (!(li == 0 && ln == c[0].lanes && vc == c[0].var_col && vr == c[0].var_row) &&
+                                (vc != 3 || col_has_r16_variant(cl.H))) {
                                 c.push_back(Shape{vc, vr, cl.var_tc, &lists[li], ln});
                                 which.push_back(li);
                             }

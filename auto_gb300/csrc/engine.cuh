@@ -62,6 +62,11 @@ bool launch_row_fp32(int W, int variant, int mode, int general, const DevWorld* 
                      int nitems, int acc_planes, const float2* tw, cudaStream_t s);
 size_t col_smem_bytes(int H);
 size_t row_smem_bytes(int W, int acc_planes);
+// Column-pass launch variants (launch_col_fp32): 0, 1 scalar builds at two register caps, 2 the paired
+// build, 3 the scalar radix-16 build where the scalar plan has radix 32
+constexpr int COL_VARIANTS = 4;
+// whether the scalar column pass of height H has a radix-16 build beside its radix-32 one (variant 3)
+bool col_has_r16_variant(int H);
 int row_item_rows(int W, int general);  // rows per row-pass item: 4, or 2 (general step, W >= 2048)
 int fp32_local_bytes(int row, int n, int variant);  // spill/stack bytes per thread of a pass instantiation
 int max_smem_optin();

@@ -12,10 +12,11 @@ static size_t col_khat_bytes_of(int H) {
     return 0;
 }
 
-// the larger of the scalar and paired builds (same sequence bytes; the paired stage tables hold
-// each twiddle twice)
+// the largest of the scalar builds' (radix-32 and radix-16 plans) and the paired build's (same
+// sequence bytes; the paired stage tables hold each twiddle twice)
 size_t col_smem_bytes(int H) {
-    const size_t scalar_tables = (lfft::tw_table_size(H, CMR) + 1) * sizeof(float2);
+    const int t32 = lfft::tw_table_size(H, CMR), t16 = lfft::tw_table_size(H);
+    const size_t scalar_tables = ((t32 > t16 ? t32 : t16) + 1) * sizeof(float2);
     const size_t paired_tables = (lfft::tw_table_size(H, PMR) + 1) * sizeof(lfft::tw2);
     return (size_t)TC * lfft::seq_stride(H) * sizeof(float2) + (scalar_tables > paired_tables ? scalar_tables : paired_tables) +
            col_khat_bytes_of(H);
@@ -31,6 +32,8 @@ size_t row_smem_bytes(int W, int acc_planes) {
 }
 
 int row_item_rows(int W, int general) { return 2 * row_seqs(W, general != 0); }
+
+bool col_has_r16_variant(int H) { return lfft::plan_radix(H, 0, CMR) == 32; }
 
 int max_smem_optin() {
     int dev = 0, v = 0;

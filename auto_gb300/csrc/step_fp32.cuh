@@ -151,9 +151,9 @@ template <int H>
 FFT_CHD constexpr int khat_cols_stride() { return (H / 2 + 1 + 3) / 4 * 4; }
 template <int H>
 constexpr size_t col_khat_bytes() { return fusable<H, CMR>() ? (size_t)TC * khat_cols_stride<H>() * sizeof(float) : 0; }
-template <int H>
+template <int H, int MR = CMR>
 __device__ __forceinline__ float* col_khat_smem(float2* stw) {
-    constexpr int TWS = tw_table_size(H, CMR);
+    constexpr int TWS = tw_table_size(H, MR);
     return reinterpret_cast<float*>(((uintptr_t)(stw + TWS) + 15) & ~(uintptr_t)15);
 }
 
@@ -631,15 +631,15 @@ __device__ __forceinline__ void store_tile(const float2* X, float2* __restrict__
 // Unchained column item: tile 0 (its column 0 packs the DC and Nyquist columns, paired ky with
 // H - ky in the khat multiply) or a khat array that is not 16-byte aligned.  Not inlined: one item
 // in W/4 takes this path, and as a separate function its registers do not add to the chained path's.
-template <int H, int NT, bool CG = false>
+template <int H, int NT, bool CG = false, int MR = CMR>
 __device__ __noinline__ void col_item_unchained(float2* X, const float2* stw, const float2* src, float2* dst,
                                                 const float* kh, int HQ, int W, int t) {
     load_tile<H, NT, CG>(X, src);
     __syncthreads();
-    fft_seqs<H, TC, NT, false, CMR>(X, stw);
+    fft_seqs<H, TC, NT, false, MR>(X, stw);
     multiply_khat<H, NT>(X, X, kh, HQ, W, t);
     __syncthreads();
-    fft_seqs<H, TC, NT, true, CMR>(X, stw);
+    fft_seqs<H, TC, NT, true, MR>(X, stw);
     store_tile<H, NT>(X, dst);
 }
 
@@ -648,7 +648,7 @@ __device__ __noinline__ void col_item_unchained(float2* X, const float2* stw, co
 // repeating the channel's forward column transform: that keeps every item on the chained path and
 // multiplies the items, which the multichannel world needs more than it needs the saved transforms.
 // CG: the tile loads bypass L1 (the persistent step, where another CTA of the same launch wrote them).
-template <int H, int NT, bool CG>
+template <int H, int NT, bool CG, int MR = CMR>
 __device__ __forceinline__ void col_item(const DevWorld& wd, const ColItem it, float2* X, float2* stw) {
     const int W = wd.W, c = it.chan, t = it.tile, k = it.kernel, HQ = wd.HQ;
     const size_t cplane = (size_t)(W / 2) * H;
@@ -658,14 +658,14 @@ __device__ __forceinline__ void col_item(const DevWorld& wd, const ColItem it, f
     // each) are copied to shared memory while the tile loads.
     constexpr int HQC = khat_cols_stride<H>();
     const float* kh = wd.khat + ((size_t)k * (W / 2 + 1) + (size_t)TC * t) * HQC;
-    if (fusable<H, CMR>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
-        float* ksm = col_khat_smem<H>(stw);
+    if (fusable<H, MR>() && t != 0 && wd.HQ == HQC && ((uintptr_t)kh & 15) == 0) {
+        float* ksm = col_khat_smem<H, MR>(stw);
         for (int e = threadIdx.x; e < TC * HQC / 4; e += NT) cp_async16(ksm + 4 * e, kh + 4 * e);
         load_tile<H, NT, CG>(X, src);
         cp_async_wait_all();
         __syncthreads();
-        fft_fused<H, TC, NT, false, true, CMR>(X, stw, [&](int s, int j, float2* v) {
-            constexpr int R = plan_radix(H, 0, CMR), NB = H / R;
+        fft_fused<H, TC, NT, false, true, MR>(X, stw, [&](int s, int j, float2* v) {
+            constexpr int R = plan_radix(H, 0, MR), NB = H / R;
             const float* kc = ksm + s * HQC;
 #pragma unroll
             for (int m = 0; m < R; m++) {
@@ -676,20 +676,22 @@ __device__ __forceinline__ void col_item(const DevWorld& wd, const ColItem it, f
         store_tile<H, NT>(X, wd.conv + k * cplane + (size_t)t * H * TC);
         return;
     }
-    col_item_unchained<H, NT, CG>(X, stw, src, wd.conv + k * cplane + (size_t)t * H * TC,
+    col_item_unchained<H, NT, CG, MR>(X, stw, src, wd.conv + k * cplane + (size_t)t * H * TC,
                                   wd.khat + (size_t)k * (W / 2 + 1) * HQ, HQ, W, t);
 }
 
-template <int H, int NT, int MINB>
+// MR: the radix cap of the build's plans (CMR; 16 for the radix-16 build of sizes whose CMR plan has
+// radix 32, launch variant 3)
+template <int H, int NT, int MINB, int MR = CMR>
 __global__ void __launch_bounds__(NT, MINB) col_pass(const DevWorld* __restrict__ worlds, const ColItem* __restrict__ items,
                                                 const float2* __restrict__ tw) {
     extern __shared__ float4 smem_raw[];
     constexpr int SEQ = seq_stride(H);
     float2* X = reinterpret_cast<float2*>(smem_raw);
     float2* stw = X + TC * SEQ;
-    fill_stage_twiddles<H, float2, 0, CMR>(stw, tw, threadIdx.x, NT);
+    fill_stage_twiddles<H, float2, 0, MR>(stw, tw, threadIdx.x, NT);
     const ColItem it = items[blockIdx.x];
-    col_item<H, NT, false>(worlds[it.world], it, X, stw);
+    col_item<H, NT, false, MR>(worlds[it.world], it, X, stw);
 }
 
 // ------------------------------------------------------------------ paired column pass
@@ -814,14 +816,21 @@ __global__ void __launch_bounds__(NT, MINB) col_pass_pair(const DevWorld* __rest
 #define LENIA_SIZES_LARGE(X) X(1024) X(1536) X(2048) X(3072) X(4096) X(6144) X(8192)
 // (The column pass keeps one first-stage butterfly per thread at every size: at 768 the balanced count,
 // 128 threads, made it slower, 66 -> 73 us a generation on the batched workload's class.)
-template <int N> constexpr int nt_of() {
-    constexpr int n = 2 * N / plan_radix(N, 0, CMR);  // one first-stage butterfly per thread, two sequences
+template <int N, int MR = CMR> constexpr int nt_of() {
+    constexpr int n = 2 * N / plan_radix(N, 0, MR);  // one first-stage butterfly per thread, two sequences
     return n < 64 ? 64 : (n > 1024 ? 1024 : n);
 }
+// whether the scalar column build's plan has radix 32 (1024, 3072, 8192): those sizes also build the
+// radix-16 plan (launch variant 3)
+template <int N> constexpr bool col_r32() { return plan_radix(N, 0, CMR) == 32; }
 // variant 0: at most 64 registers per thread (80 for radix-32 plans: the 1024 build spilled 508 B at
 // 64 and needs none at 80); variant 1: at most 128
-template <int N, int V> constexpr int minb_threads() { return V == 0 ? (plan_radix(N, 0, CMR) == 32 ? 768 : 1024) : 512; }
-template <int N, int V> constexpr int minb_of() { return minb_threads<N, V>() / nt_of<N>() < 1 ? 1 : minb_threads<N, V>() / nt_of<N>(); }
+template <int N, int V, int MR = CMR> constexpr int minb_threads() {
+    return V == 0 ? (plan_radix(N, 0, MR) == 32 ? 768 : 1024) : 512;
+}
+template <int N, int V, int MR = CMR> constexpr int minb_of() {
+    return minb_threads<N, V, MR>() / nt_of<N, MR>() < 1 ? 1 : minb_threads<N, V, MR>() / nt_of<N, MR>();
+}
 // paired column build: one first-stage butterfly per thread for the one (paired) sequence, at most
 // 128 registers a thread
 template <int N> constexpr int nt_pair_of() {
@@ -832,17 +841,17 @@ template <int N> constexpr int minb_pair_of() { return 512 / nt_pair_of<N>() < 1
 
 // Launch one instantiation.  Dynamic shared memory above 48 KB must be enabled per kernel before
 // its first launch and before any stream capture that contains it; a zero-item call does just that.
-template <int H, int NT, int MINB>
+template <int H, int NT, int MINB, int MR = CMR>
 bool col_go(const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw, cudaStream_t s) {
-    const size_t smem = (size_t)TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H, CMR>() + col_khat_bytes<H>();
+    const size_t smem = (size_t)TC * seq_stride(H) * sizeof(float2) + stage_table_bytes<H, MR>() + col_khat_bytes<H>();
     static int attr_max = 0;
     if ((int)smem > attr_max) {
-        if (cudaFuncSetAttribute(col_pass<H, NT, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        if (cudaFuncSetAttribute(col_pass<H, NT, MINB, MR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
             cudaSuccess)
             return false;
         attr_max = (int)smem;
     }
-    if (nitems > 0) col_pass<H, NT, MINB><<<nitems, NT, smem, s>>>(worlds, items, tw);
+    if (nitems > 0) col_pass<H, NT, MINB, MR><<<nitems, NT, smem, s>>>(worlds, items, tw);
     return true;
 }
 
@@ -889,13 +898,20 @@ bool row_go(int mode, int general, int planes, const DevWorld* worlds, const Row
     return true;
 }
 
-// Column-pass builds: variant 0 and 1 are the scalar build at 64 and 128 registers a thread,
-// variant 2 the paired build.
-#define LENIA_COL_CASE(N)                                                                                   \
-    case N:                                                                                                 \
-        return variant == 2   ? col_go_pair<N, nt_pair_of<N>(), minb_pair_of<N>()>(worlds, items, nitems, tw, s) \
-               : variant == 1 ? col_go<N, nt_of<N>(), minb_of<N, 1>()>(worlds, items, nitems, tw, s)           \
-                              : col_go<N, nt_of<N>(), minb_of<N, 0>()>(worlds, items, nitems, tw, s);
+// Column-pass builds: variant 0 and 1 are the scalar build at 64 (80 with a radix-32 plan) and 128
+// registers a thread, variant 2 the paired build, variant 3 the scalar build with the radix-16 plan at
+// 64 registers where the scalar plan has radix 32 (elsewhere variant 0).
+template <int N>
+bool col_go_variant(int variant, const DevWorld* worlds, const ColItem* items, int nitems, const float2* tw,
+                    cudaStream_t s) {
+    if (variant == 2) return col_go_pair<N, nt_pair_of<N>(), minb_pair_of<N>()>(worlds, items, nitems, tw, s);
+    if (variant == 1) return col_go<N, nt_of<N>(), minb_of<N, 1>()>(worlds, items, nitems, tw, s);
+    if constexpr (col_r32<N>())
+        if (variant == 3) return col_go<N, nt_of<N, 16>(), minb_of<N, 0, 16>(), 16>(worlds, items, nitems, tw, s);
+    return col_go<N, nt_of<N>(), minb_of<N, 0>()>(worlds, items, nitems, tw, s);
+}
+#define LENIA_COL_CASE(N) \
+    case N: return col_go_variant<N>(variant, worlds, items, nitems, tw, s);
 
 // Row-pass builds: variant bit 0 selects the register cap (row_minb); the single-kernel (GEN =
 // false) and general (GEN = true) builds sit in separate translation units, which keeps each
@@ -916,11 +932,16 @@ int local_bytes_of(F* f) {
     cudaFuncAttributes a;
     return cudaFuncGetAttributes(&a, f) == cudaSuccess ? (int)a.localSizeBytes : -1;
 }
-#define LENIA_COL_LOCAL_CASE(N)                                                                 \
-    case N:                                                                                     \
-        return variant == 2   ? local_bytes_of(col_pass_pair<N, nt_pair_of<N>(), minb_pair_of<N>()>) \
-               : variant == 1 ? local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>)              \
-                              : local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>);
+template <int N>
+int col_local_bytes_variant(int variant) {
+    if (variant == 2) return local_bytes_of(col_pass_pair<N, nt_pair_of<N>(), minb_pair_of<N>()>);
+    if (variant == 1) return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 1>()>);
+    if constexpr (col_r32<N>())
+        if (variant == 3) return local_bytes_of(col_pass<N, nt_of<N, 16>(), minb_of<N, 0, 16>(), 16>);
+    return local_bytes_of(col_pass<N, nt_of<N>(), minb_of<N, 0>()>);
+}
+#define LENIA_COL_LOCAL_CASE(N) \
+    case N: return col_local_bytes_variant<N>(variant);
 #define LENIA_ROW_LOCAL_CASE_G(N, G)                                                    \
     case N:                                                                             \
         return (variant & 1) ? local_bytes_of(row_pass<N, row_nt<N, G>(), row_minb<N, 1, G>(), G>) \

@@ -190,10 +190,12 @@ LENIA_API int lenia_world_stats(LeniaCtx* ctx, float* host_out, size_t count);
 LENIA_API int lenia_autotune(LeniaCtx* ctx);
 
 /* Pins the launch variant of every size class, in place of the defaults or the autotuner's
- * choice: column 0 and 1 are the scalar build at 64 and 128 registers a thread, 2 the paired
- * build (both columns of a tile as f32x2 pairs); row 0 and 1 the two register caps; -1 keeps a
- * pass's current choice.  Results do not depend on the variant beyond float rounding.  Rebuilds
- * the step graphs.  No reference counterpart: the reference has one launch shape per pass. */
+ * choice: column 0 and 1 are the scalar build at 64 (80 where its plan has radix 32: columns of 1024,
+ * 3072 and 8192) and 128 registers a thread, 2 the paired build (both columns of a tile as f32x2
+ * pairs), 3 the scalar build with the radix-16 plan at 64 registers (the same as 0 where the scalar
+ * plan has no radix 32); row 0 and 1 the two register caps; -1 keeps a pass's current choice.
+ * Results do not depend on the variant beyond float rounding.  Rebuilds the step graphs.  No
+ * reference counterpart: the reference has one launch shape per pass. */
 LENIA_API int lenia_set_variants(LeniaCtx* ctx, int32_t col_variant, int32_t row_variant);
 /* The size classes and their current launch variants: *nclasses = the number of classes; with
  * `out` (count >= 4 * classes) four int32 per class: width, height, column variant, row variant. */

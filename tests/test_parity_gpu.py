@@ -274,15 +274,16 @@ def test_async_state_copies_match_blocking_ones():
 
 @pytest.mark.parametrize("nk", [1, 2])
 def test_every_launch_variant_on_every_side(nk):
-    """Each pinned pair of launch variants (column: scalar at 64 and 128 registers, paired; row:
-    the two register caps) on every supported side along either axis, one step vs FP64."""
+    """Each pinned pair of launch variants (column: scalar at 64 and 128 registers, paired, scalar
+    with the radix-16 plan; row: the two register caps) on every supported side along either axis,
+    one step vs FP64."""
     kernels = [ag.Kernel(radius=5.0, beta=[1.0, 0.5])] + [ag.Kernel(radius=3.0, mu=0.2, sigma=0.03, weight=0.5)] * (nk - 1)
     worlds = [ag.World(n, 32, kernels, dt=0.1) for n in SIDES] + [ag.World(32, n, kernels, dt=0.1) for n in SIDES[1:]]
     rng = np.random.default_rng(29 + nk)
     states = [rng.random((1, w.height, w.width), dtype=np.float32) for w in worlds]
     want = [fp64_step(w, s) for w, s in zip(worlds, states)]
     with Sim(worlds) as sim:
-        for col in (0, 1, 2):
+        for col in (0, 1, 2, 3):
             for row in (0, 1):
                 sim.set_variants(col, row)
                 assert set(sim.variants().values()) == {(col, row)}
@@ -293,7 +294,7 @@ def test_every_launch_variant_on_every_side(nk):
                     err = float(np.abs(sim.read_state(i) - want[i]).max())
                     assert err < 1e-4, (col, row, w.width, w.height, err)
         with pytest.raises(LeniaError):
-            sim.set_variants(3, 0)
+            sim.set_variants(4, 0)
         with pytest.raises(LeniaError):
             sim.set_variants(0, 2)
 
