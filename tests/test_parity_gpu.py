@@ -561,6 +561,14 @@ def test_chunk_lanes_give_the_same_bits(path):
                 assert sh[(768, 768)]["chunks"] > lanes
             sim.step(9)
             outs.append(sim.read_states().copy())
+            if lanes == 4:
+                with pytest.raises(LeniaError):
+                    sim.set_chunk_lanes(0)
+                with pytest.raises(LeniaError):
+                    sim.set_chunk_lanes(5)
+                # per class: the column and row launches each alone, and the class as the graph runs it
+                prof = sim.profile_classes(2)
+                assert set(prof) == set(sh) and all(c > 0 and r > 0 and g > 0 for c, r, g in prof.values())
     for o in outs[1:]:
         assert np.array_equal(outs[0], o)
 
