@@ -300,9 +300,12 @@ FFT_CHD constexpr bool size_ok(int n) {
 }
 
 // Per-stage twiddle tables.  A stage with L > 1 needs w = exp(-2 pi i k / (L R)) for k < L and,
-// when R >= 8, w^4; they are copied once per CTA from the global table into shared memory.
+// when R >= 8, w^4 (and when R >= 32, w^16); they are copied once per CTA from the global table into
+// shared memory.
 FFT_CHD constexpr int stage_tw_count(int n, int i, int maxr = 16) {
-    return plan_L(n, i, maxr) > 1 ? (plan_radix(n, i, maxr) >= 8 ? 2 : 1) * plan_L(n, i, maxr) : 0;
+    return plan_L(n, i, maxr) > 1
+               ? (plan_radix(n, i, maxr) >= 32 ? 3 : plan_radix(n, i, maxr) >= 8 ? 2 : 1) * plan_L(n, i, maxr)
+               : 0;
 }
 FFT_CHD constexpr int stage_tw_offset(int n, int i, int maxr = 16) {
     int o = 0;
@@ -326,6 +329,7 @@ FFT_HD void fill_stage_twiddles(W* stw, const float2* tw, int tid, int nth) {
             for (int k = tid; k < L; k += nth) {
                 set_twiddle(stw[off + k], tw[k * step]);
                 if (R >= 8) set_twiddle(stw[off + L + k], tw[4 * k * step]);
+                if (R >= 32) set_twiddle(stw[off + 2 * L + k], tw[16 * k * step]);
             }
         }
         fill_stage_twiddles<N, W, I + 1, MR>(stw, tw, tid, nth);
@@ -338,11 +342,11 @@ FFT_HD int pad(int i) { return i + (i >> 4); }
 // 4 interleaved columns fall into different banks
 FFT_CHD constexpr int seq_stride(int n) { return n + n / 16 + 4; }
 
-// Twiddles w^m, m = 1..R-1, of one butterfly from w and (R >= 8) w^4; the other powers are
-// products of at most three factors, so each stays within a few float ulps of the exactly rounded
-// value (checked against numpy by the host test).
+// Twiddles w^m, m = 1..R-1, of one butterfly from w, (R >= 8) w^4 and (R >= 32) w^16; the other
+// powers are products of at most four factors, so each stays within a few float ulps of the exactly
+// rounded value (checked against numpy by the host test).
 template <int R, class W>
-FFT_HD void twiddle_powers(W w1, W w4, W* w) {
+FFT_HD void twiddle_powers(W w1, W w4, W w16, W* w) {
     w[1] = w1;
     if (R >= 3) w[2] = cmul(w[1], w[1]);
     if (R >= 4) w[3] = cmul(w[2], w[1]);
@@ -361,7 +365,7 @@ FFT_HD void twiddle_powers(W w1, W w4, W* w) {
         for (int m = 13; m < 16; m++) w[m] = cmul(w[12], w[m - 12]);
     }
     if (R >= 32) {
-        w[16] = cmul(w[8], w[8]);
+        w[16] = w16;
         w[24] = cmul(w[16], w[8]);
 #pragma unroll
         for (int m = 17; m < 24; m++) w[m] = cmul(w[16], w[m - 16]);
@@ -388,7 +392,7 @@ FFT_HD void stage_load(const T* seq, int j, T* v, const W* stw) {
     }
     if (L > 1) {
         W w[R];
-        twiddle_powers<R>(stw[k], R >= 8 ? stw[L + k] : stw[k], w);
+        twiddle_powers<R>(stw[k], R >= 8 ? stw[L + k] : stw[k], R >= 32 ? stw[2 * L + k] : stw[k], w);
 #pragma unroll
         for (int m = 1; m < R; m++) v[m] = INV ? cmulc(v[m], w[m]) : cmul(v[m], w[m]);
     }
