@@ -72,16 +72,17 @@ struct SizeClass {
     int* d_pctl = nullptr;
 };
 
-// Default chunk budget and lanes: a class of more than 64 MiB of per-step data runs in chunks of at
-// most 64 MiB, two chunks at a time on concurrent lanes.  A chunk keeps its worlds in L2 across its
+// Default chunk budget and lanes: a class of more than 32 MiB of per-step data runs in chunks of at
+// most 32 MiB, four chunks at a time on concurrent lanes.  A chunk keeps its worlds in L2 across its
 // generations (ncu on the 55 worlds of 1024 x 1024 in 32 MiB chunks: DRAM traffic 1.4 GB -> 23 MB per
 // generation), but a launch over a few worlds fills the GPU less, and chunks one after another
 // measured slower than one chunk (1024 x 1024: 2.07e11 cell-updates/s as one chunk, 1.87e11 in 8
-// chunks of 64 MiB, 1.53e11 in 16 of 32 MiB).  On two lanes the chunks' launches fill the GPU
-// together: 2.23e11 in 8 chunks of 64 MiB (768 x 768: 1.55e11 -> 1.79e11).  The autotuner tries
-// other budgets and 1 to 4 lanes per class.
-constexpr size_t DEFAULT_CHUNK_BUDGET = 64ull << 20;
-constexpr int DEFAULT_LANES = 2;
+// chunks of 64 MiB, 1.53e11 in 16 of 32 MiB).  On lanes the chunks' launches fill the GPU together:
+// 1024 x 1024 2.35e11 in 16 chunks of 32 MiB on four lanes (2.22e11 in 8 of 64 MiB on two; 16 MiB
+// on eight, 2.35e11, and 24 MiB on six, 2.32e11, no faster), 768 x 768 1.99e11 (1.93e11).  The
+// autotuner tries other budgets and 1 to 4 lanes per class.
+constexpr size_t DEFAULT_CHUNK_BUDGET = 32ull << 20;
+constexpr int DEFAULT_LANES = 4;
 // Whether a class the persistent step serves starts with it (the autotuner times it against the two
 // launches per generation and keeps the faster).  Off: on the batched workload every class measured
 // slower persistent (1024 x 1024: 1.73e11 cell-updates/s against 1.92e11; 128 x 128: 3.5e10 against

@@ -212,12 +212,12 @@ LENIA_API int lenia_class_variants(const LeniaCtx* ctx, int32_t* out, size_t cou
  * A chunk is a run of the class's worlds that the step graph advances through all of its steps
  * before the next run starts, sized so that its states and spectra stay in L2. */
 LENIA_API int lenia_class_shapes(const LeniaCtx* ctx, int32_t* out, size_t count, size_t* nclasses);
-/* Pins the chunk budget of every size class, in place of the default (64) or the autotuner's
+/* Pins the chunk budget of every size class, in place of the default (32) or the autotuner's
  * choice: a class is split into runs of consecutive worlds of at most `mib` MiB of per-step data each
  * (0: one run per class).  Results do not depend on it (bit for bit); only the L2 traffic does.
  * Rebuilds the step graphs.  No reference counterpart. */
 LENIA_API int lenia_set_chunk_budget(LeniaCtx* ctx, uint32_t mib);
-/* Pins the lanes of every size class, in place of the default (2) or the autotuner's choice: the
+/* Pins the lanes of every size class, in place of the default (4) or the autotuner's choice: the
  * chunks of a class on the step graph's main branch run on `lanes` (1..4) concurrent graph branches,
  * chunk c on lane c mod lanes, each lane's chunks one after another, so that the launches of
  * several L2-sized chunks fill the GPU together.  A class of one chunk is unaffected.  Results do
