@@ -24,7 +24,7 @@ EXPORTS = [
     "lenia_write_state_device", "lenia_read_state_device", "lenia_write_states", "lenia_read_states", "lenia_write_states_async", "lenia_read_states_async", "lenia_step", "lenia_step_timed", "lenia_sync",
     "lenia_tick", "lenia_seed_tiles", "lenia_seed_patches", "lenia_cells_per_step", "lenia_memory_bytes",
     "lenia_read_field_u", "lenia_read_spectrum", "lenia_world_stats", "lenia_autotune", "lenia_set_variants", "lenia_class_variants", "lenia_class_shapes", "lenia_set_chunk_budget", "lenia_set_chunk_lanes", "lenia_set_resident", "lenia_set_persistent", "lenia_set_tc_rows", "lenia_set_tc_variant", "lenia_set_branch_split", "lenia_branch_split", "lenia_profile_step", "lenia_profile_classes",
-    "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_tc_set_wait_limit", "lenia_step_noalloc",
+    "lenia_kernel_spectrum", "lenia_tc_selftest", "lenia_tc_set_wait_limit", "lenia_persist_set_wait_limit", "lenia_step_noalloc",
     "lenia_mlp_create", "lenia_mlp_destroy", "lenia_mlp_param_count", "lenia_mlp_set_params",
     "lenia_mlp_get_params", "lenia_mlp_gradients", "lenia_mlp_train_step", "lenia_mlp_predict",
     "lenia_seed_rule", "lenia_render",
@@ -103,6 +103,7 @@ def _declare(L):
         "lenia_kernel_spectrum": [ctypes.POINTER(LeniaKernel), u32, u32, _c_float_p, sz],
         "lenia_tc_selftest": [i32, i32, i32, _c_float_p, _c_float_p, _c_float_p],
         "lenia_tc_set_wait_limit": [vp, i32],
+        "lenia_persist_set_wait_limit": [vp, i32],
         "lenia_step_noalloc": [vp, u32, u32, vp, ctypes.c_float, ctypes.c_float, ctypes.c_float, u32, vp],
         "lenia_seed_rule": [vp, i32, u32, i32],
         "lenia_render": [vp, i32, i32, ctypes.c_float, ctypes.c_float, ctypes.c_float, u32, u32, u32, i32, vp],

@@ -1146,8 +1146,9 @@ int lenia_create(const LeniaWorldDesc* worlds, int32_t nworlds, int32_t path, Le
         if (packed) ctx->states = ctx->hw[0].state, ctx->states_count = off;
     }
     if ((rc = dalloc(ctx, &ctx->d_stats, 3 * (size_t)nworlds))) return bail(rc);
-    if ((rc = dalloc(ctx, &ctx->d_flags, 1))) return bail(rc);
-    if (cudaMemset(ctx->d_flags, 0, sizeof(int)) != cudaSuccess) {
+    // [0] the device error flag, [1] the persistent step's wait limit + 1 (lenia_persist_set_wait_limit)
+    if ((rc = dalloc(ctx, &ctx->d_flags, 2))) return bail(rc);
+    if (cudaMemset(ctx->d_flags, 0, 2 * sizeof(int)) != cudaSuccess) {
         fail(ctx, LENIA_ECUDA, "flag initialisation failed");
         return bail(LENIA_ECUDA);
     }
@@ -1614,6 +1615,15 @@ int lenia_tc_set_wait_limit(LeniaCtx* ctx, int32_t polls_plus_one) {
     std::string err;
     int rc = tc_set_wait_limit(ctx->tc, polls_plus_one, &err);
     if (rc) return fail(ctx, rc, "%s", err.c_str());
+    return 0;
+}
+
+int lenia_persist_set_wait_limit(LeniaCtx* ctx, int32_t polls_plus_one) {
+    if (!ctx) return LENIA_EINVAL;
+    if (polls_plus_one < 0) return fail(ctx, LENIA_EINVAL, "polls_plus_one must be >= 0");
+    if (!ctx->d_flags) return fail(ctx, LENIA_ESTATE, "the context has no persistent step");
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(ctx->d_flags + 1, &polls_plus_one, sizeof(int), cudaMemcpyHostToDevice));
     return 0;
 }
 

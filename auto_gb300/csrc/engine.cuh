@@ -87,9 +87,10 @@ bool launch_resident(int N, int variant, const DevWorld* worlds, const int* worl
 // Persistent step (persist.cu): one launch advances every world of a square, one-channel, one-kernel
 // Lenia size class of side N through `gens` generations, with the two-pass step's column and row
 // items (cols: nc a world, rows: nr a world, world after world) claimed in order by a grid of
-// resident CTAs.  ctl: persist_ctl_words(nworlds) ints, zeroed before every launch.  err: a device
-// int set to 1 if a wait gave up.  capacity (optional): CTAs the GPU holds at once.  A zero-world
-// call only configures the kernel (outside any stream capture).
+// resident CTAs.  ctl: persist_ctl_words(nworlds) ints, zeroed before every launch.  err: two device
+// ints, [0] set to 1 if a wait gave up, [1] the waits' poll limit + 1 (0: the default; 1: every
+// dependency wait gives up at once, a test hook).  capacity (optional): CTAs the GPU holds at once.
+// A zero-world call only configures the kernel (outside any stream capture).
 // variant: 0 at most 64 registers a thread, 1 at most 128 (as the two-pass step's launch variants).
 constexpr int PERSIST_VARIANTS = 2;
 bool persist_supported(int N);

@@ -26,7 +26,9 @@
 // (L1 is not coherent across SMs); results are bit-identical to the two-pass step.  A producer
 // publishes an item with __syncthreads, a device-scope fence and an atomic increment; a consumer
 // spins (one thread, bounded: 2^22 polls) with acquire loads.  A wait that gives up sets the launch's
-// abort word and the context's error flag, and every CTA then stops claiming items.
+// abort word and the context's error flag, and every CTA then stops claiming items.  A test hook
+// (err[1], lenia_persist_set_wait_limit) lowers the limit, down to every dependency wait giving up
+// at once.
 #include <cuda_runtime.h>
 
 #include "engine.cuh"
@@ -62,6 +64,9 @@ __global__ void __launch_bounds__(NT, MINB)
     int* cols_done = ctl + PST_COUNTERS;
     int* rows_done = cols_done + nw;
     const long long per_gen = (long long)nw * (nc + nr), total = per_gen * gens;
+    // err[1]: the wait limit + 1 (0: the default; 1: every dependency wait gives up at once, met or not)
+    const int lim1 = threadIdx.x == 0 ? err[1] : 0;
+    const uint32_t max_polls = lim1 > 1 ? (uint32_t)(lim1 - 1) : PST_WAIT_POLLS;
     unsigned int* claim = reinterpret_cast<unsigned int*>(ctl + PST_NEXT);
     long long next = 0;
     if (threadIdx.x == 0) next = atomicAdd(claim, 1u);
@@ -97,9 +102,9 @@ __global__ void __launch_bounds__(NT, MINB)
             // wait (bounded) for the items this one depends on
             const int* cnt = is_col ? rows_done + w : cols_done + w;
             const int target = is_col ? g * nr : (g + 1) * nc;
-            int stop = 0;
-            for (uint32_t polls = 0; ld_acquire(cnt) < target; polls++) {
-                if (ld_acquire(ctl + PST_ABORT) || polls >= PST_WAIT_POLLS) {
+            int stop = lim1 == 1 && target > 0;
+            for (uint32_t polls = 0; !stop && ld_acquire(cnt) < target; polls++) {
+                if (ld_acquire(ctl + PST_ABORT) || polls >= max_polls) {
                     stop = 1;
                     break;
                 }

@@ -226,6 +226,11 @@ class Sim:
         lenia_set_persistent)."""
         self._check(self._L.lenia_set_persistent(self._ctx, (2 + variant if variant >= 0 else 1) if on else 0))
 
+    def set_persist_wait_limit(self, polls_plus_one: int):
+        """Test hook: the persistent step's wait limit + 1 (0: the default; 1: every dependency wait
+        gives up at once; see lenia_persist_set_wait_limit)."""
+        self._check(self._L.lenia_persist_set_wait_limit(self._ctx, int(polls_plus_one)))
+
     def set_tc_variant(self, variant: int):
         """Tensor-core column pass variant of every class (see lenia_set_tc_variant)."""
         self._check(self._L.lenia_set_tc_variant(self._ctx, int(variant)))

@@ -295,6 +295,14 @@ LENIA_API int lenia_tc_selftest(int32_t path, int32_t n, int32_t k, const float*
  * surfaces failures as Err(String) rather than panics (crates/auto-core/src/sim.rs:208-219); it has
  * no device-side waits. */
 LENIA_API int lenia_tc_set_wait_limit(LeniaCtx* ctx, int32_t polls_plus_one);
+/* Failure-detection test hook of the persistent step (lenia_set_persistent): its dependency waits
+ * give up after a bounded number of polls (2^22 by default), after which the launch's CTAs stop
+ * claiming items and return, and the context's error flag is raised, reported as LENIA_ECUDA by
+ * lenia_sync / lenia_read_state.  polls_plus_one = 0 keeps the default; n > 1 sets the limit to n - 1
+ * polls; 1 makes every dependency wait give up at once, met or not.  After a give-up the step's
+ * results are invalid: rewrite the states (lenia_write_states) before stepping on.  Takes effect at
+ * the next launch (no graph rebuild).  The reference has no device-side waits. */
+LENIA_API int lenia_persist_set_wait_limit(LeniaCtx* ctx, int32_t polls_plus_one);
 
 /* Steps one world of one channel and one Lenia kernel `steps` times, in place, without allocating
  * device memory.  For callers that cannot call cudaMalloc when they step: an application that

@@ -573,6 +573,38 @@ def test_chunk_lanes_give_the_same_bits(path):
         assert np.array_equal(outs[0], o)
 
 
+def test_persistent_wait_timeout_reports_error_and_leaves_context_usable():
+    """Failure detection of the persistent step, with no GPU fault: the test hook makes every
+    dependency wait give up at once, so the launch's CTAs stop claiming items and return, and
+    lenia_sync reports LENIA_ECUDA.  With the limit restored and the states rewritten (the failed step's
+    spectra are invalid), the same context steps again in agreement with FP64."""
+    ws = configs.batched(384)
+    worlds = [w for w in ws if w.width == 256][:6]
+    with Sim(worlds, seed=0) as sim:
+        for i, w in enumerate(worlds):
+            sim.seed_patches(i, i, w.seed.patches)
+        sim.set_persistent(True)
+        assert all(v["persistent"] >= 0 for v in sim.shapes().values())
+        sim.set_persist_wait_limit(1)
+        sim.step(4)
+        with pytest.raises(LeniaError):
+            sim.wait()
+        with pytest.raises(LeniaError):
+            sim.set_persist_wait_limit(-1)
+        sim.set_persist_wait_limit(0)
+        states = sim.read_states().copy()
+        sim.write_states(states)
+        sim.step(1)
+        got = sim.read_states()
+    off, worst = 0, 0.0
+    for w in worlds:
+        n = w.channels * w.height * w.width
+        s = states[off:off + n].reshape(w.channels, w.height, w.width)
+        worst = max(worst, float(np.abs(got[off:off + n] - fp64_step(w, s).ravel()).max()))
+        off += n
+    assert worst < 1e-5, worst
+
+
 @pytest.mark.parametrize("variant", [0, 1])
 def test_persistent_step_matches_two_pass_bit_for_bit(variant):
     """The persistent step (one launch a class and step call, items claimed in order with per-world
