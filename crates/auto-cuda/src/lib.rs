@@ -6,8 +6,9 @@
 //! for the `state` field, and `tick`.  Failures come back as `Err(String)`, as `Sim::new` returns
 //! them (sim.rs:208-219); nothing panics or aborts across the ABI.
 //!
-//! Not compiled where it was written (no Rust toolchain there); the declarations follow the header
-//! line for line.
+//! Not compiled where it was written (no Rust toolchain there).  It declares the entry points this
+//! wrapper calls, each with the header's signature; the rest of the header can be declared the same
+//! way.
 
 use std::ffi::CStr;
 use std::os::raw::{c_char, c_int, c_void};
@@ -102,6 +103,12 @@ unsafe extern "C" {
     fn lenia_memory_bytes(ctx: *const LeniaCtx, bytes: *mut u64) -> c_int;
     fn lenia_autotune(ctx: *mut LeniaCtx) -> c_int;
     fn lenia_set_variants(ctx: *mut LeniaCtx, col_variant: i32, row_variant: i32) -> c_int;
+    fn lenia_set_chunk_budget(ctx: *mut LeniaCtx, mib: u32) -> c_int;
+    fn lenia_set_chunk_lanes(ctx: *mut LeniaCtx, lanes: i32) -> c_int;
+    fn lenia_set_persistent(ctx: *mut LeniaCtx, mode: i32) -> c_int;
+    fn lenia_step_timed(ctx: *mut LeniaCtx, steps: u32, ms: *mut f32) -> c_int;
+    fn lenia_seed_rule(ctx: *mut LeniaCtx, world: i32, seed: u32, kind: i32) -> c_int;
+    fn lenia_world_stats(ctx: *mut LeniaCtx, host_out: *mut f32, count: usize) -> c_int;
     fn lenia_step_noalloc(state: *mut f32, width: u32, height: u32, khat: *const f32, mu: f32, sigma: f32, dt: f32,
                           steps: u32, stream: *mut c_void) -> c_int;
 }
@@ -220,6 +227,43 @@ impl Sim {
     /// Pin the launch variants of every size class (-1 keeps a pass's current choice).
     pub fn set_variants(&mut self, column: i32, row: i32) -> Result<(), String> {
         ok(self.ctx, unsafe { lenia_set_variants(self.ctx, column, row) })
+    }
+
+    /// Chunks of at most `mib` MiB per size class (0: one per class), run on `lanes` (1..4) concurrent
+    /// graph branches; results do not depend on either.
+    pub fn set_chunks(&mut self, mib: u32, lanes: i32) -> Result<(), String> {
+        ok(self.ctx, unsafe { lenia_set_chunk_budget(self.ctx, mib) })?;
+        ok(self.ctx, unsafe { lenia_set_chunk_lanes(self.ctx, lanes) })
+    }
+
+    /// The persistent step on (`Some(variant)`, or `Some(-1)` for the default variant) or off (`None`).
+    pub fn set_persistent(&mut self, variant: Option<i32>) -> Result<(), String> {
+        let mode = match variant {
+            None => 0,
+            Some(v) if v < 0 => 1,
+            Some(v) => 2 + v,
+        };
+        ok(self.ctx, unsafe { lenia_set_persistent(self.ctx, mode) })
+    }
+
+    /// `step` then `wait`, returning the device time of those steps in milliseconds.
+    pub fn step_timed(&mut self, steps: u32) -> Result<f32, String> {
+        let mut ms = 0f32;
+        ok(self.ctx, unsafe { lenia_step_timed(self.ctx, steps, &mut ms) })?;
+        Ok(ms)
+    }
+
+    /// SmoothLife discs (kind 1) or MNCA blocks (kind 2), the reference's seed passes, on the device.
+    pub fn seed_rule(&mut self, world: usize, seed: u32, kind: i32) -> Result<(), String> {
+        ok(self.ctx, unsafe { lenia_seed_rule(self.ctx, world as i32, seed, kind) })
+    }
+
+    /// Per world: mass and toroidal centroid (x, y).
+    pub fn world_stats(&mut self) -> Result<Vec<[f32; 3]>, String> {
+        let n = self.cells.len();
+        let mut v = vec![0f32; 3 * n];
+        ok(self.ctx, unsafe { lenia_world_stats(self.ctx, v.as_mut_ptr(), v.len()) })?;
+        Ok(v.chunks(3).map(|c| [c[0], c[1], c[2]]).collect())
     }
 
     /// `Sim::tick`.
